@@ -1,0 +1,188 @@
+/*
+ * kmc_gb300.h -- C-ABI of the GB300 lattice-kMC step engine (libkmcgb300.so).
+ *
+ * The engine replaces the compiled step loop of kmos's local_smart and lat_int
+ * backends: the f2py extension module ``kmc_model`` with submodules base, lattice and
+ * proclist, built by kmos/utils/__init__.py:406-521 and imported by
+ * kmos/run/__init__.py:86-114 (mhoffman/kmos; paths relative to that project).  Every
+ * entry point returns an int status (KMC_OK or an error below) where the Fortran code
+ * would ``stop`` the whole process.  No torch types cross this boundary: plain
+ * pointers, sizes and host buffers.
+ *
+ * Two levels:
+ *   - kmc_* on a kmc_handle: one trajectory, the plain drop-in behind the f2py module
+ *     interface (one model per handle; handles are independent and re-entrant).
+ *   - kmc_pool_*: a device arena holding many resident trajectories of possibly
+ *     different models and lattice sizes, run together by one persistent kernel
+ *     (batching) and admitted / released while others run (serving).
+ *
+ * Model programs are int32 arrays produced by kmos_gb300.program.compile_model; their
+ * layout is documented there and checked here (magic 0x4B4D4331, version 1).
+ */
+#ifndef KMC_GB300_H
+#define KMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define KMC_API __attribute__((visibility("default")))
+#else
+#define KMC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define KMC_OK 0
+#define KMC_ERR_ARG 1       /* bad argument (proc/site/size out of range, bad handle) */
+#define KMC_ERR_SPECIES 2   /* replace_species found another species (base.mpy:1205-1228) */
+#define KMC_ERR_DEADLOCK 3  /* no process available (base.mpy:1293-1311) */
+#define KMC_ERR_TABLE 4     /* avail_sites inconsistency (del of an absent entry) */
+#define KMC_ERR_PROGRAM 5   /* malformed model program */
+#define KMC_ERR_NOMEM 6     /* device arena full (serving admission refuses) */
+#define KMC_ERR_CUDA 7      /* a CUDA call failed; kmc_last_error() has the text */
+#define KMC_ERR_CANCELLED 8 /* the host cancelled a running batch */
+#define KMC_ERR_NODEVICE 9  /* no CUDA device visible */
+
+/* random-number streams */
+#define KMC_RNG_GFORTRAN 0  /* gfortran RANDOM_NUMBER stream after RANDOM_SEED(PUT=seed words):
+                               reproduces the reference's own trajectories */
+#define KMC_RNG_PHILOX 1    /* Philox4x32-10 keyed by (seed, trajectory id): counter based,
+                               independent of batching and placement */
+
+typedef struct kmc_handle kmc_handle;
+typedef struct kmc_pool kmc_pool;
+
+/* Text of the last error on this thread (static storage). */
+KMC_API const char *kmc_last_error(void);
+/* Library version string. */
+KMC_API const char *kmc_version(void);
+
+/* ------------------------------------------------------------------------------
+ * One trajectory (plain drop-in)
+ * ------------------------------------------------------------------------------ */
+
+/* proclist.init(input_system_size, system_name, layer, seed_in, no_banner)
+ * (proclist_generic_subroutines.mpy:166-230) -> allocate_system (lattice.mpy:212-317,
+ * base.mpy:648-744) + initialize_state (proclist_generic_subroutines.mpy:236-304).
+ * dims: system size per axis (unused axes 1).  layer: layer id whose sites get their
+ * default species.  rng_kind: KMC_RNG_*.  traj_id: Philox key word (ignored for
+ * KMC_RNG_GFORTRAN).  The initial state is built on the device. */
+KMC_API int kmc_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer,
+               int32_t seed, int32_t rng_kind, uint32_t traj_id, kmc_handle **out);
+/* lattice.deallocate_system (lattice.mpy) */
+KMC_API int kmc_destroy(kmc_handle *h);
+
+/* base.set_rate_const(proc, rate) (base.mpy:581-601); proc is 1-based. */
+KMC_API int kmc_set_rate_const(kmc_handle *h, int32_t proc, double rate);
+/* base.update_accum_rate (base.mpy:603-623) */
+KMC_API int kmc_update_accum_rate(kmc_handle *h);
+/* base.update_integ_rate (base.mpy:626-645) */
+KMC_API int kmc_update_integ_rate(kmc_handle *h);
+
+/* proclist.do_kmc_steps(n) (proclist_generic_subroutines.mpy:1-44) */
+KMC_API int kmc_do_steps(kmc_handle *h, int64_t n);
+/* do_kmc_steps(n) that also records the (proc, site) of every step into out[2n]
+ * (a host buffer); used to check step-by-step parity. */
+KMC_API int kmc_trace_steps(kmc_handle *h, int64_t n, int32_t *out);
+/* proclist.get_next_kmc_step (proclist_generic_subroutines.mpy:85-110) */
+KMC_API int kmc_get_next_step(kmc_handle *h, int32_t *proc, int32_t *site);
+/* proclist.run_proc_nr(proc, site) (generated proclist.f90 / kmos/io/__init__.py:305-465,
+ * 1732-1764); proc 1-based, site 1-based. */
+KMC_API int kmc_run_proc_nr(kmc_handle *h, int32_t proc, int32_t site);
+/* proclist.touchup_<layer>_<site>(site) / touchup_cell(cell) (kmos/io/__init__.py:
+ * 2411-2443, 1766-1791); site is the 1-based site index of the site (local_smart) or
+ * of any site of the cell (lat_int). */
+KMC_API int kmc_touchup(kmc_handle *h, int32_t site);
+/* base.get_species(site) (base.mpy:1164-1184) */
+KMC_API int kmc_get_species(kmc_handle *h, int32_t site, int32_t *species);
+/* base.replace_species(site, old, new) (base.mpy:1187-1231) */
+KMC_API int kmc_replace_species(kmc_handle *h, int32_t site, int32_t old_species, int32_t new_species);
+
+/* base.get_kmc_time / set_kmc_time / get_kmc_time_step / get_kmc_step (base.mpy:854-1072) */
+KMC_API int kmc_get_kmc_time(kmc_handle *h, double *t);
+KMC_API int kmc_set_kmc_time(kmc_handle *h, double t);
+KMC_API int kmc_get_kmc_time_step(kmc_handle *h, double *dt);
+KMC_API int kmc_get_kmc_step(kmc_handle *h, int64_t *step);
+/* base.get_volume, nr_of_proc */
+KMC_API int kmc_get_volume(kmc_handle *h, int32_t *volume);
+KMC_API int kmc_get_nr_of_proc(kmc_handle *h, int32_t *nproc);
+/* Whole P-vectors: base.get_procstat(i), get_integ_rate(i), get_rate(i),
+ * get_accum_rate(i), get_nrofsites(i) for i = 1..P, copied into host arrays. */
+KMC_API int kmc_get_procstat(kmc_handle *h, int64_t *out);
+KMC_API int kmc_get_integ_rates(kmc_handle *h, double *out);
+KMC_API int kmc_get_rates(kmc_handle *h, double *out);
+KMC_API int kmc_get_accum_rates(kmc_handle *h, double *out);
+KMC_API int kmc_get_nr_of_sites(kmc_handle *h, int32_t *out);
+/* base.get_avail_site(proc, idx, sw) (avail_sites(proc, idx, sw), base.mpy) */
+KMC_API int kmc_get_avail_site(kmc_handle *h, int32_t proc, int32_t idx, int32_t sw, int32_t *out);
+/* The whole lattice (V species ids) and both book-keeping tables in the engine's
+ * per-process layout: as1[p][i] = avail_sites(p+1, i, 1), as2[p][s] = avail_sites(p+1, s, 2)
+ * for i, s = 0..V (index 0 unused); buffers of V and P*(V+1) int32. */
+KMC_API int kmc_get_lattice(kmc_handle *h, int32_t *out);
+KMC_API int kmc_get_tables(kmc_handle *h, int32_t *as1, int32_t *as2);
+/* proclist.get_occupation (proclist_generic_subroutines.mpy:113-158): out is
+ * [nspecies][spuck] doubles. */
+KMC_API int kmc_get_occupation(kmc_handle *h, double *out);
+
+/* ------------------------------------------------------------------------------
+ * Many resident trajectories (batching and serving)
+ * ------------------------------------------------------------------------------ */
+
+/* A pool owns one device arena of arena_bytes and room for max_slots trajectories. */
+KMC_API int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_pool **out);
+KMC_API int kmc_pool_destroy(kmc_pool *pool);
+/* Registers a model program; returns its id. */
+KMC_API int kmc_pool_add_model(kmc_pool *pool, const int32_t *program, int32_t program_len, int32_t *model_id);
+/* Device bytes one trajectory of this model and size needs (for admission control). */
+KMC_API int kmc_pool_slot_bytes(kmc_pool *pool, int32_t model_id, const int32_t dims[3], size_t *bytes);
+/* Free bytes left in the arena (largest contiguous block in *largest). */
+KMC_API int kmc_pool_free_bytes(kmc_pool *pool, size_t *total, size_t *largest);
+/* Admits one trajectory: allocates its state in the arena and queues its device-side
+ * initialisation (initialize_state + rates + update_accum_rate) on the pool stream.
+ * rates: P doubles.  Returns KMC_ERR_NOMEM when the arena has no room. */
+KMC_API int kmc_pool_admit(kmc_pool *pool, int32_t model_id, const int32_t dims[3], int32_t layer,
+                   int32_t seed, int32_t rng_kind, uint32_t traj_id, const double *rates,
+                   int32_t *slot);
+/* Admits n trajectories at once (one initialisation launch); slots receives n ids. */
+KMC_API int kmc_pool_admit_many(kmc_pool *pool, int32_t n, const int32_t *model_ids, const int32_t *dims3,
+                        int32_t layer, const int32_t *seeds, int32_t rng_kind, const uint32_t *traj_ids,
+                        const double *rates, const int32_t *rate_offsets, int32_t *slots);
+/* Frees a trajectory's arena block. */
+KMC_API int kmc_pool_release(kmc_pool *pool, int32_t slot);
+/* Runs steps[i] kMC steps on slots[i] for i < n in one persistent launch (asynchronous
+ * on the pool stream; kmc_pool_sync waits and returns the first error status). */
+KMC_API int kmc_pool_run(kmc_pool *pool, const int32_t *slots, const int64_t *steps, int32_t n);
+/* Like kmc_pool_run with one step count for every listed slot, replayed from a CUDA
+ * graph captured on first use for this (slots, steps) list. */
+KMC_API int kmc_pool_run_graph(kmc_pool *pool, const int32_t *slots, int64_t steps, int32_t n);
+KMC_API int kmc_pool_sync(kmc_pool *pool);
+/* Sets the cancel flag a running batch polls; the batch ends with KMC_ERR_CANCELLED in
+ * the slots it did not finish. */
+KMC_API int kmc_pool_cancel(kmc_pool *pool);
+/* Per-slot results: status, kmc_time, kmc_step, procstat (P), integ_rates (P),
+ * nr_of_sites (P), occupation counts ([nspecies][spuck] int64). */
+KMC_API int kmc_pool_get_status(kmc_pool *pool, int32_t slot, int32_t *status);
+KMC_API int kmc_pool_get_clock(kmc_pool *pool, int32_t slot, double *kmc_time, int64_t *kmc_step);
+KMC_API int kmc_pool_get_procstat(kmc_pool *pool, int32_t slot, int64_t *out);
+KMC_API int kmc_pool_get_integ_rates(kmc_pool *pool, int32_t slot, double *out);
+KMC_API int kmc_pool_get_nr_of_sites(kmc_pool *pool, int32_t slot, int32_t *out);
+KMC_API int kmc_pool_get_lattice(kmc_pool *pool, int32_t slot, int32_t *out);
+KMC_API int kmc_pool_get_tables(kmc_pool *pool, int32_t slot, int32_t *as1, int32_t *as2);
+/* Occupation counts of many slots at once, reduced on the device: out[i] holds the
+ * [nspecies][spuck] counts of slots[i] (int64), with stride `stride` int64 per slot. */
+KMC_API int kmc_pool_occupation_counts(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride, int64_t *out);
+/* Launch configuration used by kmc_pool_run: warps per block (1..32, 0 = automatic). */
+KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
+/* Device time (ms, CUDA events on the pool stream) of the last kmc_pool_run launch. */
+KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
+/* Kernel launches issued by this pool since creation. */
+KMC_API int kmc_pool_launch_count(kmc_pool *pool, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KMC_GB300_H */

@@ -1,0 +1,1291 @@
+// kmc_engine.cu -- GB300 (sm_103a) lattice-kMC step engine behind the C-ABI of
+// include/kmc_gb300.h.
+//
+// Kernels
+//   kmc_run_kernel     persistent; one warp owns one trajectory at a time and runs its
+//                      kMC steps (do_kmc_steps, proclist_generic_subroutines.mpy:1-44).
+//                      Warps pull trajectories from a work counter, so thousands of
+//                      uneven trajectories share one launch.  Per step:
+//                        * three FP64 draws (gfortran xoshiro256** or Philox),
+//                        * accum_rates prefix sum in the reference's serial order
+//                          (base.mpy:603-623), recomputed only from the first process
+//                          whose nr_of_sites changed (bit-identical to a full recompute),
+//                        * kmc_time += -log(r)/accum(P) (base.mpy:1123-1161),
+//                        * integ_rates update, one process per lane (base.mpy:626-645),
+//                        * the bisection of interval_search_real (base.mpy:1234-1338)
+//                          as two warp ballots: proc = min(first i with accum(i) > v,
+//                          first i with accum(i) == accum(P)),
+//                        * site = avail_sites(proc, min(n, int(1 + r*n)), 1),
+//                        * run_proc_nr: the op program of that process.
+//                      FP64 adds and multiplies use explicit _rn intrinsics (and the file
+//                      is built with -fmad=false) so nothing is contracted into an FMA.
+//   kmc_init_kernel    device-side initialize_state (proclist_generic_subroutines.mpy:
+//                      236-304): default species, then every touch-up in parallel
+//                      (fresh touch-ups only append at their own site), then a
+//                      per-process ballot compaction that lists sites in ascending
+//                      order -- the order the reference's serial touch-up loop appends.
+//   kmc_command_kernel single-warp commands on one trajectory: run_proc_nr, touchup,
+//                      get_next_kmc_step, update_accum_rate, update_integ_rate,
+//                      replace_species.
+//   kmc_occupation_kernel  per-slot species counts per site index (get_occupation).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/kmc_gb300.h"
+#include "kmc_device.cuh"
+
+using namespace kmc;
+
+#define KMC_MAXK 16
+
+// --------------------------------------------------------------------- run kernel
+struct RunArgs {
+  SlotDev *slots;
+  const ModelDev *models;
+  const int32_t *list;
+  const int64_t *steps;
+  int32_t n;
+  int32_t *counter;
+  int32_t *trace;                 // (proc, site) per step of a single-slot run, or null
+  const volatile int32_t *cancel; // host-mapped cancel flag, or null
+};
+
+template <int NP>
+struct WarpSmem {
+  double rates[NP * 32];
+  double accum[NP * 32];
+  int32_t ns[NP * 32];
+};
+
+template <int NP>
+__global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw)[wib];
+
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(a.counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= a.n) break;
+    const int slot = a.list[item];
+    const int64_t nsteps = a.steps[item];
+    SlotDev &S = a.slots[slot];
+    if (S.status != ST_OK) continue;
+    const ModelDev M = a.models[S.model];
+    const int P = M.P;
+    const int stride = S.V + 1;
+
+    View v;
+    v.lat = S.lat;
+    v.as1 = S.as1;
+    v.as2 = S.as2;
+    v.ns = sm.ns;
+    v.prog = M.prog;
+    v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
+    v.stride = stride;
+    v.backend = M.backend;
+    v.P = P;
+    v.off_groups = M.off_groups;
+    v.collect = false;
+
+    double ig[NP];
+    int64_t ps[NP];
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+      const int i = lane + 32 * j;
+      if (i < P) {
+        sm.rates[i] = S.rates[i];
+        sm.accum[i] = S.accum[i];
+        sm.ns[i] = S.nsites[i];
+        ig[j] = S.integ[i];
+        ps[j] = S.procstat[i];
+      } else {
+        ig[j] = 0.0;
+        ps[j] = 0;
+      }
+    }
+    double t = S.kmc_time, dt = S.kmc_time_step;
+    int64_t kstep = S.kmc_step;
+    uint64_t rng[4] = {S.rng[0], S.rng[1], S.rng[2], S.rng[3]};
+    const int rng_kind = S.rng_kind;
+    const uint32_t seed = S.seed, traj = S.traj;
+    int from = S.accum_from;
+    int status = ST_OK;
+    __syncwarp();
+
+    for (int64_t k = 0; k < nsteps; k++) {
+      if (a.cancel && (k & 1023) == 0 && *a.cancel) { status = ST_CANCELLED; break; }
+      double ran_time, ran_proc, ran_site;
+      draw3(rng_kind, rng, seed, traj, ran_time, ran_proc, ran_site);
+
+      // update_accum_rate from the first stale entry (entries before it are unchanged
+      // sums of unchanged terms, so the result equals a full recompute bit for bit)
+      if (lane == 0 && from < P) {
+        double acc = from > 0 ? sm.accum[from - 1] : 0.0;
+        for (int i = from; i < P; i++) {
+          const double term = __dmul_rn((double)sm.ns[i], sm.rates[i]);
+          acc = (i == 0) ? term : __dadd_rn(acc, term);
+          sm.accum[i] = acc;
+        }
+      }
+      from = P;
+      __syncwarp();
+      const double total = sm.accum[P - 1];
+      if (!(total > 0.0)) { status = ST_DEADLOCK; break; }
+
+      // update_clocks
+      dt = __ddiv_rn(-log(ran_time), total);
+      t = __dadd_rn(t, dt);
+      kstep += 1;
+
+      // update_integ_rate: integ(i) = integ(i) + n(i)*r(i)*dt
+#pragma unroll
+      for (int j = 0; j < NP; j++) {
+        const int i = lane + 32 * j;
+        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(__dmul_rn((double)sm.ns[i], sm.rates[i]), dt));
+      }
+
+      // determine_procsite
+      const double val = __dmul_rn(ran_proc, total);
+      int proc = -1;
+#pragma unroll
+      for (int j = 0; j < NP; j++) {
+        const int i = lane + 32 * j;
+        const bool pred = (i < P) && (sm.accum[i] > val || sm.accum[i] == total);
+        const unsigned b = __ballot_sync(0xffffffffu, pred);
+        if (proc < 0 && b) proc = 32 * j + __ffs(b) - 1;
+      }
+      const int n = sm.ns[proc];
+      if (n <= 0) { status = ST_DEADLOCK; break; }
+      int idx = (int)__dadd_rn(1.0, __dmul_rn(ran_site, (double)n));
+      if (idx > n) idx = n;
+
+#pragma unroll
+      for (int j = 0; j < NP; j++)
+        if (proc == lane + 32 * j) ps[j] += 1;  // increment_procstat
+
+      int err = ST_OK;
+      if (lane == 0) {
+        const int site = v.as1[(size_t)proc * stride + idx];
+        if (a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
+        int bx, by, bz, bn;
+        v.g.coords(site, bx, by, bz, bn);
+        v.minp = P;
+        v.err = ST_OK;
+        run_stream(v, M.prog[M.off_proc + proc], bx, by, bz);
+        err = v.err;
+        from = v.minp;
+      }
+      from = __shfl_sync(0xffffffffu, from, 0);
+      err = __shfl_sync(0xffffffffu, err, 0);
+      __syncwarp();
+      if (err) { status = err; break; }
+    }
+
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+      const int i = lane + 32 * j;
+      if (i < P) {
+        S.integ[i] = ig[j];
+        S.procstat[i] = ps[j];
+        S.nsites[i] = sm.ns[i];
+        S.accum[i] = sm.accum[i];
+      }
+    }
+    if (lane == 0) {
+      S.kmc_time = t;
+      S.kmc_time_step = dt;
+      S.kmc_step = kstep;
+      S.rng[0] = rng[0]; S.rng[1] = rng[1]; S.rng[2] = rng[2]; S.rng[3] = rng[3];
+      S.accum_from = from;
+      S.status = status;
+    }
+    __syncwarp();
+  }
+}
+
+// -------------------------------------------------------------------- init kernel
+struct InitArgs {
+  SlotDev *slots;
+  const ModelDev *models;
+  const SlotDev *staged;    // slot descriptors to install
+  const int32_t *list;      // slot ids
+  const double *rates;      // concatenated rate vectors
+  const int32_t *rate_off;  // per item offset into rates
+  int32_t n;
+};
+
+__global__ void __launch_bounds__(256) kmc_init_kernel(InitArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (item >= a.n) return;
+  const int slot = a.list[item];
+  SlotDev &S = a.slots[slot];
+  const SlotDev st = a.staged[item];
+  const ModelDev M = a.models[st.model];
+  const int P = M.P, V = st.V, stride = V + 1;
+  const int32_t *site_layer = M.prog + M.off_site_layer;
+  const int32_t *site_def = M.prog + M.off_site_default;
+
+  // default species on the chosen layer, null species elsewhere
+  for (int s = lane; s < V; s += 32) {
+    const int n = s % M.spuck;
+    st.lat[s] = (int8_t)(site_layer[n] == st.layer ? site_def[n] : M.null_species);
+  }
+  for (int i = lane; i < P; i += 32) {
+    st.rates[i] = a.rates[a.rate_off[item] + i];
+    st.integ[i] = 0.0;
+    st.procstat[i] = 0;
+    st.nsites[i] = 0;
+  }
+  __syncwarp();
+
+  // every touch-up in collect mode: flag (p, site) in as2
+  View v;
+  v.lat = st.lat; v.as1 = st.as1; v.as2 = st.as2; v.ns = st.nsites; v.prog = M.prog;
+  v.g.X = st.X; v.g.Y = st.Y; v.g.Z = st.Z; v.g.spuck = M.spuck;
+  v.stride = stride; v.backend = M.backend; v.P = P; v.off_groups = M.off_groups;
+  v.collect = true; v.err = ST_OK; v.minp = P;
+  const int ncells = st.X * st.Y * st.Z;
+  for (int c = lane; c < ncells; c += 32) {
+    const int x = c % st.X, y = (c / st.X) % st.Y, z = c / (st.X * st.Y);
+    if (M.backend == 1) {
+      run_stream(v, M.prog[M.off_touch], x, y, z);
+    } else {
+      for (int n = 0; n < M.spuck; n++)
+        if (site_layer[n] == st.layer) run_stream(v, M.prog[M.off_touch + n], x, y, z);
+    }
+  }
+  const unsigned bad = __ballot_sync(0xffffffffu, v.err != ST_OK);
+  __syncwarp();
+
+  // compaction: as1[p] lists the flagged sites in ascending order
+  const unsigned lt = (1u << lane) - 1u;
+  for (int p = 0; p < P; p++) {
+    int32_t *a1 = st.as1 + (size_t)p * stride;
+    int32_t *a2 = st.as2 + (size_t)p * stride;
+    int base = 0;
+    for (int s0 = 1; s0 <= V; s0 += 32) {
+      const int s = s0 + lane;
+      const bool f = (s <= V) && a2[s] != 0;
+      const unsigned b = __ballot_sync(0xffffffffu, f);
+      if (f) {
+        const int pos = base + __popc(b & lt) + 1;
+        a1[pos] = s;
+        a2[s] = pos;
+      }
+      base += __popc(b);
+    }
+    if (lane == 0) st.nsites[p] = base;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    // update_accum_rate, as kmos.run.KMC_Model.reset does after set_rate_constants
+    double acc = 0.0;
+    for (int i = 0; i < P; i++) {
+      const double term = __dmul_rn((double)st.nsites[i], st.rates[i]);
+      acc = (i == 0) ? term : __dadd_rn(acc, term);
+      st.accum[i] = acc;
+    }
+    SlotDev d = st;
+    d.status = bad ? ST_PROGRAM : ST_OK;
+    d.accum_from = P;
+    d.kmc_time = 0.0;
+    d.kmc_time_step = 0.0;
+    d.kmc_step = 0;
+    if (st.rng_kind == RNG_GFORTRAN) {
+      gfortran_seed(d.rng, (int32_t)st.seed);
+    } else {
+      d.rng[0] = 0; d.rng[1] = d.rng[2] = d.rng[3] = 0;
+    }
+    S = d;
+  }
+}
+
+// ----------------------------------------------------------------- command kernel
+enum Cmd { CMD_RUN_PROC = 1, CMD_TOUCHUP = 2, CMD_GET_NEXT = 3, CMD_ACCUM = 4, CMD_INTEG = 5, CMD_REPLACE = 6 };
+
+struct CmdArgs {
+  SlotDev *slots;
+  const ModelDev *models;
+  int32_t slot, cmd, a0, a1, a2;
+  int32_t *out;  // [status, proc, site]
+};
+
+__device__ void full_accum(SlotDev &S, int P) {
+  double acc = 0.0;
+  for (int i = 0; i < P; i++) {
+    const double term = __dmul_rn((double)S.nsites[i], S.rates[i]);
+    acc = (i == 0) ? term : __dadd_rn(acc, term);
+    S.accum[i] = acc;
+  }
+  S.accum_from = P;
+}
+
+__global__ void kmc_command_kernel(CmdArgs a) {
+  if (threadIdx.x != 0) return;
+  SlotDev &S = a.slots[a.slot];
+  const ModelDev M = a.models[S.model];
+  const int P = M.P;
+  View v;
+  v.lat = S.lat; v.as1 = S.as1; v.as2 = S.as2; v.ns = S.nsites; v.prog = M.prog;
+  v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
+  v.stride = S.V + 1; v.backend = M.backend; v.P = P; v.off_groups = M.off_groups;
+  v.collect = false; v.err = ST_OK; v.minp = S.accum_from;
+  int status = ST_OK, proc = 0, site = 0;
+  switch (a.cmd) {
+    case CMD_RUN_PROC: {
+      const int p = a.a0, s = a.a1;
+      S.procstat[p - 1] += 1;
+      int bx, by, bz, bn;
+      v.g.coords(s, bx, by, bz, bn);
+      run_stream(v, M.prog[M.off_proc + p - 1], bx, by, bz);
+      status = v.err;
+      S.accum_from = v.minp;
+      break;
+    }
+    case CMD_TOUCHUP: {
+      int bx, by, bz, bn;
+      v.g.coords(a.a0, bx, by, bz, bn);
+      run_stream(v, M.prog[M.off_touch + (M.backend == 1 ? 0 : bn - 1)], bx, by, bz);
+      status = v.err;
+      S.accum_from = v.minp;
+      break;
+    }
+    case CMD_GET_NEXT: {
+      // get_next_kmc_step: the time draw picks the site; no clock update
+      double rt, rp, rs;
+      draw3(S.rng_kind, S.rng, S.seed, S.traj, rt, rp, rs);
+      full_accum(S, P);
+      const double total = S.accum[P - 1];
+      if (!(total > 0.0)) { status = ST_DEADLOCK; break; }
+      const double val = __dmul_rn(rp, total);
+      proc = 0;
+      while (proc < P && !(S.accum[proc] > val || S.accum[proc] == total)) proc++;
+      const int n = S.nsites[proc];
+      if (n <= 0) { status = ST_DEADLOCK; break; }
+      int idx = (int)__dadd_rn(1.0, __dmul_rn(rt, (double)n));
+      if (idx > n) idx = n;
+      site = S.as1[(size_t)proc * (S.V + 1) + idx];
+      proc += 1;
+      break;
+    }
+    case CMD_ACCUM:
+      full_accum(S, P);
+      break;
+    case CMD_INTEG:
+      for (int i = 0; i < P; i++)
+        S.integ[i] = __dadd_rn(S.integ[i], __dmul_rn(__dmul_rn((double)S.nsites[i], S.rates[i]), S.kmc_time_step));
+      break;
+    case CMD_REPLACE: {
+      const int s = a.a0;
+      if (S.lat[s - 1] != a.a1) status = ST_SPECIES;
+      else S.lat[s - 1] = (int8_t)a.a2;
+      break;
+    }
+    default:
+      status = ST_ARG;
+  }
+  a.out[0] = status;
+  a.out[1] = proc;
+  a.out[2] = site;
+}
+
+// -------------------------------------------------------------- occupation kernel
+__global__ void kmc_occupation_kernel(const SlotDev *slots, const ModelDev *models, const int32_t *list,
+                                      int32_t n, int32_t stride, unsigned long long *out) {
+  __shared__ unsigned int hist[32 * 32];
+  const int item = blockIdx.x;
+  if (item >= n) return;
+  const SlotDev &S = slots[list[item]];
+  const ModelDev M = models[S.model];
+  const int ns = M.nspecies, sp = M.spuck;
+  for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < S.V; s += blockDim.x) {
+    const int spc = S.lat[s];
+    if (spc >= 0 && spc < ns && spc < 32) atomicAdd(&hist[spc * 32 + (s % sp)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ns * sp; i += blockDim.x)
+    out[(size_t)item * stride + i] = hist[(i / sp) * 32 + (i % sp)];
+}
+
+// ================================================================== host side
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(KMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct ModelHost {
+  std::vector<int32_t> prog;
+  int32_t *d_prog = nullptr;
+  ModelDev dev{};
+};
+
+struct SlotHost {
+  bool used = false;
+  size_t off = 0, bytes = 0;
+  SlotDev dev{};
+};
+
+struct GraphKey {
+  int64_t steps;
+  std::vector<int32_t> slots;
+  bool operator==(const GraphKey &o) const { return steps == o.steps && slots == o.slots; }
+};
+struct GraphKeyHash {
+  size_t operator()(const GraphKey &k) const {
+    size_t h = std::hash<int64_t>()(k.steps);
+    for (int32_t s : k.slots) h = h * 1000003u ^ (size_t)s;
+    return h;
+  }
+};
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int32_t *d_list = nullptr;
+  int64_t *d_steps = nullptr;
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct kmc_pool {
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t stream = nullptr;
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  std::map<size_t, size_t> free_blocks;  // offset -> size
+  std::vector<SlotHost> slots;
+  SlotDev *d_slots = nullptr;
+  std::vector<ModelHost> models;
+  ModelDev *d_models = nullptr;
+  int max_models = 256;
+  int32_t *d_list = nullptr;
+  int64_t *d_steps = nullptr;
+  int32_t *d_counter = nullptr;
+  int32_t *d_cmd_out = nullptr;
+  int32_t *h_cancel = nullptr;   // host-mapped
+  int32_t *d_cancel = nullptr;
+  // admission staging
+  int32_t *d_adm_list = nullptr;
+  SlotDev *d_adm_staged = nullptr;
+  double *d_adm_rates = nullptr;
+  int32_t *d_adm_roff = nullptr;
+  size_t adm_rates_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false;
+  int64_t launches = 0;
+  int warps_per_block = 4;
+  int blocks_per_sm = 0;  // 0 = occupancy maximum
+  std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> graphs;
+  std::mutex mu;
+};
+
+struct kmc_handle {
+  kmc_pool *pool = nullptr;
+  int slot = -1;
+  int model = -1;
+  int P = 0, V = 0, spuck = 1, nspecies = 0;
+  int32_t *d_trace = nullptr;
+  int64_t trace_cap = 0;
+};
+
+namespace {
+
+int alloc_block(kmc_pool *p, size_t bytes, size_t *off) {
+  bytes = align_up(bytes, 256);
+  for (auto it = p->free_blocks.begin(); it != p->free_blocks.end(); ++it) {
+    if (it->second >= bytes) {
+      *off = it->first;
+      const size_t rest = it->second - bytes;
+      const size_t noff = it->first + bytes;
+      p->free_blocks.erase(it);
+      if (rest) p->free_blocks[noff] = rest;
+      return KMC_OK;
+    }
+  }
+  return fail(KMC_ERR_NOMEM, "device arena has no free block of the requested size");
+}
+
+void free_block(kmc_pool *p, size_t off, size_t bytes) {
+  bytes = align_up(bytes, 256);
+  auto it = p->free_blocks.emplace(off, bytes).first;
+  auto next = std::next(it);
+  if (next != p->free_blocks.end() && it->first + it->second == next->first) {
+    it->second += next->second;
+    p->free_blocks.erase(next);
+  }
+  if (it != p->free_blocks.begin()) {
+    auto prev = std::prev(it);
+    if (prev->first + prev->second == it->first) {
+      prev->second += it->second;
+      p->free_blocks.erase(it);
+    }
+  }
+}
+
+// Byte layout of one slot block.
+struct Layout {
+  size_t lat, as1, as2, rates, integ, accum, nsites, procstat, total;
+};
+
+Layout slot_layout(int P, int V) {
+  Layout L;
+  size_t o = 0;
+  L.lat = o; o = align_up(o + (size_t)V, 16);
+  L.as1 = o; o = align_up(o + (size_t)P * (V + 1) * 4, 16);
+  L.as2 = o; o = align_up(o + (size_t)P * (V + 1) * 4, 16);
+  L.rates = o; o += (size_t)P * 8;
+  L.integ = o; o += (size_t)P * 8;
+  L.accum = o; o += (size_t)P * 8;
+  L.procstat = o; o += (size_t)P * 8;
+  L.nsites = o; o = align_up(o + (size_t)P * 4, 16);
+  L.total = o;
+  return L;
+}
+
+int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
+  if (!prog || len < 20) return fail(KMC_ERR_PROGRAM, "program too short");
+  if ((uint32_t)prog[0] != 0x4B4D4331u || prog[1] != 1) return fail(KMC_ERR_PROGRAM, "bad program magic/version");
+  m->backend = prog[2]; m->P = prog[3]; m->nspecies = prog[4]; m->null_species = prog[5];
+  m->spuck = prog[6]; m->ngroups = prog[8];
+  m->off_proc = prog[10]; m->off_touch = prog[11]; m->off_groups = prog[12];
+  m->off_site_layer = prog[13]; m->off_site_default = prog[14]; m->len = len;
+  if (prog[15] != len) return fail(KMC_ERR_PROGRAM, "program length mismatch");
+  if (m->P < 1 || m->P > 256) return fail(KMC_ERR_PROGRAM, "process count must be in 1..256");
+  if (m->spuck < 1 || m->spuck > 32) return fail(KMC_ERR_PROGRAM, "sites per unit cell must be in 1..32");
+  if (m->nspecies < 1 || m->nspecies > 30) return fail(KMC_ERR_PROGRAM, "species count must be in 1..30");
+  if (m->backend != 0 && m->backend != 1) return fail(KMC_ERR_PROGRAM, "unknown backend");
+  const int nt = m->backend == 1 ? 1 : m->spuck;
+  for (int i = 0; i <= m->P; i++)
+    if (prog[m->off_proc + i] <= 0 || prog[m->off_proc + i] > len) return fail(KMC_ERR_PROGRAM, "bad op offset");
+  for (int i = 0; i <= nt; i++)
+    if (prog[m->off_touch + i] <= 0 || prog[m->off_touch + i] > len) return fail(KMC_ERR_PROGRAM, "bad touch-up offset");
+  // walk every op stream: known ops, in-range processes/groups/sites/species, and an
+  // OP_END before the end of the program
+  auto coord_ok = [&](int32_t w) { const int n = (int)((uint32_t)w >> 24); return n >= 1 && n <= m->spuck; };
+  auto species_ok = [&](int32_t s) { return s >= -1 && s <= m->nspecies; };
+  auto walk = [&](int pos) -> bool {
+    while (pos < len) {
+      const uint32_t h = (uint32_t)prog[pos];
+      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+      switch (op) {
+        case OP_END: return true;
+        case OP_REPLACE:
+          if (pos + 3 >= len || !coord_ok(prog[pos + 1]) || !species_ok(prog[pos + 3])) return false;
+          pos += 4; break;
+        case OP_GDEL:
+          if (pos + 1 >= len || arg < 1 || arg > m->P || !coord_ok(prog[pos + 1])) return false;
+          pos += 2; break;
+        case OP_ADD:
+          if (pos + 1 + 2 * cnt >= len || arg < 1 || arg > m->P || !coord_ok(prog[pos + 1])) return false;
+          for (int c = 0; c < cnt; c++) if (!coord_ok(prog[pos + 2 + 2 * c])) return false;
+          pos += 2 + 2 * cnt; break;
+        case OP_LI_DEL: case OP_LI_ADD:
+          if (pos + 1 >= len || arg >= m->ngroups || !coord_ok(prog[pos + 1])) return false;
+          pos += 2; break;
+        case OP_STRIP:
+          if (pos + 1 >= len || !coord_ok(prog[pos + 1])) return false;
+          pos += 2; break;
+        default: return false;
+      }
+    }
+    return false;
+  };
+  for (int i = 0; i < m->P; i++)
+    if (!walk(prog[m->off_proc + i])) return fail(KMC_ERR_PROGRAM, "malformed op stream of process " + std::to_string(i + 1));
+  for (int i = 0; i < nt; i++)
+    if (!walk(prog[m->off_touch + i])) return fail(KMC_ERR_PROGRAM, "malformed touch-up stream");
+  if (m->off_site_layer < 0 || m->off_site_layer + m->spuck > len || m->off_site_default < 0 ||
+      m->off_site_default + m->spuck > len)
+    return fail(KMC_ERR_PROGRAM, "bad site tables");
+  for (int n = 0; n < m->spuck; n++)
+    if (!species_ok(prog[m->off_site_default + n])) return fail(KMC_ERR_PROGRAM, "bad default species");
+  m->max_k = 0;
+  for (int g = 0; g < m->ngroups; g++) {
+    const int off = prog[m->off_groups + g];
+    if (off <= 0 || off + 2 > len) return fail(KMC_ERR_PROGRAM, "bad group offset");
+    const int M = prog[off], K = prog[off + 1];
+    if (K > KMC_MAXK) return fail(KMC_ERR_PROGRAM, "lateral-interaction group tests more than 16 sites");
+    if (off + 2 + K + M * (1 + K) > len) return fail(KMC_ERR_PROGRAM, "group record overruns program");
+    for (int k = 0; k < K; k++)
+      if (!coord_ok(prog[off + 2 + k])) return fail(KMC_ERR_PROGRAM, "bad group coordinate");
+    for (int mm = 0; mm < M; mm++) {
+      const int pid = prog[off + 2 + K + mm * (1 + K)];
+      if (pid < 1 || pid > m->P) return fail(KMC_ERR_PROGRAM, "bad group member");
+    }
+    m->max_k = std::max(m->max_k, K);
+  }
+  return KMC_OK;
+}
+
+int launch_run(kmc_pool *p, const int32_t *d_list, const int64_t *d_steps, int n, int32_t *d_trace) {
+  RunArgs a;
+  a.slots = p->d_slots;
+  a.models = p->d_models;
+  a.list = d_list;
+  a.steps = d_steps;
+  a.n = n;
+  a.counter = p->d_counter;
+  a.trace = d_trace;
+  a.cancel = p->d_cancel;
+  int maxP = 0;
+  for (auto &m : p->models) maxP = std::max(maxP, m.dev.P);
+  const int wpb = p->warps_per_block;
+  const int threads = 32 * wpb;
+  CK(cudaMemsetAsync(p->d_counter, 0, sizeof(int32_t), p->stream));
+  int bps = p->blocks_per_sm;
+  auto go = [&](auto kern, size_t smem_per_warp) -> int {
+    const size_t smem = smem_per_warp * wpb;  // at most 8 x 5 KB: below the 48 KB default
+    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, smem));
+    if (bps <= 0) bps = 1;
+    int blocks = std::min((n + wpb - 1) / wpb, p->num_sms * bps);
+    if (blocks < 1) blocks = 1;
+    kern<<<blocks, threads, smem, p->stream>>>(a);
+    CK(cudaGetLastError());
+    return KMC_OK;
+  };
+  int rc;
+  if (maxP <= 32) rc = go(kmc_run_kernel<1>, sizeof(WarpSmem<1>));
+  else if (maxP <= 64) rc = go(kmc_run_kernel<2>, sizeof(WarpSmem<2>));
+  else if (maxP <= 128) rc = go(kmc_run_kernel<4>, sizeof(WarpSmem<4>));
+  else rc = go(kmc_run_kernel<8>, sizeof(WarpSmem<8>));
+  if (rc == KMC_OK) p->launches++;
+  return rc;
+}
+
+int read_slot(kmc_pool *p, int slot, SlotDev *out) {
+  CK(cudaStreamSynchronize(p->stream));
+  CK(cudaMemcpy(out, p->d_slots + slot, sizeof(SlotDev), cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
+int check_slot(kmc_pool *p, int slot) {
+  if (!p || slot < 0 || slot >= (int)p->slots.size() || !p->slots[slot].used) return fail(KMC_ERR_ARG, "bad slot");
+  return KMC_OK;
+}
+
+int run_command(kmc_pool *p, int slot, int cmd, int a0, int a1, int a2, int32_t *proc, int32_t *site) {
+  CmdArgs c;
+  c.slots = p->d_slots; c.models = p->d_models; c.slot = slot; c.cmd = cmd;
+  c.a0 = a0; c.a1 = a1; c.a2 = a2; c.out = p->d_cmd_out;
+  kmc_command_kernel<<<1, 32, 0, p->stream>>>(c);
+  CK(cudaGetLastError());
+  p->launches++;
+  int32_t out[3];
+  CK(cudaMemcpyAsync(out, p->d_cmd_out, sizeof(out), cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  if (proc) *proc = out[1];
+  if (site) *site = out[2];
+  if (out[0]) return fail(out[0], "command failed with status " + std::to_string(out[0]));
+  return KMC_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C-ABI
+extern "C" {
+
+const char *kmc_last_error(void) { return g_err.c_str(); }
+const char *kmc_version(void) { return "kmc_gb300 1.0 (sm_103a)"; }
+
+int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_pool **out) {
+  if (!out || max_slots < 1) return fail(KMC_ERR_ARG, "bad arguments");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(KMC_ERR_NODEVICE, "no CUDA device");
+  if (device < 0 || device >= ndev) return fail(KMC_ERR_ARG, "bad device");
+  CK(cudaSetDevice(device));
+  kmc_pool *p = new kmc_pool();
+  p->device = device;
+  CK(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  arena_bytes = align_up(std::max<size_t>(arena_bytes, 256), 256);
+  CK(cudaMalloc(&p->arena, arena_bytes));
+  p->arena_bytes = arena_bytes;
+  p->free_blocks[0] = arena_bytes;
+  p->slots.resize(max_slots);
+  CK(cudaMalloc(&p->d_slots, sizeof(SlotDev) * max_slots));
+  CK(cudaMemset(p->d_slots, 0, sizeof(SlotDev) * max_slots));
+  CK(cudaMalloc(&p->d_models, sizeof(ModelDev) * p->max_models));
+  CK(cudaMalloc(&p->d_list, sizeof(int32_t) * max_slots));
+  CK(cudaMalloc(&p->d_steps, sizeof(int64_t) * max_slots));
+  CK(cudaMalloc(&p->d_counter, sizeof(int32_t)));
+  CK(cudaMalloc(&p->d_cmd_out, sizeof(int32_t) * 4));
+  CK(cudaHostAlloc(&p->h_cancel, sizeof(int32_t), cudaHostAllocMapped));
+  *p->h_cancel = 0;
+  CK(cudaHostGetDevicePointer(&p->d_cancel, p->h_cancel, 0));
+  CK(cudaMalloc(&p->d_adm_list, sizeof(int32_t) * max_slots));
+  CK(cudaMalloc(&p->d_adm_staged, sizeof(SlotDev) * max_slots));
+  CK(cudaMalloc(&p->d_adm_roff, sizeof(int32_t) * max_slots));
+  CK(cudaEventCreate(&p->ev0));
+  CK(cudaEventCreate(&p->ev1));
+  *out = p;
+  return KMC_OK;
+}
+
+int kmc_pool_destroy(kmc_pool *p) {
+  if (!p) return KMC_OK;
+  cudaSetDevice(p->device);
+  cudaStreamSynchronize(p->stream);
+  for (auto &kv : p->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    cudaFree(kv.second.d_list);
+    cudaFree(kv.second.d_steps);
+  }
+  for (auto &m : p->models) cudaFree(m.d_prog);
+  cudaFree(p->arena); cudaFree(p->d_slots); cudaFree(p->d_models); cudaFree(p->d_list);
+  cudaFree(p->d_steps); cudaFree(p->d_counter); cudaFree(p->d_cmd_out); cudaFreeHost(p->h_cancel);
+  cudaFree(p->d_adm_list); cudaFree(p->d_adm_staged); cudaFree(p->d_adm_rates); cudaFree(p->d_adm_roff);
+  cudaEventDestroy(p->ev0); cudaEventDestroy(p->ev1);
+  cudaStreamDestroy(p->stream);
+  delete p;
+  return KMC_OK;
+}
+
+int kmc_pool_add_model(kmc_pool *p, const int32_t *program, int32_t len, int32_t *model_id) {
+  if (!p || !model_id) return fail(KMC_ERR_ARG, "bad arguments");
+  if ((int)p->models.size() >= p->max_models) return fail(KMC_ERR_ARG, "too many models");
+  ModelHost m;
+  int rc = validate_program(program, len, &m.dev);
+  if (rc) return rc;
+  m.prog.assign(program, program + len);
+  CK(cudaSetDevice(p->device));
+  CK(cudaMalloc(&m.d_prog, sizeof(int32_t) * len));
+  CK(cudaMemcpy(m.d_prog, program, sizeof(int32_t) * len, cudaMemcpyHostToDevice));
+  m.dev.prog = m.d_prog;
+  const int id = (int)p->models.size();
+  CK(cudaMemcpy(p->d_models + id, &m.dev, sizeof(ModelDev), cudaMemcpyHostToDevice));
+  p->models.push_back(std::move(m));
+  *model_id = id;
+  return KMC_OK;
+}
+
+int kmc_pool_slot_bytes(kmc_pool *p, int32_t model_id, const int32_t dims[3], size_t *bytes) {
+  if (!p || model_id < 0 || model_id >= (int)p->models.size() || !dims || !bytes) return fail(KMC_ERR_ARG, "bad arguments");
+  const int V = dims[0] * dims[1] * dims[2] * p->models[model_id].dev.spuck;
+  *bytes = align_up(slot_layout(p->models[model_id].dev.P, V).total, 256);
+  return KMC_OK;
+}
+
+int kmc_pool_free_bytes(kmc_pool *p, size_t *total, size_t *largest) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  size_t t = 0, l = 0;
+  for (auto &kv : p->free_blocks) { t += kv.second; l = std::max(l, kv.second); }
+  if (total) *total = t;
+  if (largest) *largest = l;
+  return KMC_OK;
+}
+
+int kmc_pool_admit_many(kmc_pool *p, int32_t n, const int32_t *model_ids, const int32_t *dims3, int32_t layer,
+                        const int32_t *seeds, int32_t rng_kind, const uint32_t *traj_ids, const double *rates,
+                        const int32_t *rate_offsets, int32_t *slots_out) {
+  if (!p || n < 1 || !model_ids || !dims3 || !seeds || !rates || !rate_offsets || !slots_out)
+    return fail(KMC_ERR_ARG, "bad arguments");
+  if (rng_kind != RNG_GFORTRAN && rng_kind != RNG_PHILOX) return fail(KMC_ERR_ARG, "bad rng kind");
+  std::lock_guard<std::mutex> lock(p->mu);
+  CK(cudaSetDevice(p->device));
+  std::vector<int32_t> got;
+  std::vector<SlotDev> staged;
+  size_t nrates = 0;
+  for (int i = 0; i < n; i++) {
+    const int mid = model_ids[i];
+    if (mid < 0 || mid >= (int)p->models.size()) return fail(KMC_ERR_ARG, "bad model id");
+    nrates = std::max(nrates, (size_t)rate_offsets[i] + p->models[mid].dev.P);
+  }
+  int rc = KMC_OK;
+  for (int i = 0; i < n && rc == KMC_OK; i++) {
+    const ModelDev &m = p->models[model_ids[i]].dev;
+    const int X = dims3[3 * i], Y = dims3[3 * i + 1], Z = dims3[3 * i + 2];
+    if (X < 1 || Y < 1 || Z < 1 || (int64_t)X * Y * Z * m.spuck > (1 << 28)) { rc = fail(KMC_ERR_ARG, "bad system size"); break; }
+    const int V = X * Y * Z * m.spuck;
+    int slot = -1;
+    for (int s = 0; s < (int)p->slots.size(); s++)
+      if (!p->slots[s].used) { slot = s; break; }
+    if (slot < 0) { rc = fail(KMC_ERR_NOMEM, "no free trajectory slot"); break; }
+    const Layout L = slot_layout(m.P, V);
+    size_t off;
+    rc = alloc_block(p, L.total, &off);
+    if (rc) break;
+    char *base = p->arena + off;
+    SlotDev d{};
+    d.lat = (int8_t *)(base + L.lat);
+    d.as1 = (int32_t *)(base + L.as1);
+    d.as2 = (int32_t *)(base + L.as2);
+    d.rates = (double *)(base + L.rates);
+    d.integ = (double *)(base + L.integ);
+    d.accum = (double *)(base + L.accum);
+    d.nsites = (int32_t *)(base + L.nsites);
+    d.procstat = (int64_t *)(base + L.procstat);
+    d.X = X; d.Y = Y; d.Z = Z; d.V = V;
+    d.model = model_ids[i]; d.P = m.P; d.layer = layer; d.status = ST_OK;
+    d.rng_kind = rng_kind; d.seed = (uint32_t)seeds[i]; d.traj = traj_ids ? traj_ids[i] : (uint32_t)i;
+    p->slots[slot].used = true;
+    p->slots[slot].off = off;
+    p->slots[slot].bytes = L.total;
+    p->slots[slot].dev = d;
+    // tables start at zero
+    CK(cudaMemsetAsync(base + L.as1, 0, L.rates - L.as1, p->stream));
+    got.push_back(slot);
+    staged.push_back(d);
+  }
+  if (rc) {
+    for (int s : got) { free_block(p, p->slots[s].off, p->slots[s].bytes); p->slots[s].used = false; }
+    return rc;
+  }
+  if (nrates > p->adm_rates_cap) {
+    cudaFree(p->d_adm_rates);
+    CK(cudaMalloc(&p->d_adm_rates, sizeof(double) * nrates));
+    p->adm_rates_cap = nrates;
+  }
+  CK(cudaMemcpyAsync(p->d_adm_list, got.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_adm_staged, staged.data(), sizeof(SlotDev) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_adm_rates, rates, sizeof(double) * nrates, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_adm_roff, rate_offsets, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  InitArgs a;
+  a.slots = p->d_slots; a.models = p->d_models; a.staged = p->d_adm_staged; a.list = p->d_adm_list;
+  a.rates = p->d_adm_rates; a.rate_off = p->d_adm_roff; a.n = n;
+  const int threads = 256;
+  const int blocks = (n * 32 + threads - 1) / threads;
+  kmc_init_kernel<<<blocks, threads, 0, p->stream>>>(a);
+  CK(cudaGetLastError());
+  p->launches++;
+  // the staging buffers are reused by the next admission: wait for this one
+  CK(cudaStreamSynchronize(p->stream));
+  for (int i = 0; i < n; i++) slots_out[i] = got[i];
+  return KMC_OK;
+}
+
+int kmc_pool_admit(kmc_pool *p, int32_t model_id, const int32_t dims[3], int32_t layer, int32_t seed,
+                   int32_t rng_kind, uint32_t traj_id, const double *rates, int32_t *slot) {
+  const int32_t roff = 0;
+  return kmc_pool_admit_many(p, 1, &model_id, dims, layer, &seed, rng_kind, &traj_id, rates, &roff, slot);
+}
+
+int kmc_pool_release(kmc_pool *p, int32_t slot) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(p->mu);
+  CK(cudaStreamSynchronize(p->stream));
+  free_block(p, p->slots[slot].off, p->slots[slot].bytes);
+  p->slots[slot] = SlotHost();
+  return KMC_OK;
+}
+
+int kmc_pool_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int32_t n) {
+  if (!p || n < 0 || (n && (!slots || !steps))) return fail(KMC_ERR_ARG, "bad arguments");
+  if (n == 0) return KMC_OK;
+  if (n > (int)p->slots.size()) return fail(KMC_ERR_ARG, "too many slots");
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+    if (steps[i] < 0) return fail(KMC_ERR_ARG, "negative step count");
+  }
+  CK(cudaSetDevice(p->device));
+  *p->h_cancel = 0;
+  CK(cudaMemcpyAsync(p->d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_steps, steps, sizeof(int64_t) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaEventRecord(p->ev0, p->stream));
+  int rc = launch_run(p, p->d_list, p->d_steps, n, nullptr);
+  CK(cudaEventRecord(p->ev1, p->stream));
+  p->timed = true;
+  return rc;
+}
+
+int kmc_pool_run_graph(kmc_pool *p, const int32_t *slots, int64_t steps, int32_t n) {
+  if (!p || n < 1 || !slots || steps < 0) return fail(KMC_ERR_ARG, "bad arguments");
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+  }
+  CK(cudaSetDevice(p->device));
+  GraphKey key{steps, std::vector<int32_t>(slots, slots + n)};
+  auto it = p->graphs.find(key);
+  if (it == p->graphs.end()) {
+    GraphEntry e;
+    CK(cudaMalloc(&e.d_list, sizeof(int32_t) * n));
+    CK(cudaMalloc(&e.d_steps, sizeof(int64_t) * n));
+    std::vector<int64_t> st(n, steps);
+    CK(cudaMemcpy(e.d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e.d_steps, st.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
+    // set the kernel attributes and occupancy outside capture
+    CK(cudaStreamSynchronize(p->stream));
+    CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t before = p->launches;
+    int rc = launch_run(p, e.d_list, e.d_steps, n, nullptr);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    p->launches = before;
+    if (rc) return rc;
+    if (ce != cudaSuccess) return fail(KMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    e.graph = g;
+    CK(cudaGraphInstantiate(&e.exec, g, 0));
+    it = p->graphs.emplace(key, e).first;
+  }
+  *p->h_cancel = 0;
+  CK(cudaEventRecord(p->ev0, p->stream));
+  CK(cudaGraphLaunch(it->second.exec, p->stream));
+  CK(cudaEventRecord(p->ev1, p->stream));
+  p->timed = true;
+  p->launches++;
+  return KMC_OK;
+}
+
+int kmc_pool_sync(kmc_pool *p) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  CK(cudaStreamSynchronize(p->stream));
+  return KMC_OK;
+}
+
+int kmc_pool_cancel(kmc_pool *p) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  *(volatile int32_t *)p->h_cancel = 1;
+  return KMC_OK;
+}
+
+int kmc_pool_last_kernel_ms(kmc_pool *p, float *ms) {
+  if (!p || !ms || !p->timed) return fail(KMC_ERR_ARG, "no timed launch");
+  CK(cudaEventSynchronize(p->ev1));
+  CK(cudaEventElapsedTime(ms, p->ev0, p->ev1));
+  return KMC_OK;
+}
+
+int kmc_pool_launch_count(kmc_pool *p, int64_t *count) {
+  if (!p || !count) return fail(KMC_ERR_ARG, "bad arguments");
+  *count = p->launches;
+  return KMC_OK;
+}
+
+int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per_sm) {
+  if (!p || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
+  p->warps_per_block = warps_per_block ? warps_per_block : 4;
+  p->blocks_per_sm = blocks_per_sm;
+  for (auto &kv : p->graphs) {
+    cudaGraphExecDestroy(kv.second.exec);
+    cudaGraphDestroy(kv.second.graph);
+    cudaFree(kv.second.d_list);
+    cudaFree(kv.second.d_steps);
+  }
+  p->graphs.clear();
+  return KMC_OK;
+}
+
+int kmc_pool_get_status(kmc_pool *p, int32_t slot, int32_t *status) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  SlotDev d;
+  rc = read_slot(p, slot, &d);
+  if (rc) return rc;
+  *status = d.status;
+  return KMC_OK;
+}
+
+int kmc_pool_get_clock(kmc_pool *p, int32_t slot, double *t, int64_t *step) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  SlotDev d;
+  rc = read_slot(p, slot, &d);
+  if (rc) return rc;
+  if (t) *t = d.kmc_time;
+  if (step) *step = d.kmc_step;
+  return KMC_OK;
+}
+
+#define POOL_VEC_GETTER(NAME, FIELD, TYPE)                                                   \
+  int NAME(kmc_pool *p, int32_t slot, TYPE *out) {                                           \
+    int rc = check_slot(p, slot);                                                            \
+    if (rc) return rc;                                                                       \
+    CK(cudaStreamSynchronize(p->stream));                                                    \
+    const SlotDev &d = p->slots[slot].dev;                                                   \
+    CK(cudaMemcpy(out, d.FIELD, sizeof(TYPE) * d.P, cudaMemcpyDeviceToHost));                 \
+    return KMC_OK;                                                                           \
+  }
+POOL_VEC_GETTER(kmc_pool_get_procstat, procstat, int64_t)
+POOL_VEC_GETTER(kmc_pool_get_integ_rates, integ, double)
+POOL_VEC_GETTER(kmc_pool_get_nr_of_sites, nsites, int32_t)
+
+int kmc_pool_get_lattice(kmc_pool *p, int32_t slot, int32_t *out) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(p->stream));
+  const SlotDev &d = p->slots[slot].dev;
+  std::vector<int8_t> tmp(d.V);
+  CK(cudaMemcpy(tmp.data(), d.lat, d.V, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < d.V; i++) out[i] = tmp[i];
+  return KMC_OK;
+}
+
+int kmc_pool_get_tables(kmc_pool *p, int32_t slot, int32_t *as1, int32_t *as2) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(p->stream));
+  const SlotDev &d = p->slots[slot].dev;
+  const size_t bytes = sizeof(int32_t) * (size_t)d.P * (d.V + 1);
+  if (as1) CK(cudaMemcpy(as1, d.as1, bytes, cudaMemcpyDeviceToHost));
+  if (as2) CK(cudaMemcpy(as2, d.as2, bytes, cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
+int kmc_pool_occupation_counts(kmc_pool *p, const int32_t *slots, int32_t n, int32_t stride, int64_t *out) {
+  if (!p || n < 1 || !slots || !out || stride < 1) return fail(KMC_ERR_ARG, "bad arguments");
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+  }
+  int32_t *d_list = nullptr;
+  unsigned long long *d_out = nullptr;
+  CK(cudaMallocAsync(&d_list, sizeof(int32_t) * n, p->stream));
+  CK(cudaMallocAsync(&d_out, sizeof(unsigned long long) * (size_t)n * stride, p->stream));
+  CK(cudaMemsetAsync(d_out, 0, sizeof(unsigned long long) * (size_t)n * stride, p->stream));
+  CK(cudaMemcpyAsync(d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  kmc_occupation_kernel<<<n, 256, 0, p->stream>>>(p->d_slots, p->d_models, d_list, n, stride, d_out);
+  CK(cudaGetLastError());
+  p->launches++;
+  CK(cudaMemcpyAsync(out, d_out, sizeof(unsigned long long) * (size_t)n * stride, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaFreeAsync(d_list, p->stream));
+  CK(cudaFreeAsync(d_out, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  return KMC_OK;
+}
+
+// ---------------------------------------------------------- single trajectory API
+int kmc_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer, int32_t seed,
+               int32_t rng_kind, uint32_t traj_id, kmc_handle **out) {
+  if (!program || !dims || !out) return fail(KMC_ERR_ARG, "bad arguments");
+  ModelDev md;
+  int rc = validate_program(program, program_len, &md);
+  if (rc) return rc;
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(KMC_ERR_ARG, "bad system size");
+  const int V = dims[0] * dims[1] * dims[2] * md.spuck;
+  const size_t bytes = align_up(slot_layout(md.P, V).total, 256);
+  kmc_pool *p = nullptr;
+  rc = kmc_pool_create(0, bytes, 1, &p);
+  if (rc) return rc;
+  kmc_handle *h = new kmc_handle();
+  h->pool = p;
+  rc = kmc_pool_add_model(p, program, program_len, &h->model);
+  if (rc) { kmc_pool_destroy(p); delete h; return rc; }
+  std::vector<double> zeros(md.P, 0.0);
+  rc = kmc_pool_admit(p, h->model, dims, layer, seed, rng_kind, traj_id, zeros.data(), &h->slot);
+  if (rc) { kmc_pool_destroy(p); delete h; return rc; }
+  h->P = md.P; h->V = V; h->spuck = md.spuck; h->nspecies = md.nspecies;
+  int32_t st = 0;
+  rc = kmc_pool_get_status(p, h->slot, &st);
+  if (rc || st) { kmc_pool_destroy(p); delete h; return rc ? rc : fail(st, "initialize_state failed"); }
+  *out = h;
+  return KMC_OK;
+}
+
+int kmc_destroy(kmc_handle *h) {
+  if (!h) return KMC_OK;
+  if (h->d_trace) cudaFree(h->d_trace);
+  kmc_pool_destroy(h->pool);
+  delete h;
+  return KMC_OK;
+}
+
+#define HCHECK(h) \
+  if (!(h) || !(h)->pool) return fail(KMC_ERR_ARG, "bad handle");
+
+int kmc_set_rate_const(kmc_handle *h, int32_t proc, double rate) {
+  HCHECK(h);
+  if (proc < 1 || proc > h->P) return fail(KMC_ERR_ARG, "proc out of range");
+  const SlotDev &d = h->pool->slots[h->slot].dev;
+  CK(cudaStreamSynchronize(h->pool->stream));
+  CK(cudaMemcpy(d.rates + proc - 1, &rate, sizeof(double), cudaMemcpyHostToDevice));
+  const int32_t zero = 0;
+  CK(cudaMemcpy(&h->pool->d_slots[h->slot].accum_from, &zero, sizeof(int32_t), cudaMemcpyHostToDevice));
+  return KMC_OK;
+}
+
+int kmc_update_accum_rate(kmc_handle *h) {
+  HCHECK(h);
+  return run_command(h->pool, h->slot, CMD_ACCUM, 0, 0, 0, nullptr, nullptr);
+}
+
+int kmc_update_integ_rate(kmc_handle *h) {
+  HCHECK(h);
+  return run_command(h->pool, h->slot, CMD_INTEG, 0, 0, 0, nullptr, nullptr);
+}
+
+static int finish_run(kmc_handle *h) {
+  int32_t st = 0;
+  int rc = kmc_pool_get_status(h->pool, h->slot, &st);
+  if (rc) return rc;
+  if (st) {
+    // keep the trajectory usable for inspection: clear the status word
+    const int32_t zero = 0;
+    CK(cudaMemcpy(&h->pool->d_slots[h->slot].status, &zero, sizeof(int32_t), cudaMemcpyHostToDevice));
+    return fail(st, "kMC step failed with status " + std::to_string(st));
+  }
+  return KMC_OK;
+}
+
+int kmc_do_steps(kmc_handle *h, int64_t n) {
+  HCHECK(h);
+  if (n < 0) return fail(KMC_ERR_ARG, "negative step count");
+  int rc = kmc_pool_run(h->pool, &h->slot, &n, 1);
+  if (rc) return rc;
+  return finish_run(h);
+}
+
+int kmc_trace_steps(kmc_handle *h, int64_t n, int32_t *out) {
+  HCHECK(h);
+  if (n < 0 || !out) return fail(KMC_ERR_ARG, "bad arguments");
+  if (n == 0) return KMC_OK;
+  kmc_pool *p = h->pool;
+  if (h->trace_cap < n) {
+    if (h->d_trace) cudaFree(h->d_trace);
+    CK(cudaMalloc(&h->d_trace, sizeof(int32_t) * 2 * n));
+    h->trace_cap = n;
+  }
+  CK(cudaMemcpyAsync(p->d_list, &h->slot, sizeof(int32_t), cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_steps, &n, sizeof(int64_t), cudaMemcpyHostToDevice, p->stream));
+  *p->h_cancel = 0;
+  int rc = launch_run(p, p->d_list, p->d_steps, 1, h->d_trace);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out, h->d_trace, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, p->stream));
+  return finish_run(h);
+}
+
+int kmc_get_next_step(kmc_handle *h, int32_t *proc, int32_t *site) {
+  HCHECK(h);
+  return run_command(h->pool, h->slot, CMD_GET_NEXT, 0, 0, 0, proc, site);
+}
+
+int kmc_run_proc_nr(kmc_handle *h, int32_t proc, int32_t site) {
+  HCHECK(h);
+  if (proc < 1 || proc > h->P || site < 1 || site > h->V) return fail(KMC_ERR_ARG, "proc or site out of range");
+  return run_command(h->pool, h->slot, CMD_RUN_PROC, proc, site, 0, nullptr, nullptr);
+}
+
+int kmc_touchup(kmc_handle *h, int32_t site) {
+  HCHECK(h);
+  if (site < 1 || site > h->V) return fail(KMC_ERR_ARG, "site out of range");
+  return run_command(h->pool, h->slot, CMD_TOUCHUP, site, 0, 0, nullptr, nullptr);
+}
+
+int kmc_replace_species(kmc_handle *h, int32_t site, int32_t old_species, int32_t new_species) {
+  HCHECK(h);
+  if (site < 1 || site > h->V) return fail(KMC_ERR_ARG, "site out of range");
+  return run_command(h->pool, h->slot, CMD_REPLACE, site, old_species, new_species, nullptr, nullptr);
+}
+
+int kmc_get_species(kmc_handle *h, int32_t site, int32_t *species) {
+  HCHECK(h);
+  if (site < 1 || site > h->V || !species) return fail(KMC_ERR_ARG, "site out of range");
+  CK(cudaStreamSynchronize(h->pool->stream));
+  int8_t s;
+  CK(cudaMemcpy(&s, h->pool->slots[h->slot].dev.lat + site - 1, 1, cudaMemcpyDeviceToHost));
+  *species = s;
+  return KMC_OK;
+}
+
+int kmc_get_kmc_time(kmc_handle *h, double *t) {
+  HCHECK(h);
+  return kmc_pool_get_clock(h->pool, h->slot, t, nullptr);
+}
+
+int kmc_set_kmc_time(kmc_handle *h, double t) {
+  HCHECK(h);
+  CK(cudaStreamSynchronize(h->pool->stream));
+  CK(cudaMemcpy(&h->pool->d_slots[h->slot].kmc_time, &t, sizeof(double), cudaMemcpyHostToDevice));
+  return KMC_OK;
+}
+
+int kmc_get_kmc_time_step(kmc_handle *h, double *dt) {
+  HCHECK(h);
+  SlotDev d;
+  int rc = read_slot(h->pool, h->slot, &d);
+  if (rc) return rc;
+  *dt = d.kmc_time_step;
+  return KMC_OK;
+}
+
+int kmc_get_kmc_step(kmc_handle *h, int64_t *step) {
+  HCHECK(h);
+  return kmc_pool_get_clock(h->pool, h->slot, nullptr, step);
+}
+
+int kmc_get_volume(kmc_handle *h, int32_t *volume) {
+  HCHECK(h);
+  *volume = h->V;
+  return KMC_OK;
+}
+
+int kmc_get_nr_of_proc(kmc_handle *h, int32_t *nproc) {
+  HCHECK(h);
+  *nproc = h->P;
+  return KMC_OK;
+}
+
+int kmc_get_procstat(kmc_handle *h, int64_t *out) { HCHECK(h); return kmc_pool_get_procstat(h->pool, h->slot, out); }
+int kmc_get_integ_rates(kmc_handle *h, double *out) { HCHECK(h); return kmc_pool_get_integ_rates(h->pool, h->slot, out); }
+int kmc_get_nr_of_sites(kmc_handle *h, int32_t *out) { HCHECK(h); return kmc_pool_get_nr_of_sites(h->pool, h->slot, out); }
+
+int kmc_get_rates(kmc_handle *h, double *out) {
+  HCHECK(h);
+  CK(cudaStreamSynchronize(h->pool->stream));
+  CK(cudaMemcpy(out, h->pool->slots[h->slot].dev.rates, sizeof(double) * h->P, cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
+int kmc_get_accum_rates(kmc_handle *h, double *out) {
+  HCHECK(h);
+  CK(cudaStreamSynchronize(h->pool->stream));
+  CK(cudaMemcpy(out, h->pool->slots[h->slot].dev.accum, sizeof(double) * h->P, cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
+int kmc_get_avail_site(kmc_handle *h, int32_t proc, int32_t idx, int32_t sw, int32_t *out) {
+  HCHECK(h);
+  if (proc < 1 || proc > h->P || idx < 1 || idx > h->V || (sw != 1 && sw != 2) || !out)
+    return fail(KMC_ERR_ARG, "index out of range");
+  CK(cudaStreamSynchronize(h->pool->stream));
+  const SlotDev &d = h->pool->slots[h->slot].dev;
+  const int32_t *tab = sw == 1 ? d.as1 : d.as2;
+  CK(cudaMemcpy(out, tab + (size_t)(proc - 1) * (h->V + 1) + idx, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
+int kmc_get_lattice(kmc_handle *h, int32_t *out) { HCHECK(h); return kmc_pool_get_lattice(h->pool, h->slot, out); }
+int kmc_get_tables(kmc_handle *h, int32_t *as1, int32_t *as2) { HCHECK(h); return kmc_pool_get_tables(h->pool, h->slot, as1, as2); }
+
+int kmc_get_occupation(kmc_handle *h, double *out) {
+  HCHECK(h);
+  const int stride = h->nspecies * h->spuck;
+  std::vector<int64_t> counts(stride);
+  int rc = kmc_pool_occupation_counts(h->pool, &h->slot, 1, stride, counts.data());
+  if (rc) return rc;
+  const SlotDev &d = h->pool->slots[h->slot].dev;
+  const double cells = (double)d.X * d.Y * d.Z;
+  for (int i = 0; i < stride; i++) out[i] = (double)counts[i] / cells;
+  return KMC_OK;
+}
+
+}  // extern "C"

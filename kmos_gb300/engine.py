@@ -1,0 +1,426 @@
+"""ctypes binding of ``libkmcgb300.so`` (include/kmc_gb300.h).
+
+:class:`Trajectory` is one trajectory behind the f2py-style module interface (the plain
+drop-in); :class:`Pool` holds many resident trajectories for batching and serving.
+There is no CPU fallback: if the library or a CUDA device is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Iterable, List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+KMC_OK = 0
+ERRORS = {
+    1: "bad argument",
+    2: "replace_species: wrong species on site",
+    3: "dead lock: no process available",
+    4: "avail_sites inconsistency",
+    5: "malformed model program",
+    6: "device arena full",
+    7: "CUDA error",
+    8: "cancelled",
+    9: "no CUDA device",
+}
+RNG_GFORTRAN = 0
+RNG_PHILOX = 1
+
+# Every function the header declares: name -> (restype, argtypes)
+_vp, _i32, _i64, _dbl, _u32, _sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_uint32, ctypes.c_size_t
+_P = ctypes.POINTER
+_p32, _p64, _pd, _pu32 = _P(_i32), _P(_i64), _P(_dbl), _P(_u32)
+SIGNATURES = {
+    "kmc_last_error": (ctypes.c_char_p, []),
+    "kmc_version": (ctypes.c_char_p, []),
+    "kmc_create": (_i32, [_p32, _i32, _p32, _i32, _i32, _i32, _u32, _P(_vp)]),
+    "kmc_destroy": (_i32, [_vp]),
+    "kmc_set_rate_const": (_i32, [_vp, _i32, _dbl]),
+    "kmc_update_accum_rate": (_i32, [_vp]),
+    "kmc_update_integ_rate": (_i32, [_vp]),
+    "kmc_do_steps": (_i32, [_vp, _i64]),
+    "kmc_trace_steps": (_i32, [_vp, _i64, _p32]),
+    "kmc_get_next_step": (_i32, [_vp, _p32, _p32]),
+    "kmc_run_proc_nr": (_i32, [_vp, _i32, _i32]),
+    "kmc_touchup": (_i32, [_vp, _i32]),
+    "kmc_get_species": (_i32, [_vp, _i32, _p32]),
+    "kmc_replace_species": (_i32, [_vp, _i32, _i32, _i32]),
+    "kmc_get_kmc_time": (_i32, [_vp, _pd]),
+    "kmc_set_kmc_time": (_i32, [_vp, _dbl]),
+    "kmc_get_kmc_time_step": (_i32, [_vp, _pd]),
+    "kmc_get_kmc_step": (_i32, [_vp, _p64]),
+    "kmc_get_volume": (_i32, [_vp, _p32]),
+    "kmc_get_nr_of_proc": (_i32, [_vp, _p32]),
+    "kmc_get_procstat": (_i32, [_vp, _p64]),
+    "kmc_get_integ_rates": (_i32, [_vp, _pd]),
+    "kmc_get_rates": (_i32, [_vp, _pd]),
+    "kmc_get_accum_rates": (_i32, [_vp, _pd]),
+    "kmc_get_nr_of_sites": (_i32, [_vp, _p32]),
+    "kmc_get_avail_site": (_i32, [_vp, _i32, _i32, _i32, _p32]),
+    "kmc_get_lattice": (_i32, [_vp, _p32]),
+    "kmc_get_tables": (_i32, [_vp, _p32, _p32]),
+    "kmc_get_occupation": (_i32, [_vp, _pd]),
+    "kmc_pool_create": (_i32, [_i32, _sz, _i32, _P(_vp)]),
+    "kmc_pool_destroy": (_i32, [_vp]),
+    "kmc_pool_add_model": (_i32, [_vp, _p32, _i32, _p32]),
+    "kmc_pool_slot_bytes": (_i32, [_vp, _i32, _p32, _P(_sz)]),
+    "kmc_pool_free_bytes": (_i32, [_vp, _P(_sz), _P(_sz)]),
+    "kmc_pool_admit": (_i32, [_vp, _i32, _p32, _i32, _i32, _i32, _u32, _pd, _p32]),
+    "kmc_pool_admit_many": (_i32, [_vp, _i32, _p32, _p32, _i32, _p32, _i32, _pu32, _pd, _p32, _p32]),
+    "kmc_pool_release": (_i32, [_vp, _i32]),
+    "kmc_pool_run": (_i32, [_vp, _p32, _p64, _i32]),
+    "kmc_pool_run_graph": (_i32, [_vp, _p32, _i64, _i32]),
+    "kmc_pool_sync": (_i32, [_vp]),
+    "kmc_pool_cancel": (_i32, [_vp]),
+    "kmc_pool_get_status": (_i32, [_vp, _i32, _p32]),
+    "kmc_pool_get_clock": (_i32, [_vp, _i32, _pd, _p64]),
+    "kmc_pool_get_procstat": (_i32, [_vp, _i32, _p64]),
+    "kmc_pool_get_integ_rates": (_i32, [_vp, _i32, _pd]),
+    "kmc_pool_get_nr_of_sites": (_i32, [_vp, _i32, _p32]),
+    "kmc_pool_get_lattice": (_i32, [_vp, _i32, _p32]),
+    "kmc_pool_get_tables": (_i32, [_vp, _i32, _p32, _p32]),
+    "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
+    "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
+    "kmc_pool_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
+    "kmc_pool_launch_count": (_i32, [_vp, _p64]),
+}
+
+_lib = None
+
+
+class KMCError(RuntimeError):
+    def __init__(self, code: int, text: str = ""):
+        self.code = code
+        super().__init__("%s (status %d)%s" % (ERRORS.get(code, "error"), code, ": " + text if text else ""))
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads the engine library (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        if build_if_missing and _build.needs_build():
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError("kmc engine library %s is missing; run kmos_gb300.build.build()" % _build.LIB)
+        L = ctypes.CDLL(_build.LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int):
+    if rc != KMC_OK:
+        raise KMCError(rc, load().kmc_last_error().decode(errors="replace"))
+
+
+def _a32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _dims3(size: Sequence[int]) -> np.ndarray:
+    size = [int(s) for s in size] + [1] * (3 - len(size))
+    return _a32(size[:3])
+
+
+class Trajectory:
+    """One trajectory on the GPU (``kmc_create``).  ``program`` is a compiled
+    :class:`~kmos_gb300.program.Program` or its int32 words."""
+
+    def __init__(self, program, size, layer: int = 0, seed: int = 1, rng: int = RNG_GFORTRAN, traj: int = 0):
+        L = load()
+        words = _a32(getattr(program, "words", program))
+        self._words = words
+        dims = _dims3(size)
+        h = ctypes.c_void_p()
+        _check(L.kmc_create(_ptr(words, _i32), len(words), _ptr(dims, _i32), int(layer),
+                            int(np.int32(seed)), int(rng), int(traj) & 0xFFFFFFFF, ctypes.byref(h)))
+        self.h = h
+        self.P = int(words[3])
+        self.nspecies = int(words[4])
+        self.spuck = int(words[6])
+        self.size = [int(x) for x in dims]
+        v = _i32()
+        _check(L.kmc_get_volume(self.h, ctypes.byref(v)))
+        self.V = v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- base ---
+    def set_rate_const(self, proc: int, rate: float):
+        _check(load().kmc_set_rate_const(self.h, int(proc), float(rate)))
+
+    def set_rates(self, rates: Iterable[float]):
+        for p, r in enumerate(rates, start=1):
+            self.set_rate_const(p, r)
+
+    def update_accum_rate(self):
+        _check(load().kmc_update_accum_rate(self.h))
+
+    def update_integ_rate(self):
+        _check(load().kmc_update_integ_rate(self.h))
+
+    # --- proclist ---
+    def do_kmc_steps(self, n: int):
+        _check(load().kmc_do_steps(self.h, int(n)))
+
+    def trace(self, n: int) -> np.ndarray:
+        out = np.zeros(2 * int(n), dtype=np.int32)
+        _check(load().kmc_trace_steps(self.h, int(n), _ptr(out, _i32)))
+        return out.reshape(-1, 2)
+
+    def get_next_kmc_step(self):
+        p, s = _i32(), _i32()
+        _check(load().kmc_get_next_step(self.h, ctypes.byref(p), ctypes.byref(s)))
+        return p.value, s.value
+
+    def run_proc_nr(self, proc: int, site: int):
+        _check(load().kmc_run_proc_nr(self.h, int(proc), int(site)))
+
+    def touchup(self, site: int):
+        _check(load().kmc_touchup(self.h, int(site)))
+
+    def get_species(self, site: int) -> int:
+        s = _i32()
+        _check(load().kmc_get_species(self.h, int(site), ctypes.byref(s)))
+        return s.value
+
+    def replace_species(self, site: int, old: int, new: int):
+        _check(load().kmc_replace_species(self.h, int(site), int(old), int(new)))
+
+    # --- getters ---
+    @property
+    def kmc_time(self) -> float:
+        t = _dbl()
+        _check(load().kmc_get_kmc_time(self.h, ctypes.byref(t)))
+        return t.value
+
+    @kmc_time.setter
+    def kmc_time(self, t: float):
+        _check(load().kmc_set_kmc_time(self.h, float(t)))
+
+    @property
+    def kmc_time_step(self) -> float:
+        t = _dbl()
+        _check(load().kmc_get_kmc_time_step(self.h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def kmc_step(self) -> int:
+        s = _i64()
+        _check(load().kmc_get_kmc_step(self.h, ctypes.byref(s)))
+        return s.value
+
+    def _vec(self, fn, dtype, ctype, n=None):
+        out = np.zeros(self.P if n is None else n, dtype=dtype)
+        _check(fn(self.h, _ptr(out, ctype)))
+        return out
+
+    def procstat(self):
+        return self._vec(load().kmc_get_procstat, np.int64, _i64)
+
+    def integ_rates(self):
+        return self._vec(load().kmc_get_integ_rates, np.float64, _dbl)
+
+    def rates(self):
+        return self._vec(load().kmc_get_rates, np.float64, _dbl)
+
+    def accum_rates(self):
+        return self._vec(load().kmc_get_accum_rates, np.float64, _dbl)
+
+    def nr_of_sites(self):
+        return self._vec(load().kmc_get_nr_of_sites, np.int32, _i32)
+
+    def avail_site(self, proc: int, idx: int, sw: int) -> int:
+        o = _i32()
+        _check(load().kmc_get_avail_site(self.h, int(proc), int(idx), int(sw), ctypes.byref(o)))
+        return o.value
+
+    def lattice(self) -> np.ndarray:
+        return self._vec(load().kmc_get_lattice, np.int32, _i32, self.V)
+
+    def tables(self):
+        as1 = np.zeros(self.P * (self.V + 1), np.int32)
+        as2 = np.zeros(self.P * (self.V + 1), np.int32)
+        _check(load().kmc_get_tables(self.h, _ptr(as1, _i32), _ptr(as2, _i32)))
+        return as1.reshape(self.P, self.V + 1), as2.reshape(self.P, self.V + 1)
+
+    def occupation(self) -> np.ndarray:
+        out = np.zeros(self.nspecies * self.spuck)
+        _check(load().kmc_get_occupation(self.h, _ptr(out, _dbl)))
+        return out.reshape(self.nspecies, self.spuck)
+
+
+class Pool:
+    """Many resident trajectories in one device arena (``kmc_pool_*``)."""
+
+    def __init__(self, arena_bytes: int, max_slots: int, device: int = 0):
+        L = load()
+        h = ctypes.c_void_p()
+        _check(L.kmc_pool_create(int(device), int(arena_bytes), int(max_slots), ctypes.byref(h)))
+        self.h = h
+        self.models: List[np.ndarray] = []
+        self.slot_model = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kmc_pool_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_model(self, program) -> int:
+        words = _a32(getattr(program, "words", program))
+        mid = _i32()
+        _check(load().kmc_pool_add_model(self.h, _ptr(words, _i32), len(words), ctypes.byref(mid)))
+        self.models.append(words)
+        return mid.value
+
+    def nproc(self, model_id: int) -> int:
+        return int(self.models[model_id][3])
+
+    def slot_bytes(self, model_id: int, size) -> int:
+        b = _sz()
+        dims = _dims3(size)
+        _check(load().kmc_pool_slot_bytes(self.h, int(model_id), _ptr(dims, _i32), ctypes.byref(b)))
+        return b.value
+
+    def free_bytes(self):
+        t, l = _sz(), _sz()
+        _check(load().kmc_pool_free_bytes(self.h, ctypes.byref(t), ctypes.byref(l)))
+        return t.value, l.value
+
+    def admit(self, model_id: int, size, rates, layer: int = 0, seed: int = 1, rng: int = RNG_PHILOX,
+              traj: int = 0) -> int:
+        return self.admit_many([model_id], [size], [rates], layer=layer, seeds=[seed], rng=rng, trajs=[traj])[0]
+
+    def admit_many(self, model_ids, sizes, rates_list, layer: int = 0, seeds=None, rng: int = RNG_PHILOX,
+                   trajs=None) -> List[int]:
+        n = len(model_ids)
+        mids = _a32(model_ids)
+        dims = _a32(np.concatenate([_dims3(s) for s in sizes]))
+        seeds = _a32(seeds if seeds is not None else [1] * n)
+        trajs = np.ascontiguousarray(trajs if trajs is not None else np.arange(n), dtype=np.uint32)
+        offs, flat = [], []
+        for r in rates_list:
+            offs.append(len(flat))
+            flat.extend(float(x) for x in r)
+        offs = _a32(offs)
+        flat = np.ascontiguousarray(flat, dtype=np.float64)
+        slots = np.zeros(n, np.int32)
+        _check(load().kmc_pool_admit_many(self.h, n, _ptr(mids, _i32), _ptr(dims, _i32), int(layer),
+                                          _ptr(seeds, _i32), int(rng), _ptr(trajs, _u32), _ptr(flat, _dbl),
+                                          _ptr(offs, _i32), _ptr(slots, _i32)))
+        for s, m in zip(slots, model_ids):
+            self.slot_model[int(s)] = int(m)
+        return [int(s) for s in slots]
+
+    def release(self, slot: int):
+        _check(load().kmc_pool_release(self.h, int(slot)))
+        self.slot_model.pop(int(slot), None)
+
+    def run(self, slots, steps, sync: bool = True):
+        slots = _a32(slots)
+        steps = np.ascontiguousarray(np.broadcast_to(np.asarray(steps, dtype=np.int64), slots.shape))
+        _check(load().kmc_pool_run(self.h, _ptr(slots, _i32), _ptr(steps, _i64), len(slots)))
+        if sync:
+            self.sync()
+
+    def run_graph(self, slots, steps: int, sync: bool = True):
+        slots = _a32(slots)
+        _check(load().kmc_pool_run_graph(self.h, _ptr(slots, _i32), int(steps), len(slots)))
+        if sync:
+            self.sync()
+
+    def sync(self):
+        _check(load().kmc_pool_sync(self.h))
+
+    def cancel(self):
+        _check(load().kmc_pool_cancel(self.h))
+
+    def set_launch(self, warps_per_block: int = 0, blocks_per_sm: int = 0):
+        _check(load().kmc_pool_set_launch(self.h, int(warps_per_block), int(blocks_per_sm)))
+
+    def last_kernel_ms(self) -> float:
+        ms = ctypes.c_float()
+        _check(load().kmc_pool_last_kernel_ms(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        c = _i64()
+        _check(load().kmc_pool_launch_count(self.h, ctypes.byref(c)))
+        return c.value
+
+    def status(self, slot: int) -> int:
+        s = _i32()
+        _check(load().kmc_pool_get_status(self.h, int(slot), ctypes.byref(s)))
+        return s.value
+
+    def clock(self, slot: int):
+        t, k = _dbl(), _i64()
+        _check(load().kmc_pool_get_clock(self.h, int(slot), ctypes.byref(t), ctypes.byref(k)))
+        return t.value, k.value
+
+    def _pvec(self, fn, slot, dtype, ctype):
+        out = np.zeros(self.nproc(self.slot_model[int(slot)]), dtype=dtype)
+        _check(fn(self.h, int(slot), _ptr(out, ctype)))
+        return out
+
+    def procstat(self, slot):
+        return self._pvec(load().kmc_pool_get_procstat, slot, np.int64, _i64)
+
+    def integ_rates(self, slot):
+        return self._pvec(load().kmc_pool_get_integ_rates, slot, np.float64, _dbl)
+
+    def nr_of_sites(self, slot):
+        return self._pvec(load().kmc_pool_get_nr_of_sites, slot, np.int32, _i32)
+
+    def lattice(self, slot, volume: int):
+        out = np.zeros(volume, np.int32)
+        _check(load().kmc_pool_get_lattice(self.h, int(slot), _ptr(out, _i32)))
+        return out
+
+    def tables(self, slot, volume: int):
+        P = self.nproc(self.slot_model[int(slot)])
+        as1 = np.zeros(P * (volume + 1), np.int32)
+        as2 = np.zeros(P * (volume + 1), np.int32)
+        _check(load().kmc_pool_get_tables(self.h, int(slot), _ptr(as1, _i32), _ptr(as2, _i32)))
+        return as1.reshape(P, volume + 1), as2.reshape(P, volume + 1)
+
+    def occupation_counts(self, slots, stride: int) -> np.ndarray:
+        slots = _a32(slots)
+        out = np.zeros(len(slots) * stride, np.int64)
+        _check(load().kmc_pool_occupation_counts(self.h, _ptr(slots, _i32), len(slots), int(stride), _ptr(out, _i64)))
+        return out.reshape(len(slots), stride)

@@ -445,3 +445,67 @@ def from_project(project) -> Model:
         meta=meta,
         representations={s.name: getattr(s, "representation", "") for s in project.species_list},
     )
+
+
+# --------------------------------------------------------------------------------------
+# JSON form (used for test fixtures and the serving protocol)
+# --------------------------------------------------------------------------------------
+def to_dict(model: Model) -> dict:
+    def cd(c: Condition):
+        d = {"species": c.species, "coord": [c.coord.name, list(c.coord.offset), c.coord.layer]}
+        if c.implicit:
+            d["implicit"] = True
+        return d
+
+    return {
+        "name": model.name,
+        "dimension": model.dimension,
+        "species": list(model.species),
+        "default_species": model.default_species,
+        "layers": [{"name": l.name, "sites": [[s.name, list(s.pos), s.default_species, s.tags] for s in l.sites]}
+                   for l in model.layers],
+        "default_layer": model.default_layer,
+        "substrate_layer": model.substrate_layer,
+        "cell": [list(r) for r in model.cell],
+        "parameters": [[p.name, p.value, p.adjustable, p.min, p.max, p.scale] for p in model.parameters],
+        "processes": [{"name": p.name, "rate_constant": p.rate_constant, "enabled": p.enabled,
+                       "tof_count": p.tof_count, "conditions": [cd(c) for c in p.conditions],
+                       "actions": [cd(a) for a in p.actions]} for p in model.processes],
+        "meta": dict(model.meta),
+        "representations": dict(model.representations),
+    }
+
+
+def from_dict(d: dict) -> Model:
+    def cd(x):
+        n, off, lay = x["coord"]
+        return Condition(x["species"], Coord(n, tuple(int(v) for v in off), lay), bool(x.get("implicit", False)))
+
+    return Model(
+        name=d["name"],
+        dimension=int(d["dimension"]),
+        species=list(d["species"]),
+        default_species=d["default_species"],
+        layers=[Layer(l["name"], [Site(s[0], tuple(s[1]), s[2], s[3]) for s in l["sites"]]) for l in d["layers"]],
+        default_layer=d["default_layer"],
+        substrate_layer=d["substrate_layer"],
+        cell=tuple(tuple(r) for r in d["cell"]),
+        parameters=[Parameter(*p) for p in d["parameters"]],
+        processes=[Process(p["name"], p["rate_constant"], [cd(c) for c in p["conditions"]],
+                           [cd(a) for a in p["actions"]], p.get("enabled", True), p.get("tof_count"))
+                   for p in d["processes"]],
+        meta=dict(d.get("meta", {})),
+        representations=dict(d.get("representations", {})),
+    )
+
+
+def save_json(model: Model, path: str):
+    import json
+    with open(path, "w") as fh:
+        json.dump(to_dict(model), fh, indent=1)
+
+
+def load_json(path: str) -> Model:
+    import json
+    with open(path) as fh:
+        return from_dict(json.load(fh))

@@ -1,0 +1,180 @@
+"""GPU engine against the CPU oracle: bit-exact processes, sites, occupations and
+tables after every sampled step; kmc_time and integ_rates within 1e-12 relative (the
+device log() and glibc's log() may differ in the last place)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fixture_model
+from kmos_gb300 import configs, engine as E, program as PG
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+CASES = [("AB_model", "local_smart", (20, 20)), ("ZGB_model", "local_smart", (16, 12)),
+         ("ZGB_model", "lat_int", (12, 16)), ("CO_oxidation_Ruo2", "local_smart", (10, 10)),
+         ("CO_oxidation_Ruo2", "lat_int", (9, 11)), ("pairwise_interaction", "lat_int", (16, 16)),
+         ("pairwise_interaction", "local_smart", (8, 8)), ("default_xml", "local_smart", (10, 10)),
+         ("pdopd_xml", "local_smart", (8, 8)), ("pdopd_xml", "lat_int", (8, 8))]
+
+
+def random_rates(P, seed):
+    return (10.0 ** np.random.default_rng(seed).uniform(-1, 3, size=P)).tolist()
+
+
+def assert_same_state(gpu, orc, P, V):
+    st = orc.export()
+    np.testing.assert_array_equal(gpu.lattice(), st["lattice"])
+    as1, as2 = gpu.tables()
+    np.testing.assert_array_equal(as1, st["as1"])
+    np.testing.assert_array_equal(as2, st["as2"])
+    np.testing.assert_array_equal(gpu.nr_of_sites(), st["nsites"])
+    np.testing.assert_array_equal(gpu.procstat(), st["procstat"])
+    np.testing.assert_allclose(gpu.integ_rates(), st["integ"], rtol=RTOL, atol=0)
+    assert gpu.kmc_step == orc.kmc_step
+    assert abs(gpu.kmc_time - orc.kmc_time) <= RTOL * abs(orc.kmc_time)
+
+
+def test_golden_trajectory_on_gpu():
+    """The reference's own golden trajectory (tests/test_run/test_run.py) through the
+    C-ABI: get_next_kmc_step + run_proc_nr, gfortran stream, seed 1."""
+    ref = np.load(os.path.join(GOLDEN, "ab_model_ref_procs_sites.npy"))
+    m = fixture_model("AB_model")
+    rates = json.load(open(os.path.join(GOLDEN, "ab_model_rates.json")))["rates"]
+    with E.Trajectory(PG.compile_model(m, "local_smart"), (20, 20), seed=1, rng=E.RNG_GFORTRAN) as t:
+        t.set_rates(rates)
+        t.update_accum_rate()
+        out = np.zeros_like(ref)
+        for i in range(len(ref)):
+            p, s = t.get_next_kmc_step()
+            out[i] = (p, s)
+            t.run_proc_nr(p, s)
+    np.testing.assert_array_equal(out, ref)
+
+
+@pytest.mark.parametrize("name,backend,size", CASES)
+def test_initial_state(name, backend, size):
+    prog = PG.compile_model(fixture_model(name), backend)
+    with E.Trajectory(prog, size, seed=5) as g:
+        o = O.Oracle(prog, size, seed=5)
+        st = o.export()
+        np.testing.assert_array_equal(g.lattice(), st["lattice"])
+        as1, as2 = g.tables()
+        np.testing.assert_array_equal(as1, st["as1"])
+        np.testing.assert_array_equal(as2, st["as2"])
+
+
+@pytest.mark.parametrize("rng", [E.RNG_GFORTRAN, E.RNG_PHILOX])
+@pytest.mark.parametrize("name,backend,size", CASES)
+def test_trace_matches_oracle(name, backend, size, rng):
+    prog = PG.compile_model(fixture_model(name), backend)
+    rates = random_rates(prog.nproc, 11)
+    with E.Trajectory(prog, size, seed=17, rng=rng, traj=4) as g:
+        o = O.Oracle(prog, size, seed=17, rng=rng, traj=4)
+        for x in (g, o):
+            x.set_rates(rates)
+            x.update_accum_rate()
+        for chunk in (1, 999, 9000):
+            np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+            assert_same_state(g, o, prog.nproc, o.V)
+        np.testing.assert_allclose(g.accum_rates(), o.accum_rates(), rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("config", [1, 2, 3, 4])
+def test_benchmark_configs_match_oracle(config):
+    wl = configs.build(config, n=3, steps=5000, sides=[16, 32])
+    for i in range(wl.n):
+        with E.Trajectory(wl.program, wl.sizes[i], seed=wl.seeds[i], rng=E.RNG_PHILOX, traj=wl.trajs[i]) as g:
+            o = O.Oracle(wl.program, wl.sizes[i], seed=wl.seeds[i], rng=O.RNG_PHILOX, traj=wl.trajs[i])
+            for x in (g, o):
+                x.set_rates(wl.rates[i])
+                x.update_accum_rate()
+            g.do_kmc_steps(wl.steps)
+            o.do_kmc_steps(wl.steps)
+            assert_same_state(g, o, wl.program.nproc, o.V)
+            np.testing.assert_allclose(g.occupation(), o.occupation(), rtol=0, atol=0)
+
+
+class PoolRun:
+    """A pool with several models and uneven lattices, run in one launch."""
+
+    def __init__(self, graph=False):
+        self.wls = [configs.build(2, n=3, steps=0), configs.build(3, n=4, steps=0, sides=[16, 32, 64]),
+                    configs.build(4, n=3, steps=0)]
+        self.pool = E.Pool(arena_bytes=256 << 20, max_slots=64)
+        self.items = []
+        for wl in self.wls:
+            mid = self.pool.add_model(wl.program)
+            for i in range(wl.n):
+                slot = self.pool.admit(mid, wl.sizes[i], wl.rates[i], seed=wl.seeds[i], rng=E.RNG_PHILOX,
+                                       traj=wl.trajs[i])
+                self.items.append((wl, i, slot))
+
+
+def oracle_for(wl, i, steps):
+    o = O.Oracle(wl.program, wl.sizes[i], seed=wl.seeds[i], rng=O.RNG_PHILOX, traj=wl.trajs[i])
+    o.set_rates(wl.rates[i])
+    o.update_accum_rate()
+    o.do_kmc_steps(steps)
+    return o
+
+
+def test_pool_batch_matches_oracle():
+    pr = PoolRun()
+    slots = [s for _wl, _i, s in pr.items]
+    steps = [1000 + 357 * k for k in range(len(slots))]  # uneven step counts
+    pr.pool.run(slots, steps)
+    for (wl, i, slot), n in zip(pr.items, steps):
+        o = oracle_for(wl, i, n)
+        st = o.export()
+        assert pr.pool.status(slot) == 0
+        np.testing.assert_array_equal(pr.pool.lattice(slot, o.V), st["lattice"])
+        as1, as2 = pr.pool.tables(slot, o.V)
+        np.testing.assert_array_equal(as1, st["as1"])
+        np.testing.assert_array_equal(as2, st["as2"])
+        np.testing.assert_array_equal(pr.pool.procstat(slot), st["procstat"])
+        t, k = pr.pool.clock(slot)
+        assert k == n and abs(t - o.kmc_time) <= RTOL * o.kmc_time
+
+
+def test_same_alone_and_in_the_mix():
+    """A trajectory's result does not depend on what else shares the launch."""
+    pr = PoolRun()
+    slots = [s for _wl, _i, s in pr.items]
+    pr.pool.run(slots, 3000)
+    mixed = {s: (pr.pool.procstat(s), pr.pool.clock(s)) for s in slots}
+    alone = PoolRun()
+    for (_wl, _i, s) in alone.items:
+        alone.pool.run([s], 3000)
+        ps, clk = alone.pool.procstat(s), alone.pool.clock(s)
+        np.testing.assert_array_equal(ps, mixed[s][0])
+        assert clk == mixed[s][1]
+
+
+def test_graph_replay_equals_plain_launch():
+    a, b = PoolRun(), PoolRun()
+    slots = [s for _wl, _i, s in a.items]
+    for _ in range(3):
+        a.pool.run(slots, 700)
+        b.pool.run_graph(slots, 700)
+    for s in slots:
+        np.testing.assert_array_equal(a.pool.procstat(s), b.pool.procstat(s))
+        assert a.pool.clock(s) == b.pool.clock(s)
+
+
+def test_deadlock_is_an_error_status_not_a_crash():
+    """Adsorption without desorption fills the lattice; the next step finds no process
+    (base.mpy:1293-1311 stops the process; here the call returns an error)."""
+    m = configs.model_config1()
+    prog = PG.compile_model(m, "local_smart")
+    with E.Trajectory(prog, (4, 4), seed=1, rng=E.RNG_PHILOX) as t:
+        t.set_rates([1.0, 0.0])
+        t.update_accum_rate()
+        with pytest.raises(E.KMCError) as err:
+            t.do_kmc_steps(100)
+        assert err.value.code == 3
+        assert t.kmc_step == 16
+        assert (t.lattice() == m.species_ids()["CO"]).all()
