@@ -1,0 +1,369 @@
+"""Aggregate kMC steps/s of the GB300 engine on one benchmark configuration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config C] [--impl ours|reference]
+
+One bench *step* = one persistent launch in which every trajectory of the batch
+advances ``--chunk`` kMC steps (do_kmc_steps on every trajectory).  The default
+workload is configuration 3, the one the 100x target is quoted on: 2048 lat_int
+trajectories of uneven square lattices (side 16..256, P=21, 6 lateral-interaction
+groups).  ``--config 2`` is the 4096-trajectory 64x64 ZGB-type batch; its CO-rich
+trajectories (y above ~0.525) reach the absorbing CO-poisoned state, where the
+reference stops ("can't find available process") and the engine retires the
+trajectory with a dead-lock status, so steps are always counted from the trajectories'
+own kmc_step counters.  The resident state (about 6 GB for configuration 3) is far
+larger than the 129 MB L2, so no explicit L2 flush is needed between steps.
+
+``value`` is device-timed (CUDA events on the engine's stream around the K launches,
+max over ranks); ``e2e`` is the same metric through the public pool API with the
+per-step host->device run list and a device->host read of every trajectory's
+procstat, integ_rates and clock.  ``--impl reference`` times the CPU restatement of the
+reference step loop (the reference's Fortran build needs a Fortran compiler that this
+machine does not have) on all host cores, on a bounded sample of the same workload.
+Under torchrun each rank runs its own batch (trajectory ids offset by rank): weak
+scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "aggregate kMC steps/s"
+UNIT = "steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4])
+    ap.add_argument("--chunk", type=int, default=0, help="kMC steps per trajectory per bench step")
+    ap.add_argument("--ntraj", type=int, default=0, help="override the trajectory count")
+    ap.add_argument("--graph", type=int, default=1, help="replay the launch from a CUDA graph")
+    ap.add_argument("--cpu-baseline", type=int, default=1)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--bps", type=int, default=0)
+    return ap.parse_args()
+
+
+DEFAULT_CHUNK = {1: 100000, 2: 20000, 3: 20000, 4: 10000}
+
+
+# ------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks sampler
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU side
+def _cpu_worker(args):
+    config, idx, steps = args
+    from kmos_gb300 import configs
+    from oracle import oracle as O
+    wl = configs.build(config, n=idx + 1, steps=steps)
+    o = O.Oracle(wl.program, wl.sizes[idx], seed=wl.seeds[idx], rng=O.RNG_PHILOX, traj=wl.trajs[idx])
+    o.set_rates(wl.rates[idx])
+    o.update_accum_rate()
+    t0 = time.perf_counter()
+    try:
+        o.do_kmc_steps(steps)
+    except O.OracleError:
+        pass  # absorbing state reached: the trajectory ends, as in the reference
+    return o.kmc_step, time.perf_counter() - t0
+
+
+CPU_STEPS = {1: 2_000_000, 2: 1_000_000, 3: 300_000, 4: 1_000_000}
+
+
+def cpu_sample(config: int, rounds: int = 1):
+    """The oracle (the CPU restatement of the reference loop, one process per core, each
+    on its own trajectory) on all host cores.  Returns (steps/s aggregate, cores, sample)."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    steps = CPU_STEPS[config]
+    ctx = mp.get_context("spawn")
+    total, wall = 0, 0.0
+    with ctx.Pool(cores) as pool:
+        for r in range(rounds):
+            # all workers run at once; the slowest one's own timer bounds the round
+            res = pool.map(_cpu_worker, [(config, (r * cores + i) % 64, steps) for i in range(cores)])
+            wall += max(t for _, t in res)
+            total += sum(s for s, _ in res)
+    sample = "%d trajectories x %d kMC steps of config %d, one process per core" % (cores * rounds, steps, config)
+    return total / wall, cores, sample
+
+
+def step_bytes(config: int, chunk: int = 50000):
+    """Algorithmic bytes per kMC step: 20P + 28P + 28 + 4*N_as + b_occ*N_occ, with N_as /
+    N_occ the mean int32 book-keeping / occupation accesses of run_proc_nr counted by
+    the instrumented oracle on this workload (int8 occupation, b_occ = 1)."""
+    from kmos_gb300 import configs
+    from oracle import oracle as O
+    wl = configs.build(config, n=1, steps=chunk)
+    o = O.Oracle(wl.program, wl.sizes[0], seed=wl.seeds[0], rng=O.RNG_PHILOX, traj=wl.trajs[0])
+    o.set_rates(wl.rates[0])
+    o.update_accum_rate()
+    o.do_kmc_steps(chunk)
+    o.reset_counters()
+    o.do_kmc_steps(chunk)
+    n_as, n_occ = o.counters()
+    P = wl.program.nproc
+    n_as, n_occ = n_as / chunk, n_occ / chunk
+    return 20 * P + 28 * P + 28 + 4 * n_as + 1 * n_occ, n_as, n_occ
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        dist.close()
+        return
+    warm = [cpu_sample(args.config) for _ in range(min(args.warmup, 1))]
+    vals = [cpu_sample(args.config) for _ in range(max(1, min(args.steps, 3)))]
+    value = statistics.median(v for v, _c, _s in vals)
+    _v, cores, sample = vals[0]
+    from kmos_gb300 import configs
+    wl = configs.build(args.config, n=1, steps=1)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": len(vals), "warmup": len(warm), "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl.name, "parallelism": "%d host processes" % cores},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference step loop (oracle/kmc_oracle.c); the reference's "
+                "Fortran build is unavailable here (no Fortran compiler on this machine)",
+    }
+    print(json.dumps(line))
+    dist.close()
+
+
+# ------------------------------------------------------------------ GPU run
+def run_ours(args, dist: Dist):
+    from kmos_gb300 import configs, engine as E
+
+    chunk = args.chunk or DEFAULT_CHUNK[args.config]
+    wl = configs.build(args.config, n=args.ntraj or None)
+    n = wl.n
+    dev = dist.local
+    pool_probe = None
+    E.load()
+    # size the arena from the per-slot byte counts
+    pool = E.Pool(arena_bytes=1 << 20, max_slots=1, device=dev)
+    mid = pool.add_model(wl.program)
+    need = sum(pool.slot_bytes(mid, s) for s in wl.sizes)
+    pool.close()
+    pool = E.Pool(arena_bytes=need + (64 << 20), max_slots=n, device=dev)
+    if args.warps or args.bps:
+        pool.set_launch(args.warps, args.bps)
+    mid = pool.add_model(wl.program)
+    trajs = [t + dist.rank * n for t in wl.trajs]
+    slots = []
+    B = 1024
+    for i in range(0, n, B):
+        slots += pool.admit_many([mid] * len(wl.sizes[i:i + B]), wl.sizes[i:i + B], wl.rates[i:i + B],
+                                 seeds=wl.seeds[i:i + B], rng=E.RNG_PHILOX, trajs=trajs[i:i + B])
+    # longest lattices first so uneven work balances across warps
+    order = sorted(range(n), key=lambda i: -wl.sizes[i][0] * wl.sizes[i][1])
+    slots = [slots[i] for i in order]
+    P = wl.program.nproc
+
+    def launch():
+        if args.graph:
+            pool.run_graph(slots, chunk, sync=False)
+        else:
+            pool.run(slots, chunk, sync=False)
+
+    for _ in range(args.warmup):
+        launch()
+    pool.sync()
+    _ps, _ig, _t, ksteps0, _st = pool.results(slots, P)
+
+    clocks = Clocks(dev)
+    dist.barrier()
+    pool.sync()
+    launches0 = pool.launch_count()
+    clocks.start()
+    pool.timer_start()
+    for _ in range(args.steps):
+        launch()
+    ms = pool.timer_stop()
+    clk = clocks.stop()
+    launches = pool.launch_count() - launches0
+    dist.barrier()
+    ms = dist.max(ms)
+    _ps, _ig, _t, ksteps, status = pool.results(slots, P)
+    bad = set(status.tolist()) - {0, 3}
+    if bad:
+        raise SystemExit("trajectories ended with status %s" % sorted(bad))
+    if not (ksteps - ksteps0 <= args.steps * chunk).all() or not ((ksteps - ksteps0 == args.steps * chunk) | (status == 3)).all():
+        raise SystemExit("step counters disagree with the launches")
+    kmc_steps_rank = int((ksteps - ksteps0).sum())
+    active = int((status == 0).sum())
+    total_steps = dist.sum(kmc_steps_rank)
+    value = total_steps / (ms / 1e3)
+
+    # end to end through the public API: host run list in, every trajectory's
+    # procstat / integ_rates / clock out, each step
+    e2e_steps = max(2, min(args.steps, 5))
+    dist.barrier()
+    k_before = ksteps
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        pool.run(slots, chunk, sync=False)
+        res = pool.results(slots, P)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.sum(int((res[3] - k_before).sum())) / e2e_s
+    h2d = n * 4 + n * 8
+    d2h = n * P * 16 + n * (8 + 8 + 4)
+
+    line = None
+    if dist.rank == 0:
+        import json as _json
+        peaks = {}
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            peaks = _json.load(open(pk))
+        peak = peaks.get("hbm_gbs", 6800.0)
+        bstep, n_as, n_occ = step_bytes(args.config)
+        per_launch_s = (ms / 1e3) / args.steps
+        achieved = bstep * (kmc_steps_rank / args.steps) / per_launch_s / 1e9
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic_config%d.json" % args.config)
+        if os.path.exists(prof):
+            tr = _json.load(open(prof))
+            traffic = tr.get("bytes_per_kmc_step", 0) * kmc_steps_rank / args.steps
+        cpu = None
+        if args.cpu_baseline:
+            v, cores, sample = cpu_sample(args.config)
+            cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl.name, "trajectories_per_gpu": n, "kmc_steps_per_traj_per_step": chunk,
+                       "active_at_end": active,
+                       "lattice": "x".join(str(v) for v in wl.sizes[0][:2]) if args.config != 3 else "uneven 16..256",
+                       "nproc": P, "backend": wl.backend, "rng": "philox4x32-10",
+                       "parallelism": "replicas%d" % dist.world, "graph": bool(args.graph),
+                       "l2": "resident state %.2f GB > L2, no flush" % (need / 1e9)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "bytes_per_kmc_step": bstep, "n_as": n_as, "n_occ": n_occ,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+    pool.close()
+    dist.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

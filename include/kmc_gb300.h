@@ -175,10 +175,20 @@ KMC_API int kmc_pool_get_tables(kmc_pool *pool, int32_t slot, int32_t *as1, int3
 /* Occupation counts of many slots at once, reduced on the device: out[i] holds the
  * [nspecies][spuck] counts of slots[i] (int64), with stride `stride` int64 per slot. */
 KMC_API int kmc_pool_occupation_counts(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride, int64_t *out);
+/* Results of many slots in one device gather and one copy: for slots[i], procstat
+ * (int64) and integ_rates (double) into rows of `stride` entries, kmc_time and
+ * kmc_step into times[i] / steps[i], status into status[i].  Any output may be null. */
+KMC_API int kmc_pool_get_results(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride,
+                                 int64_t *procstat, double *integ, double *times, int64_t *steps,
+                                 int32_t *status);
 /* Launch configuration used by kmc_pool_run: warps per block (1..32, 0 = automatic). */
 KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
 /* Device time (ms, CUDA events on the pool stream) of the last kmc_pool_run launch. */
 KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
+/* CUDA events on the pool stream around a region of work: start, then stop waits for
+ * the region to finish and returns its device time in ms. */
+KMC_API int kmc_pool_timer_start(kmc_pool *pool);
+KMC_API int kmc_pool_timer_stop(kmc_pool *pool, float *ms);
 /* Kernel launches issued by this pool since creation. */
 KMC_API int kmc_pool_launch_count(kmc_pool *pool, int64_t *count);
 

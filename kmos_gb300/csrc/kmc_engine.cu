@@ -422,6 +422,33 @@ __global__ void kmc_occupation_kernel(const SlotDev *slots, const ModelDev *mode
     out[(size_t)item * stride + i] = hist[(i / sp) * 32 + (i % sp)];
 }
 
+// ---------------------------------------------------------------- results gather
+struct ResultRow {
+  double kmc_time;
+  int64_t kmc_step;
+  int32_t status, pad;
+};
+
+__global__ void kmc_results_kernel(const SlotDev *slots, const int32_t *list, int32_t n, int32_t stride,
+                                   int64_t *procstat, double *integ, ResultRow *rows) {
+  const int item = blockIdx.x;
+  if (item >= n) return;
+  const SlotDev &S = slots[list[item]];
+  for (int i = threadIdx.x; i < stride; i += blockDim.x) {
+    const bool in = i < S.P;
+    procstat[(size_t)item * stride + i] = in ? S.procstat[i] : 0;
+    integ[(size_t)item * stride + i] = in ? S.integ[i] : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    ResultRow r;
+    r.kmc_time = S.kmc_time;
+    r.kmc_step = S.kmc_step;
+    r.status = S.status;
+    r.pad = 0;
+    rows[item] = r;
+  }
+}
+
 // ================================================================== host side
 namespace {
 
@@ -497,13 +524,16 @@ struct kmc_pool {
   double *d_adm_rates = nullptr;
   int32_t *d_adm_roff = nullptr;
   size_t adm_rates_cap = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
   bool timed = false;
   int64_t launches = 0;
   int warps_per_block = 4;
   int blocks_per_sm = 0;  // 0 = occupancy maximum
   std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> graphs;
   std::mutex mu;
+  char *d_res = nullptr;   // results gather buffers
+  char *h_res = nullptr;   // pinned
+  size_t res_cap = 0;
 };
 
 struct kmc_handle {
@@ -744,6 +774,8 @@ int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_p
   CK(cudaMalloc(&p->d_adm_roff, sizeof(int32_t) * max_slots));
   CK(cudaEventCreate(&p->ev0));
   CK(cudaEventCreate(&p->ev1));
+  CK(cudaEventCreate(&p->tev0));
+  CK(cudaEventCreate(&p->tev1));
   *out = p;
   return KMC_OK;
 }
@@ -761,8 +793,9 @@ int kmc_pool_destroy(kmc_pool *p) {
   for (auto &m : p->models) cudaFree(m.d_prog);
   cudaFree(p->arena); cudaFree(p->d_slots); cudaFree(p->d_models); cudaFree(p->d_list);
   cudaFree(p->d_steps); cudaFree(p->d_counter); cudaFree(p->d_cmd_out); cudaFreeHost(p->h_cancel);
+  cudaFree(p->d_res); cudaFreeHost(p->h_res);
   cudaFree(p->d_adm_list); cudaFree(p->d_adm_staged); cudaFree(p->d_adm_rates); cudaFree(p->d_adm_roff);
-  cudaEventDestroy(p->ev0); cudaEventDestroy(p->ev1);
+  cudaEventDestroy(p->ev0); cudaEventDestroy(p->ev1); cudaEventDestroy(p->tev0); cudaEventDestroy(p->tev1);
   cudaStreamDestroy(p->stream);
   delete p;
   return KMC_OK;
@@ -975,6 +1008,20 @@ int kmc_pool_last_kernel_ms(kmc_pool *p, float *ms) {
   return KMC_OK;
 }
 
+int kmc_pool_timer_start(kmc_pool *p) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  CK(cudaEventRecord(p->tev0, p->stream));
+  return KMC_OK;
+}
+
+int kmc_pool_timer_stop(kmc_pool *p, float *ms) {
+  if (!p || !ms) return fail(KMC_ERR_ARG, "bad arguments");
+  CK(cudaEventRecord(p->tev1, p->stream));
+  CK(cudaEventSynchronize(p->tev1));
+  CK(cudaEventElapsedTime(ms, p->tev0, p->tev1));
+  return KMC_OK;
+}
+
 int kmc_pool_launch_count(kmc_pool *p, int64_t *count) {
   if (!p || !count) return fail(KMC_ERR_ARG, "bad arguments");
   *count = p->launches;
@@ -1070,6 +1117,51 @@ int kmc_pool_occupation_counts(kmc_pool *p, const int32_t *slots, int32_t n, int
   CK(cudaFreeAsync(d_list, p->stream));
   CK(cudaFreeAsync(d_out, p->stream));
   CK(cudaStreamSynchronize(p->stream));
+  return KMC_OK;
+}
+
+int kmc_pool_get_results(kmc_pool *p, const int32_t *slots, int32_t n, int32_t stride, int64_t *procstat,
+                         double *integ, double *times, int64_t *steps, int32_t *status) {
+  if (!p || n < 1 || !slots || stride < 1) return fail(KMC_ERR_ARG, "bad arguments");
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+  }
+  CK(cudaSetDevice(p->device));
+  const size_t nps = (size_t)n * stride;
+  const size_t bytes = sizeof(int32_t) * n + nps * 16 + sizeof(ResultRow) * n + 256;
+  if (bytes > p->res_cap) {
+    CK(cudaStreamSynchronize(p->stream));
+    cudaFree(p->d_res);
+    cudaFreeHost(p->h_res);
+    CK(cudaMalloc(&p->d_res, bytes));
+    CK(cudaMallocHost(&p->h_res, bytes));
+    p->res_cap = bytes;
+  }
+  char *d = p->d_res;
+  int32_t *d_list = (int32_t *)d;
+  int64_t *d_ps = (int64_t *)(d + align_up(sizeof(int32_t) * n, 16));
+  double *d_ig = (double *)((char *)d_ps + nps * 8);
+  ResultRow *d_rows = (ResultRow *)((char *)d_ig + nps * 8);
+  const size_t used = (char *)(d_rows + n) - d;
+  memcpy(p->h_res, slots, sizeof(int32_t) * n);
+  CK(cudaMemcpyAsync(d_list, p->h_res, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  kmc_results_kernel<<<n, 64, 0, p->stream>>>(p->d_slots, d_list, n, stride, d_ps, d_ig, d_rows);
+  CK(cudaGetLastError());
+  p->launches++;
+  const size_t off = align_up(sizeof(int32_t) * n, 16);
+  CK(cudaMemcpyAsync(p->h_res + off, d + off, used - off, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  const int64_t *h_ps = (const int64_t *)(p->h_res + off);
+  const double *h_ig = (const double *)((const char *)h_ps + nps * 8);
+  const ResultRow *h_rows = (const ResultRow *)((const char *)h_ig + nps * 8);
+  if (procstat) memcpy(procstat, h_ps, nps * 8);
+  if (integ) memcpy(integ, h_ig, nps * 8);
+  for (int i = 0; i < n; i++) {
+    if (times) times[i] = h_rows[i].kmc_time;
+    if (steps) steps[i] = h_rows[i].kmc_step;
+    if (status) status[i] = h_rows[i].status;
+  }
   return KMC_OK;
 }
 

@@ -83,8 +83,11 @@ SIGNATURES = {
     "kmc_pool_get_lattice": (_i32, [_vp, _i32, _p32]),
     "kmc_pool_get_tables": (_i32, [_vp, _i32, _p32, _p32]),
     "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
+    "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
     "kmc_pool_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
+    "kmc_pool_timer_start": (_i32, [_vp]),
+    "kmc_pool_timer_stop": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_pool_launch_count": (_i32, [_vp, _p64]),
 }
 
@@ -378,6 +381,14 @@ class Pool:
         _check(load().kmc_pool_last_kernel_ms(self.h, ctypes.byref(ms)))
         return ms.value
 
+    def timer_start(self):
+        _check(load().kmc_pool_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = ctypes.c_float()
+        _check(load().kmc_pool_timer_stop(self.h, ctypes.byref(ms)))
+        return ms.value
+
     def launch_count(self) -> int:
         c = _i64()
         _check(load().kmc_pool_launch_count(self.h, ctypes.byref(c)))
@@ -418,6 +429,20 @@ class Pool:
         as2 = np.zeros(P * (volume + 1), np.int32)
         _check(load().kmc_pool_get_tables(self.h, int(slot), _ptr(as1, _i32), _ptr(as2, _i32)))
         return as1.reshape(P, volume + 1), as2.reshape(P, volume + 1)
+
+    def results(self, slots, stride: int):
+        """procstat [n, stride], integ [n, stride], kmc_time [n], kmc_step [n], status [n]
+        of many slots, gathered on the device and copied back in one transfer."""
+        slots = _a32(slots)
+        n = len(slots)
+        ps = np.zeros((n, stride), np.int64)
+        ig = np.zeros((n, stride), np.float64)
+        t = np.zeros(n, np.float64)
+        k = np.zeros(n, np.int64)
+        st = np.zeros(n, np.int32)
+        _check(load().kmc_pool_get_results(self.h, _ptr(slots, _i32), n, int(stride), _ptr(ps, _i64), _ptr(ig, _dbl),
+                                           _ptr(t, _dbl), _ptr(k, _i64), _ptr(st, _i32)))
+        return ps, ig, t, k, st
 
     def occupation_counts(self, slots, stride: int) -> np.ndarray:
         slots = _a32(slots)

@@ -82,7 +82,8 @@ typedef struct {
     uint64_t xs[4];
     uint32_t seed, traj;
     uint64_t ctr;
-    /* instrumentation: int32 book-keeping accesses and occupation accesses */
+    /* instrumentation: int32 avail_sites / nr_of_sites accesses made by run_proc_nr
+     * (add_proc, del_proc, can_do) and occupation reads/writes, as the Fortran does them */
     int64_t n_as, n_occ;
     int err;
 } oracle_t;
@@ -317,14 +318,12 @@ static void update_accum_rate(oracle_t *o)
     o->accum_rates[0] = (double)o->nr_of_sites[0] * o->rates[0];
     for (int i = 1; i < o->P; i++)
         o->accum_rates[i] = o->accum_rates[i - 1] + (double)o->nr_of_sites[i] * o->rates[i];
-    o->n_as += o->P;
 }
 
 static void update_integ_rate(oracle_t *o)
 {
     for (int i = 0; i < o->P; i++)
         o->integ_rates[i] = o->integ_rates[i] + (double)o->nr_of_sites[i] * o->rates[i] * o->kmc_time_step;
-    o->n_as += o->P;
 }
 
 static void update_clocks(oracle_t *o, double ran_time)
@@ -365,7 +364,6 @@ static int determine_procsite(oracle_t *o, double ran_proc, double ran_site, int
     if (idx > n) idx = n;
     *proc = p;
     *site = AS(o, p, idx, 1);
-    o->n_as += 2;
     return ORACLE_OK;
 }
 
