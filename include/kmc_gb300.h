@@ -183,6 +183,9 @@ KMC_API int kmc_pool_get_results(kmc_pool *pool, const int32_t *slots, int32_t n
                                  int32_t *status);
 /* Launch configuration used by kmc_pool_run: warps per block (1..32, 0 = automatic). */
 KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
+/* 1 (default): steps whose process has a fast stream run through the gather /
+ * replay / scatter path; 0: every step runs the serial interpreter (same results). */
+KMC_API int kmc_pool_set_fast_path(kmc_pool *pool, int32_t enable);
 /* Device time (ms, CUDA events on the pool stream) of the last kmc_pool_run launch. */
 KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
 /* CUDA events on the pool stream around a region of work: start, then stop waits for

@@ -28,6 +28,7 @@ struct ModelDev {
   const int32_t *prog;
   int32_t len, backend, P, nspecies, null_species, spuck, ngroups;
   int32_t off_proc, off_touch, off_groups, off_site_layer, off_site_default, max_k;
+  int32_t off_hot, hot_len, hot_grp, hot_tab, reach_x, reach_y, reach_z;
 };
 
 struct __align__(16) SlotDev {
@@ -291,6 +292,110 @@ __device__ inline void run_stream(View &v, int pos, int bx, int by, int bz) {
         return;
     }
   }
+}
+
+}  // namespace kmc
+
+// ==================================================================================
+// Fast step: gather -> parallel evaluation -> overlay replay -> scatter
+// ==================================================================================
+// A process's resolved fast stream (kmos_gb300/program.py) lists every lattice
+// coordinate it reads or writes as a slot; every condition reads a slot's value from
+// before the step or a constant, so the edits of one step are evaluated in parallel:
+//   1. lanes load every slot's species and check the old species of the replaces;
+//   2. lanes evaluate the edits (guarded dels, adds, nli dels / adds), and a ballot
+//      compacts the ones that happen into a list in program order;
+//   3. lanes load, for every del edit, avail_sites(p, site, 2) and the entry of
+//      avail_sites(p, :, 1) that the swap-remove of that del can read;
+//   4. lane 0 replays the edits in order with exactly the reference's add_proc /
+//      del_proc arithmetic on an on-chip overlay (open addressing) of the table
+//      entries written this step;
+//   5. lanes write the final lattice species and the overlay entries back.
+// The edits and their order are those of the serial interpreter above; only where
+// the values live differs.
+namespace kmc {
+
+constexpr int FAST_SLOTS = 128;
+constexpr int FAST_EDITS = 96;
+constexpr int OV_SIZE = 512;  // power of two, >= 4 keys per edit
+constexpr int FAST_MAXV = (1 << 23) - 1;
+
+enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
+
+struct FastSmem {
+  int32_t latv[FAST_SLOTS];
+  int32_t latsite[FAST_SLOTS];
+  int8_t ekind[FAST_EDITS];    // E_GDEL / E_DEL / E_ADD
+  int8_t eprev[FAST_EDITS];    // previous del edit of the same process, -1 if none
+  int16_t ep[FAST_EDITS];      // process, 0-based
+  int32_t esite[FAST_EDITS];   // target site
+  int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2)
+  int32_t eti[FAST_EDITS];     // tail index prefetched for this del edit
+  int32_t et[FAST_EDITS];      // prefetched avail_sites(p, eti, 1)
+  uint32_t okey[OV_SIZE];      // overlay of table entries written this step
+  int32_t oval[OV_SIZE];
+  uint16_t oused[OV_SIZE];
+};
+
+__device__ inline uint32_t ov_key(int table, int p, int index) {
+  return 1u + (((uint32_t)table << 31) | ((uint32_t)p << 23) | (uint32_t)index);
+}
+
+// lane 0 only
+__device__ inline int ov_find(const FastSmem &f, uint32_t key) {
+  uint32_t h = (key * 2654435761u) >> 23;
+  for (int probe = 0; probe < OV_SIZE; probe++) {
+    const uint32_t k = f.okey[h];
+    if (k == key) return (int)h;
+    if (k == 0) return -1 - (int)h;  // free slot where it would go
+    h = (h + 1) & (OV_SIZE - 1);
+  }
+  return -(OV_SIZE + 1);  // full
+}
+
+__device__ inline bool ov_set(FastSmem &f, int &nused, uint32_t key, int32_t val) {
+  const int i = ov_find(f, key);
+  if (i >= 0) { f.oval[i] = val; return true; }
+  if (i == -(OV_SIZE + 1) || nused >= OV_SIZE) return false;
+  const int slot = -1 - i;
+  f.okey[slot] = key;
+  f.oval[slot] = val;
+  f.oused[nused++] = (uint16_t)slot;
+  return true;
+}
+
+// The hot section of a model program: fast streams, group records and nli tables with
+// offsets relative to its start (shared memory when the block staged it).
+struct Hot {
+  const int32_t *h;
+  int grp, tab, nspecies;
+};
+
+__device__ inline int ref_value(int32_t ref, const int32_t *latv) { return ref >= 0 ? latv[ref] : -ref - 2; }
+
+// nli from slot references: table lookup when the program has one, else a member scan
+__device__ inline int nli_refs(const Hot &H, int g, const int32_t *refs, const int32_t *latv) {
+  const int32_t *rec = H.h + H.h[H.grp + g];
+  const int M = rec[0], K = rec[1];
+  const int toff = H.h[H.tab + g];
+  if (toff) {
+    const int base = H.nspecies + 1;
+    int idx = 0, mul = 1;
+    for (int k = 0; k < K; k++) {
+      const int s = ref_value(refs[k], latv);
+      idx += (s < 0 ? H.nspecies : s) * mul;
+      mul *= base;
+    }
+    return H.h[toff + idx];
+  }
+  int result = 0;
+  const int32_t *mem = rec + 2 + K;
+  for (int m = 0; m < M; m++, mem += 1 + K) {
+    bool ok = true;
+    for (int k = 0; k < K && ok; k++) ok = in_mask(ref_value(refs[k], latv), mem[1 + k]);
+    if (ok) result = mem[0];
+  }
+  return result;
 }
 
 }  // namespace kmc

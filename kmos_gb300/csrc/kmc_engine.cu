@@ -47,6 +47,153 @@ using namespace kmc;
 
 #define KMC_MAXK 16
 
+template <int NP>
+struct WarpSmem {
+  double rates[NP * 32];
+  double accum[NP * 32];
+  double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
+  int32_t ns[NP * 32];
+  int16_t lastdel[NP * 32];
+  FastSmem f;
+};
+
+// One kMC step's run_proc_nr through the gather / evaluate / replay / scatter path.
+// All lanes call it and get the status.
+template <int NP>
+__device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
+                         int lane) {
+  FastSmem &f = sm.f;
+  const int nlat = fs[0], nchk = fs[1], nwr = fs[2], nedit = fs[3];
+  const int32_t *coords = fs + 4;
+  const int32_t *chk = coords + nlat;
+  const int32_t *wr = chk + 2 * nchk;
+  const int32_t *eoff = wr + 2 * nwr;
+  const int stride = v.stride;
+  const unsigned lt = (1u << lane) - 1u;
+  // 1. gather every slot; check the old species of first replaces
+  for (int i = lane; i < nlat; i += 32) {
+    const int s = v.g.site(bx, by, bz, coords[i]);
+    f.latsite[i] = s;
+    f.latv[i] = v.lat[s - 1];
+  }
+  __syncwarp();
+  bool bad = false;
+  for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);
+  if (__any_sync(0xffffffffu, bad)) return ST_SPECIES;
+  // 2. evaluate every edit in parallel; compact the ones that happen, in order
+  int ne = 0;
+  for (int r = 0; r < nedit; r += 32) {
+    const int k = r + lane;
+    bool on = false;
+    int kind = E_GDEL, p = 0, site = 0;
+    if (k < nedit) {
+      const int32_t *e = fs + eoff[k];
+      const uint32_t h = (uint32_t)e[0];
+      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+      if (op == 2) {
+        on = true; p = arg;
+      } else if (op == 3) {
+        on = true;
+        for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], f.latv), e[2 + cnt + c]);
+        p = arg; kind = E_ADD;
+      } else {
+        p = nli_refs(H, arg, e + 2, f.latv);
+        on = p != 0;
+        kind = op == 4 ? E_DEL : E_ADD;
+      }
+      if (on) site = v.g.site(bx, by, bz, e[1]);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, on);
+    if (on) {
+      const int pos = ne + __popc(b & lt);
+      f.ekind[pos] = (int8_t)kind;
+      f.ep[pos] = (int16_t)(p - 1);
+      f.esite[pos] = site;
+    }
+    ne += __popc(b);
+  }
+  __syncwarp();
+  // chain the del edits of each process: the k-th del of p can read as1(p, n0 - k)
+  if (lane == 0) {
+    for (int k = 0; k < ne; k++) {
+      if (f.ekind[k] == E_ADD) continue;
+      const int p = f.ep[k];
+      const int prev = sm.lastdel[p];
+      f.eprev[k] = (int8_t)prev;
+      f.eti[k] = prev < 0 ? sm.ns[p] : f.eti[prev] - 1;
+      sm.lastdel[p] = (int16_t)k;
+    }
+    for (int k = 0; k < ne; k++)
+      if (f.ekind[k] != E_ADD) sm.lastdel[f.ep[k]] = -1;
+  }
+  __syncwarp();
+  // 3. prefetch avail_sites(p, site, 2) and the tail entry of every del edit
+  for (int k = lane; k < ne; k += 32) {
+    if (f.ekind[k] == E_ADD) continue;
+    const size_t row = (size_t)f.ep[k] * stride;
+    f.em[k] = v.as2[row + f.esite[k]];
+    const int ti = f.eti[k];
+    f.et[k] = ti >= 1 ? v.as1[row + ti] : 0;
+  }
+  __syncwarp();
+  // 4. replay add_proc / del_proc in program order on the overlay
+  int err = ST_OK, nused = 0;
+  if (lane == 0) {
+    for (int k = 0; k < ne && err == ST_OK; k++) {
+      const int kind = f.ekind[k], p = f.ep[k], site = f.esite[k];
+      if (kind == E_ADD) {
+        const int n = sm.ns[p] + 1;
+        sm.ns[p] = n;
+        if (!ov_set(f, nused, ov_key(0, p, n), site) || !ov_set(f, nused, ov_key(1, p, site), n)) err = ST_TABLE;
+        continue;
+      }
+      int i = ov_find(f, ov_key(1, p, site));
+      const int m = i >= 0 ? f.oval[i] : f.em[k];
+      if (m == 0) {
+        if (kind == E_DEL) err = ST_TABLE;  // nli names a process that is not there
+        continue;
+      }
+      const int n = sm.ns[p];
+      bool ok = true;
+      if (m < n) {
+        int last;
+        i = ov_find(f, ov_key(0, p, n));
+        if (i >= 0) {
+          last = f.oval[i];
+        } else {
+          int j = k;
+          while (j >= 0 && f.eti[j] != n) j = f.eprev[j];
+          last = j >= 0 ? f.et[j] : v.as1[(size_t)p * stride + n];
+        }
+        ok = ov_set(f, nused, ov_key(0, p, m), last) && ov_set(f, nused, ov_key(0, p, n), 0) &&
+             ov_set(f, nused, ov_key(1, p, last), m);
+      } else {
+        ok = ov_set(f, nused, ov_key(0, p, m), 0);
+      }
+      ok = ok && ov_set(f, nused, ov_key(1, p, site), 0);
+      if (!ok) err = ST_TABLE;
+      sm.ns[p] = n - 1;
+    }
+  }
+  err = __shfl_sync(0xffffffffu, err, 0);
+  nused = __shfl_sync(0xffffffffu, nused, 0);
+  __syncwarp();
+  // 5. scatter the overlay and the final species of the replaced slots
+  for (int i = lane; i < nused; i += 32) {
+    const int h = f.oused[i];
+    const uint32_t key = f.okey[h] - 1u;
+    if (err == ST_OK) {
+      const size_t at = (size_t)((key >> 23) & 0xFF) * stride + (key & 0x7FFFFF);
+      if (key >> 31) v.as2[at] = f.oval[h]; else v.as1[at] = f.oval[h];
+    }
+    f.okey[h] = 0u;
+  }
+  if (err == ST_OK)
+    for (int i = lane; i < nwr; i += 32) v.lat[f.latsite[wr[2 * i]] - 1] = (int8_t)wr[2 * i + 1];
+  __syncwarp();
+  return err;
+}
+
 // --------------------------------------------------------------------- run kernel
 struct RunArgs {
   SlotDev *slots;
@@ -57,13 +204,9 @@ struct RunArgs {
   int32_t *counter;
   int32_t *trace;                 // (proc, site) per step of a single-slot run, or null
   const volatile int32_t *cancel; // host-mapped cancel flag, or null
-};
-
-template <int NP>
-struct WarpSmem {
-  double rates[NP * 32];
-  double accum[NP * 32];
-  int32_t ns[NP * 32];
+  int32_t fast;                   // 1: use the gather / replay path where it applies
+  int32_t model;                  // every listed slot runs this model
+  int32_t stage_words;            // hot-section words copied to shared memory (0 = read it from global)
 };
 
 template <int NP>
@@ -71,7 +214,22 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw)[wib];
+  const ModelDev M = a.models[a.model];
+  const int P = M.P;
+  // stage the model's hot section (fast streams, group records, nli tables)
+  int32_t *hot_s = reinterpret_cast<int32_t *>(smem_raw);
+  const int stage = a.stage_words;
+  for (int i = threadIdx.x; i < stage; i += blockDim.x) hot_s[i] = M.prog[M.off_hot + i];
+  Hot H;
+  H.h = stage ? hot_s : M.prog + M.off_hot;
+  H.grp = M.hot_grp;
+  H.tab = M.hot_tab;
+  H.nspecies = M.nspecies;
+  const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
+  WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw + hot_bytes)[wib];
+  for (int i = lane; i < OV_SIZE; i += 32) sm.f.okey[i] = 0u;
+  for (int i = lane; i < NP * 32; i += 32) sm.lastdel[i] = -1;
+  __syncthreads();
 
   for (;;) {
     int item = 0;
@@ -81,9 +239,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
     const int slot = a.list[item];
     const int64_t nsteps = a.steps[item];
     SlotDev &S = a.slots[slot];
-    if (S.status != ST_OK) continue;
-    const ModelDev M = a.models[S.model];
-    const int P = M.P;
+    if (S.status != ST_OK || S.model != a.model) continue;
     const int stride = S.V + 1;
 
     View v;
@@ -99,18 +255,27 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
     v.off_groups = M.off_groups;
     v.collect = false;
 
+    const bool fast_ok = a.fast && M.off_hot != 0 && S.V <= FAST_MAXV && P <= 256 &&
+                         (M.reach_x == 0 || S.X > 2 * M.reach_x) && (M.reach_y == 0 || S.Y > 2 * M.reach_y) &&
+                         (M.reach_z == 0 || S.Z > 2 * M.reach_z);
     double ig[NP];
     int64_t ps[NP];
+    int32_t n0[NP];
 #pragma unroll
     for (int j = 0; j < NP; j++) {
       const int i = lane + 32 * j;
       if (i < P) {
-        sm.rates[i] = S.rates[i];
+        const double r = S.rates[i];
+        const int n = S.nsites[i];
+        sm.rates[i] = r;
         sm.accum[i] = S.accum[i];
-        sm.ns[i] = S.nsites[i];
+        sm.ns[i] = n;
+        sm.term[i] = __dmul_rn((double)n, r);
+        n0[j] = n;
         ig[j] = S.integ[i];
         ps[j] = S.procstat[i];
       } else {
+        n0[j] = 0;
         ig[j] = 0.0;
         ps[j] = 0;
       }
@@ -129,13 +294,15 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       double ran_time, ran_proc, ran_site;
       draw3(rng_kind, rng, seed, traj, ran_time, ran_proc, ran_site);
 
-      // update_accum_rate from the first stale entry (entries before it are unchanged
-      // sums of unchanged terms, so the result equals a full recompute bit for bit)
+      // update_accum_rate from the first stale entry: entries before it are the same
+      // sums of the same terms, so the result equals a full recompute bit for bit
       if (lane == 0 && from < P) {
         double acc = from > 0 ? sm.accum[from - 1] : 0.0;
-        for (int i = from; i < P; i++) {
-          const double term = __dmul_rn((double)sm.ns[i], sm.rates[i]);
-          acc = (i == 0) ? term : __dadd_rn(acc, term);
+        int i = from;
+        if (i == 0) { acc = sm.term[0]; sm.accum[0] = acc; i = 1; }
+#pragma unroll 4
+        for (; i < P; i++) {
+          acc = __dadd_rn(acc, sm.term[i]);
           sm.accum[i] = acc;
         }
       }
@@ -153,7 +320,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
 #pragma unroll
       for (int j = 0; j < NP; j++) {
         const int i = lane + 32 * j;
-        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(__dmul_rn((double)sm.ns[i], sm.rates[i]), dt));
+        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(sm.term[i], dt));
       }
 
       // determine_procsite
@@ -176,21 +343,42 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
         if (proc == lane + 32 * j) ps[j] += 1;  // increment_procstat
 
       int err = ST_OK;
+      const int fs_off = fast_ok ? H.h[proc] : 0;
+      int site = 0;
       if (lane == 0) {
-        const int site = v.as1[(size_t)proc * stride + idx];
+        site = v.as1[(size_t)proc * stride + idx];
         if (a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
-        int bx, by, bz, bn;
-        v.g.coords(site, bx, by, bz, bn);
-        v.minp = P;
-        v.err = ST_OK;
-        run_stream(v, M.prog[M.off_proc + proc], bx, by, bz);
-        err = v.err;
-        from = v.minp;
       }
-      from = __shfl_sync(0xffffffffu, from, 0);
-      err = __shfl_sync(0xffffffffu, err, 0);
-      __syncwarp();
+      site = __shfl_sync(0xffffffffu, site, 0);
+      int bx, by, bz, bn;
+      v.g.coords(site, bx, by, bz, bn);
+      if (fs_off) {
+        err = fast_step<NP>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
+      } else {
+        if (lane == 0) {
+          v.minp = P;
+          v.err = ST_OK;
+          run_stream(v, M.prog[M.off_proc + proc], bx, by, bz);
+          err = v.err;
+        }
+        err = __shfl_sync(0xffffffffu, err, 0);
+        __syncwarp();
+      }
       if (err) { status = err; break; }
+      // refresh the terms of processes whose nr_of_sites changed; accum restarts at
+      // the first of them
+      int first = P;
+#pragma unroll
+      for (int j = 0; j < NP; j++) {
+        const int i = lane + 32 * j;
+        const int nn = i < P ? sm.ns[i] : 0;
+        const bool ch = i < P && nn != n0[j];
+        if (ch) { sm.term[i] = __dmul_rn((double)nn, sm.rates[i]); n0[j] = nn; }
+        const unsigned b = __ballot_sync(0xffffffffu, ch);
+        if (first == P && b) first = 32 * j + __ffs(b) - 1;
+      }
+      from = first;
+      __syncwarp();
     }
 
 #pragma unroll
@@ -490,6 +678,7 @@ struct GraphKeyHash {
   }
 };
 struct GraphEntry {
+  int64_t nlaunch = 0;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   int32_t *d_list = nullptr;
@@ -528,6 +717,7 @@ struct kmc_pool {
   bool timed = false;
   int64_t launches = 0;
   int warps_per_block = 4;
+  int fast_path = 1;
   int blocks_per_sm = 0;  // 0 = occupancy maximum
   std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> graphs;
   std::mutex mu;
@@ -656,6 +846,75 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
     return fail(KMC_ERR_PROGRAM, "bad site tables");
   for (int n = 0; n < m->spuck; n++)
     if (!species_ok(prog[m->off_site_default + n])) return fail(KMC_ERR_PROGRAM, "bad default species");
+  // hot section: fast streams with slot references below nlat, known edit kinds,
+  // in-range processes / groups / species, edit offsets inside the stream
+  m->off_hot = prog[21];
+  m->hot_len = prog[20];
+  m->hot_grp = prog[17];
+  m->hot_tab = prog[18];
+  m->reach_x = prog[19] & 0xFF; m->reach_y = (prog[19] >> 8) & 0xFF; m->reach_z = (prog[19] >> 16) & 0xFF;
+  if (m->off_hot <= 0 || m->hot_len <= m->P || m->off_hot + m->hot_len > len) {
+    m->off_hot = 0;
+  } else {
+    const int32_t *hot = prog + m->off_hot;
+    const int hl = m->hot_len, G = std::max(m->ngroups, 1);
+    if (m->hot_grp < m->P + 1 || m->hot_grp + G > hl || m->hot_tab < m->P + 1 || m->hot_tab + G > hl)
+      return fail(KMC_ERR_PROGRAM, "bad hot-section tables");
+    for (int g = 0; g < m->ngroups; g++) {
+      const int off = hot[m->hot_grp + g];
+      if (off <= 0 || off + 2 > hl) return fail(KMC_ERR_PROGRAM, "bad hot group record");
+      const int M = hot[off], K = hot[off + 1];
+      if (K > KMC_MAXK || K < 0 || M < 0 || off + 2 + K + M * (1 + K) > hl) return fail(KMC_ERR_PROGRAM, "bad hot group record");
+      for (int mm = 0; mm < M; mm++) {
+        const int pid = hot[off + 2 + K + mm * (1 + K)];
+        if (pid < 1 || pid > m->P) return fail(KMC_ERR_PROGRAM, "bad group member");
+      }
+      const int toff = hot[m->hot_tab + g];
+      if (toff) {
+        int64_t size = 1;
+        for (int k = 0; k < K; k++) size *= (m->nspecies + 1);
+        if (toff < 0 || toff + size > hl) return fail(KMC_ERR_PROGRAM, "nli table overruns program");
+        for (int64_t i = 0; i < size; i++)
+          if (hot[toff + i] < 0 || hot[toff + i] > m->P) return fail(KMC_ERR_PROGRAM, "bad nli table entry");
+      }
+    }
+    for (int i = 0; i < m->P; i++) {
+      const int off = hot[i];
+      if (off == 0) continue;
+      if (off < m->P + 1 || off + 4 > hl) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
+      const int nlat = hot[off], nchk = hot[off + 1], nwr = hot[off + 2], nedit = hot[off + 3];
+      if (nlat < 0 || nlat > FAST_SLOTS || nchk < 0 || nchk > nlat || nwr < 0 || nwr > nlat || nedit < 0 ||
+          nedit > FAST_EDITS)
+        return fail(KMC_ERR_PROGRAM, "fast stream exceeds the on-chip limits");
+      const int head = 4 + nlat + 2 * nchk + 2 * nwr + nedit;
+      if (off + head > hl) return fail(KMC_ERR_PROGRAM, "fast stream overruns program");
+      for (int c = 0; c < nlat; c++) if (!coord_ok(hot[off + 4 + c])) return fail(KMC_ERR_PROGRAM, "bad fast slot");
+      const int32_t *chk = hot + off + 4 + nlat, *wr = chk + 2 * nchk, *eo = wr + 2 * nwr;
+      for (int c = 0; c < nchk; c++) if (chk[2 * c] < 0 || chk[2 * c] >= nlat) return fail(KMC_ERR_PROGRAM, "bad check");
+      for (int c = 0; c < nwr; c++)
+        if (wr[2 * c] < 0 || wr[2 * c] >= nlat || !species_ok(wr[2 * c + 1])) return fail(KMC_ERR_PROGRAM, "bad write");
+      auto ref_ok = [&](int32_t r) { return r >= 0 ? r < nlat : species_ok(-r - 2); };
+      for (int k = 0; k < nedit; k++) {
+        const int e = off + eo[k];
+        if (eo[k] < head || e + 2 > hl) return fail(KMC_ERR_PROGRAM, "bad edit offset");
+        const uint32_t h = (uint32_t)hot[e];
+        const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+        if (!coord_ok(hot[e + 1])) return fail(KMC_ERR_PROGRAM, "bad edit target");
+        if (op == 2) {
+          if (arg < 1 || arg > m->P) return fail(KMC_ERR_PROGRAM, "bad edit process");
+        } else if (op == 3) {
+          if (arg < 1 || arg > m->P || e + 2 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad add edit");
+          for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad add ref");
+        } else if (op == 4 || op == 5) {
+          if (arg >= m->ngroups || e + 2 + cnt > hl || cnt != hot[hot[m->hot_grp + arg] + 1])
+            return fail(KMC_ERR_PROGRAM, "bad nli edit");
+          for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad nli ref");
+        } else {
+          return fail(KMC_ERR_PROGRAM, "bad edit kind");
+        }
+      }
+    }
+  }
   m->max_k = 0;
   for (int g = 0; g < m->ngroups; g++) {
     const int off = prog[m->off_groups + g];
@@ -669,44 +928,111 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
       const int pid = prog[off + 2 + K + mm * (1 + K)];
       if (pid < 1 || pid > m->P) return fail(KMC_ERR_PROGRAM, "bad group member");
     }
+
     m->max_k = std::max(m->max_k, K);
   }
   return KMC_OK;
 }
 
-int launch_run(kmc_pool *p, const int32_t *d_list, const int64_t *d_steps, int n, int32_t *d_trace) {
+constexpr int STAGE_MAX_WORDS = 16384;  // hot sections up to 64 KB go to shared memory
+
+// One launch of the run kernel: every listed slot runs `model`.
+struct LaunchPlan {
+  int model, first, count, blocks, threads, np;
+  size_t smem;
   RunArgs a;
-  a.slots = p->d_slots;
-  a.models = p->d_models;
-  a.list = d_list;
-  a.steps = d_steps;
-  a.n = n;
-  a.counter = p->d_counter;
-  a.trace = d_trace;
-  a.cancel = p->d_cancel;
-  int maxP = 0;
-  for (auto &m : p->models) maxP = std::max(maxP, m.dev.P);
+};
+
+template <int NP>
+int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   const int wpb = p->warps_per_block;
-  const int threads = 32 * wpb;
-  CK(cudaMemsetAsync(p->d_counter, 0, sizeof(int32_t), p->stream));
+  L.threads = 32 * wpb;
+  L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
+  L.np = NP;
+  CK(cudaFuncSetAttribute(kmc_run_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
   int bps = p->blocks_per_sm;
-  auto go = [&](auto kern, size_t smem_per_warp) -> int {
-    const size_t smem = smem_per_warp * wpb;  // at most 8 x 5 KB: below the 48 KB default
-    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, threads, smem));
-    if (bps <= 0) bps = 1;
-    int blocks = std::min((n + wpb - 1) / wpb, p->num_sms * bps);
-    if (blocks < 1) blocks = 1;
-    kern<<<blocks, threads, smem, p->stream>>>(a);
+  if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP>, L.threads, L.smem));
+  if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
+  L.blocks = std::max(1, std::min((L.count + wpb - 1) / wpb, p->num_sms * bps));
+  return KMC_OK;
+}
+
+// Sorts the run list by model (stable) into ls / st and plans one launch per model.
+int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std::vector<int32_t> &ls,
+             std::vector<int64_t> &st, std::vector<LaunchPlan> &plans) {
+  std::vector<int32_t> order(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return p->slots[slots[x]].dev.model < p->slots[slots[y]].dev.model; });
+  ls.resize(n);
+  st.resize(n);
+  for (int i = 0; i < n; i++) { ls[i] = slots[order[i]]; st[i] = steps[order[i]]; }
+  plans.clear();
+  int i = 0;
+  while (i < n) {
+    const int model = p->slots[ls[i]].dev.model;
+    int j = i;
+    while (j < n && p->slots[ls[j]].dev.model == model) j++;
+    LaunchPlan L;
+    L.model = model;
+    L.first = i;
+    L.count = j - i;
+    const ModelDev &md = p->models[model].dev;
+    RunArgs &a = L.a;
+    a.slots = p->d_slots;
+    a.models = p->d_models;
+    a.n = L.count;
+    a.counter = p->d_counter + plans.size();
+    a.cancel = p->d_cancel;
+    a.fast = p->fast_path;
+    a.model = model;
+    a.stage_words = (md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
+    const size_t hot_bytes = ((size_t)a.stage_words * 4 + 15) / 16 * 16;
+    int rc;
+    if (md.P <= 32) rc = plan_kernel<1>(p, L, hot_bytes);
+    else if (md.P <= 64) rc = plan_kernel<2>(p, L, hot_bytes);
+    else if (md.P <= 128) rc = plan_kernel<4>(p, L, hot_bytes);
+    else rc = plan_kernel<8>(p, L, hot_bytes);
+    if (rc) return rc;
+    plans.push_back(L);
+    i = j;
+  }
+  if ((int)plans.size() > p->max_models) return fail(KMC_ERR_ARG, "too many models in one run");
+  return KMC_OK;
+}
+
+// Issues the planned launches on the pool stream (capturable: no host copies).
+int issue_run(kmc_pool *p, std::vector<LaunchPlan> &plans, const int32_t *d_list, const int64_t *d_steps,
+              int32_t *d_trace) {
+  CK(cudaMemsetAsync(p->d_counter, 0, sizeof(int32_t) * plans.size(), p->stream));
+  for (auto &L : plans) {
+    L.a.list = d_list + L.first;
+    L.a.steps = d_steps + L.first;
+    L.a.trace = d_trace;
+    switch (L.np) {
+      case 1: kmc_run_kernel<1><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
+      case 2: kmc_run_kernel<2><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
+      case 4: kmc_run_kernel<4><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
+      default: kmc_run_kernel<8><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
+    }
     CK(cudaGetLastError());
-    return KMC_OK;
-  };
-  int rc;
-  if (maxP <= 32) rc = go(kmc_run_kernel<1>, sizeof(WarpSmem<1>));
-  else if (maxP <= 64) rc = go(kmc_run_kernel<2>, sizeof(WarpSmem<2>));
-  else if (maxP <= 128) rc = go(kmc_run_kernel<4>, sizeof(WarpSmem<4>));
-  else rc = go(kmc_run_kernel<8>, sizeof(WarpSmem<8>));
-  if (rc == KMC_OK) p->launches++;
-  return rc;
+    p->launches++;
+  }
+  return KMC_OK;
+}
+
+// Plans, copies the sorted list to d_list / d_steps and issues the launches.
+int launch_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, int32_t *d_list, int64_t *d_steps,
+               int32_t *d_trace) {
+  std::vector<int32_t> ls;
+  std::vector<int64_t> st;
+  std::vector<LaunchPlan> plans;
+  int rc = plan_run(p, slots, steps, n, ls, st, plans);
+  if (rc) return rc;
+  // pageable sources: the copies have read them when cudaMemcpyAsync returns
+  CK(cudaMemcpyAsync(d_list, ls.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(d_steps, st.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, p->stream));
+  return issue_run(p, plans, d_list, d_steps, d_trace);
 }
 
 int read_slot(kmc_pool *p, int slot, SlotDev *out) {
@@ -764,7 +1090,7 @@ int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_p
   CK(cudaMalloc(&p->d_models, sizeof(ModelDev) * p->max_models));
   CK(cudaMalloc(&p->d_list, sizeof(int32_t) * max_slots));
   CK(cudaMalloc(&p->d_steps, sizeof(int64_t) * max_slots));
-  CK(cudaMalloc(&p->d_counter, sizeof(int32_t)));
+  CK(cudaMalloc(&p->d_counter, sizeof(int32_t) * p->max_models));
   CK(cudaMalloc(&p->d_cmd_out, sizeof(int32_t) * 4));
   CK(cudaHostAlloc(&p->h_cancel, sizeof(int32_t), cudaHostAllocMapped));
   *p->h_cancel = 0;
@@ -941,10 +1267,8 @@ int kmc_pool_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int32_
   }
   CK(cudaSetDevice(p->device));
   *p->h_cancel = 0;
-  CK(cudaMemcpyAsync(p->d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
-  CK(cudaMemcpyAsync(p->d_steps, steps, sizeof(int64_t) * n, cudaMemcpyHostToDevice, p->stream));
   CK(cudaEventRecord(p->ev0, p->stream));
-  int rc = launch_run(p, p->d_list, p->d_steps, n, nullptr);
+  int rc = launch_run(p, slots, steps, n, p->d_list, p->d_steps, nullptr);
   CK(cudaEventRecord(p->ev1, p->stream));
   p->timed = true;
   return rc;
@@ -963,16 +1287,21 @@ int kmc_pool_run_graph(kmc_pool *p, const int32_t *slots, int64_t steps, int32_t
     GraphEntry e;
     CK(cudaMalloc(&e.d_list, sizeof(int32_t) * n));
     CK(cudaMalloc(&e.d_steps, sizeof(int64_t) * n));
-    std::vector<int64_t> st(n, steps);
-    CK(cudaMemcpy(e.d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice));
+    std::vector<int64_t> st0(n, steps), st;
+    std::vector<int32_t> ls;
+    std::vector<LaunchPlan> plans;
+    // sort, set kernel attributes and query occupancy outside the capture
+    int rc = plan_run(p, slots, st0.data(), n, ls, st, plans);
+    if (rc) return rc;
+    CK(cudaMemcpy(e.d_list, ls.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e.d_steps, st.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
-    // set the kernel attributes and occupancy outside capture
     CK(cudaStreamSynchronize(p->stream));
     CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t before = p->launches;
-    int rc = launch_run(p, e.d_list, e.d_steps, n, nullptr);
+    rc = issue_run(p, plans, e.d_list, e.d_steps, nullptr);
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    e.nlaunch = p->launches - before;
     p->launches = before;
     if (rc) return rc;
     if (ce != cudaSuccess) return fail(KMC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
@@ -985,7 +1314,7 @@ int kmc_pool_run_graph(kmc_pool *p, const int32_t *slots, int64_t steps, int32_t
   CK(cudaGraphLaunch(it->second.exec, p->stream));
   CK(cudaEventRecord(p->ev1, p->stream));
   p->timed = true;
-  p->launches++;
+  p->launches += it->second.nlaunch;
   return KMC_OK;
 }
 
@@ -1032,6 +1361,19 @@ int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per
   if (!p || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
   p->warps_per_block = warps_per_block ? warps_per_block : 4;
   p->blocks_per_sm = blocks_per_sm;
+  for (auto &kv : p->graphs) {
+    cudaGraphExecDestroy(kv.second.exec);
+    cudaGraphDestroy(kv.second.graph);
+    cudaFree(kv.second.d_list);
+    cudaFree(kv.second.d_steps);
+  }
+  p->graphs.clear();
+  return KMC_OK;
+}
+
+int kmc_pool_set_fast_path(kmc_pool *p, int32_t enable) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  p->fast_path = enable ? 1 : 0;
   for (auto &kv : p->graphs) {
     cudaGraphExecDestroy(kv.second.exec);
     cudaGraphDestroy(kv.second.graph);
@@ -1256,10 +1598,8 @@ int kmc_trace_steps(kmc_handle *h, int64_t n, int32_t *out) {
     CK(cudaMalloc(&h->d_trace, sizeof(int32_t) * 2 * n));
     h->trace_cap = n;
   }
-  CK(cudaMemcpyAsync(p->d_list, &h->slot, sizeof(int32_t), cudaMemcpyHostToDevice, p->stream));
-  CK(cudaMemcpyAsync(p->d_steps, &n, sizeof(int64_t), cudaMemcpyHostToDevice, p->stream));
   *p->h_cancel = 0;
-  int rc = launch_run(p, p->d_list, p->d_steps, 1, h->d_trace);
+  int rc = launch_run(p, &h->slot, &n, 1, p->d_list, p->d_steps, h->d_trace);
   if (rc) return rc;
   CK(cudaMemcpyAsync(out, h->d_trace, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, p->stream));
   return finish_run(h);

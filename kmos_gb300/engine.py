@@ -85,6 +85,7 @@ SIGNATURES = {
     "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
     "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
+    "kmc_pool_set_fast_path": (_i32, [_vp, _i32]),
     "kmc_pool_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_pool_timer_start": (_i32, [_vp]),
     "kmc_pool_timer_stop": (_i32, [_vp, _P(ctypes.c_float)]),
@@ -292,6 +293,7 @@ class Pool:
         self.h = h
         self.models: List[np.ndarray] = []
         self.slot_model = {}
+        self.slot_volume = {}
 
     def close(self):
         if getattr(self, "h", None):
@@ -346,13 +348,16 @@ class Pool:
         _check(load().kmc_pool_admit_many(self.h, n, _ptr(mids, _i32), _ptr(dims, _i32), int(layer),
                                           _ptr(seeds, _i32), int(rng), _ptr(trajs, _u32), _ptr(flat, _dbl),
                                           _ptr(offs, _i32), _ptr(slots, _i32)))
-        for s, m in zip(slots, model_ids):
+        for s, m, sz in zip(slots, model_ids, sizes):
             self.slot_model[int(s)] = int(m)
+            d = _dims3(sz)
+            self.slot_volume[int(s)] = int(d[0]) * int(d[1]) * int(d[2]) * int(self.models[int(m)][6])
         return [int(s) for s in slots]
 
     def release(self, slot: int):
         _check(load().kmc_pool_release(self.h, int(slot)))
         self.slot_model.pop(int(slot), None)
+        self.slot_volume.pop(int(slot), None)
 
     def run(self, slots, steps, sync: bool = True):
         slots = _a32(slots)
@@ -375,6 +380,9 @@ class Pool:
 
     def set_launch(self, warps_per_block: int = 0, blocks_per_sm: int = 0):
         _check(load().kmc_pool_set_launch(self.h, int(warps_per_block), int(blocks_per_sm)))
+
+    def set_fast_path(self, enable: bool):
+        _check(load().kmc_pool_set_fast_path(self.h, 1 if enable else 0))
 
     def last_kernel_ms(self) -> float:
         ms = ctypes.c_float()
@@ -418,12 +426,16 @@ class Pool:
     def nr_of_sites(self, slot):
         return self._pvec(load().kmc_pool_get_nr_of_sites, slot, np.int32, _i32)
 
-    def lattice(self, slot, volume: int):
-        out = np.zeros(volume, np.int32)
+    def volume(self, slot) -> int:
+        return self.slot_volume[int(slot)]
+
+    def lattice(self, slot, volume: Optional[int] = None):
+        out = np.zeros(self.volume(slot), np.int32)
         _check(load().kmc_pool_get_lattice(self.h, int(slot), _ptr(out, _i32)))
         return out
 
-    def tables(self, slot, volume: int):
+    def tables(self, slot, volume: Optional[int] = None):
+        volume = self.volume(slot)
         P = self.nproc(self.slot_model[int(slot)])
         as1 = np.zeros(P * (volume + 1), np.int32)
         as2 = np.zeros(P * (volume + 1), np.int32)

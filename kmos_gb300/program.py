@@ -37,6 +37,11 @@ Program layout (all int32; see ``include/kmc_gb300.h`` for the authoritative tab
     [14] off_site_default -> spuck default species ids
     [15] total length
     [16] max ops executed by one process (sizing hint)
+    [17] hot-relative offset of the group-record offsets (ngroups entries)
+    [18] hot-relative offset of the nli-table offsets (ngroups entries, 0 = none)
+    [19] reach          -> largest |dx|, |dy|, |dz| of the fast streams, one byte each
+    [20] hot section length, [21] off_hot (the hot section starts with the nproc+1
+         hot-relative fast-stream offsets; 0 = no fast stream for that process)
 
 Ops (first word: op | count << 8 | arg << 16; coordinates packed as four signed
 bytes dx, dy, dz, n with n the absolute 1-based site index)::
@@ -50,6 +55,34 @@ bytes dx, dy, dz, n with n the absolute 1-based site index)::
 
 Group record: ``[nmembers M, ncoords K, coord * K, (proc, mask * K) * M]``.
 Species masks have bit ``s`` for species ``s`` and bit 31 for the null species -1.
+
+Fast streams and the hot section (header words 17-22).  For the engine's gather /
+evaluate / replay / scatter step every process stream is also emitted in a resolved
+form.  The stream lists the distinct lattice coordinates it can touch (relative to the
+base cell, every nli coordinate shifted by its op offset) as *slots*.  Because
+``replace_species`` writes a constant species, the value any later read of a replaced
+slot sees is known here: conditions on replaced slots are decided at compile time (an
+add that can never fire is dropped), and every remaining read is of the value the slot
+had before the step.  All edits of a step can therefore be evaluated in parallel::
+
+    [nlat, nchk, nwr, nedit, coord * nlat, (slot, old_mask) * nchk,
+     (slot, species) * nwr, edit_offset * nedit, edits...]
+    edit  [kind | cnt << 8 | arg << 16, target coord, ref * cnt, (mask * cnt for adds)]
+    kind  2 = guarded del (arg = proc), 3 = add (arg = proc, cnt conditions),
+          4 = nli del, 5 = nli add (arg = group, cnt = the group's K coordinates)
+    ref   >= 0: slot index (value before the step); < 0: constant species -ref-2
+
+``chk`` are the old-species checks of first replaces (later ones are checked here),
+``wr`` the final species of every replaced slot.  Edit offsets are relative to the
+stream start.  The hot section (header word 21) holds the fast-stream offset table,
+the streams, the group records and the nli tables with offsets relative to its own
+start, so a block can copy it to shared memory in one piece.  Header word 19 is the
+largest |offset| any fast stream reaches per axis: a lattice at least 2*reach+1 cells
+wide keeps all slots distinct sites, which the fast path requires.
+
+nli tables (in the hot section): for a group of K coordinates over ns species, a table of
+(ns+1)^K process ids indexed by sum(code_k * (ns+1)^k), code = species or ns for the
+null species; 0 when it would exceed 4096 entries (the engine then scans members).
 """
 from __future__ import annotations
 
@@ -73,7 +106,10 @@ OP_LI_DEL = 4
 OP_LI_ADD = 5
 OP_STRIP = 6
 
-HEADER_WORDS = 20
+HEADER_WORDS = 24
+FAST_MAX_SLOTS = 128
+FAST_MAX_EDITS = 96
+NLI_TABLE_MAX = 4096
 
 
 def species_bit(sid: int) -> int:
@@ -471,6 +507,83 @@ class ProgramBuilder:
         w.emit(OP_END)
         return len(ops)
 
+    @staticmethod
+    def _fast_stream(stream, records):
+        """Resolved slot form of one process stream (see the module docstring); None
+        when it exceeds the on-chip limits."""
+        slots: Dict[RelCoord, int] = {}
+
+        def slot(c):
+            if c not in slots:
+                slots[c] = len(slots)
+            return slots[c]
+
+        static: Dict[int, int] = {}  # slot -> species written earlier in the stream
+        chk: List[Tuple[int, int]] = []
+        edits: List[List[int]] = []
+        reach = [0, 0, 0]
+
+        def ref(sl):
+            return -(static[sl] + 2) if sl in static else sl
+
+        def in_mask(sp, mask):
+            return ((mask & 0xFFFFFFFF) >> (31 if sp < 0 else sp)) & 1
+
+        for op in stream:
+            kind = op[0]
+            if kind == "replace":
+                sl = slot(op[1])
+                if sl in static:
+                    if not in_mask(static[sl], op[2]):
+                        raise ValueError("process replaces a species it has just written with another")
+                else:
+                    chk.append((sl, op[2]))
+                static[sl] = op[3]
+            elif kind == "gdel":
+                edits.append([op_header(2, 0, op[1]), pack_coord(*op[2])])
+                t = op[2]
+                reach = [max(reach[i], abs(t[i])) for i in range(3)]
+            elif kind == "add":
+                refs, masks, dead = [], [], False
+                for c, mk in op[3]:
+                    sl = slot(c)
+                    if sl in static:
+                        if not in_mask(static[sl], mk):
+                            dead = True
+                        continue
+                    refs.append(sl)
+                    masks.append(mk)
+                t = op[2]
+                reach = [max(reach[i], abs(t[i])) for i in range(3)]
+                if dead:
+                    continue  # this add_proc can never fire after the writes before it
+                edits.append([op_header(3, len(refs), op[1]), pack_coord(*op[2])] + refs + masks)
+            elif kind in ("li_del", "li_add"):
+                g, o = op[1], op[2]
+                coords, _mems = records[g]
+                refs = [ref(slot((o[0] + c[0], o[1] + c[1], o[2] + c[2], c[3]))) for c in coords]
+                edits.append([op_header(4 if kind == "li_del" else 5, len(coords), g), pack_coord(*o)] + refs)
+                reach = [max(reach[i], abs(o[i])) for i in range(3)]
+            else:
+                return None
+        if len(slots) > FAST_MAX_SLOTS or len(edits) > FAST_MAX_EDITS:
+            return None
+        coords = sorted(slots, key=slots.get)
+        for c in coords:
+            reach = [max(reach[i], abs(c[i])) for i in range(3)]
+        wr = sorted(static.items())
+        head = [len(coords), len(chk), len(wr), len(edits)] + [pack_coord(*c) for c in coords]
+        for sl, mk in chk:
+            head += [sl, mk]
+        for sl, sp in wr:
+            head += [sl, sp]
+        offs, body = [], []
+        base = len(head) + len(edits)
+        for e in edits:
+            offs.append(base + len(body))
+            body += e
+        return head + offs + body, reach
+
     def build(self) -> "Program":
         m = self.model
         P = len(m.processes)
@@ -522,10 +635,58 @@ class ProgramBuilder:
             w.emit(len(mems), len(coords), *[pack_coord(*c) for c in coords])
             for proc, masks in mems:
                 w.emit(proc, *masks)
+        # hot section: fast-stream offsets, fast streams, group records, nli tables;
+        # offsets inside it are relative to its start
+        off_hot = len(w.words)
+        hot: List[int] = [0] * (P + 1)
+        reach = [0, 0, 0]
+        for p, stream in enumerate(proc_streams):
+            fast = self._fast_stream(stream, records)
+            if fast is None:
+                continue
+            words, rch = fast
+            reach = [max(a, b) for a, b in zip(reach, rch)]
+            hot[p] = len(hot)
+            hot.extend(words)
+        hot[P] = len(hot)
+        grp_off = len(hot)
+        hot.extend([0] * max(ngroups, 1))
+        tab_off = len(hot)
+        hot.extend([0] * max(ngroups, 1))
+        for gi, (coords, mems) in enumerate(records):
+            hot[grp_off + gi] = len(hot)
+            hot.extend([len(mems), len(coords)] + [pack_coord(*c) for c in coords])
+            for proc, masks in mems:
+                hot.extend([proc] + list(masks))
+        base = len(m.species) + 1
+        for gi, (coords, mems) in enumerate(records):
+            K = len(coords)
+            if base ** K > NLI_TABLE_MAX:
+                continue
+            table = []
+            for idx in range(base ** K):
+                codes, r = [], idx
+                for _k in range(K):
+                    codes.append(r % base)
+                    r //= base
+                if self.null >= 0:
+                    species = codes  # multi-lattice: the null species is ns
+                else:
+                    species = [c if c < len(m.species) else -1 for c in codes]
+                result = 0
+                for proc, masks in mems:
+                    if all((int(mk) & 0xFFFFFFFF) >> (31 if sp < 0 else sp) & 1 for sp, mk in zip(species, masks)):
+                        result = proc
+                table.append(result)
+            hot[tab_off + gi] = len(hot)
+            hot.extend(table)
+        w.emit(*hot)
         header = [MAGIC, VERSION, BACKENDS[self.backend], P, len(m.species), self.null, m.spuck,
                   m.dimension, ngroups, len(m.layers), off_proc, off_touch, off_groups,
-                  off_site_layer, off_site_default, len(w.words), max_ops]
+                  off_site_layer, off_site_default, 0, max_ops, grp_off, tab_off,
+                  reach[0] | (reach[1] << 8) | (reach[2] << 16), len(hot), off_hot]
         w.words[:len(header)] = header
+        w.words[15] = len(w.words)
         arr = np.array([x if x < 2**31 else x - 2**32 for x in w.words], dtype=np.int64).astype(np.int32)
         return Program(self.model, self.backend, arr)
 

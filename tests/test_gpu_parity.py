@@ -18,7 +18,9 @@ CASES = [("AB_model", "local_smart", (20, 20)), ("ZGB_model", "local_smart", (16
          ("ZGB_model", "lat_int", (12, 16)), ("CO_oxidation_Ruo2", "local_smart", (10, 10)),
          ("CO_oxidation_Ruo2", "lat_int", (9, 11)), ("pairwise_interaction", "lat_int", (16, 16)),
          ("pairwise_interaction", "local_smart", (8, 8)), ("default_xml", "local_smart", (10, 10)),
-         ("pdopd_xml", "local_smart", (8, 8)), ("pdopd_xml", "lat_int", (8, 8))]
+         ("pdopd_xml", "local_smart", (8, 8)), ("pdopd_xml", "lat_int", (8, 8)),
+         # lattices narrower than 2*reach+1: every step takes the serial interpreter
+         ("pairwise_interaction", "lat_int", (5, 5)), ("ZGB_model", "local_smart", (3, 3))]
 
 
 def random_rates(P, seed):
@@ -131,8 +133,8 @@ def test_pool_batch_matches_oracle():
         o = oracle_for(wl, i, n)
         st = o.export()
         assert pr.pool.status(slot) == 0
-        np.testing.assert_array_equal(pr.pool.lattice(slot, o.V), st["lattice"])
-        as1, as2 = pr.pool.tables(slot, o.V)
+        np.testing.assert_array_equal(pr.pool.lattice(slot), st["lattice"])
+        as1, as2 = pr.pool.tables(slot)
         np.testing.assert_array_equal(as1, st["as1"])
         np.testing.assert_array_equal(as2, st["as2"])
         np.testing.assert_array_equal(pr.pool.procstat(slot), st["procstat"])
@@ -178,3 +180,25 @@ def test_deadlock_is_an_error_status_not_a_crash():
         assert err.value.code == 3
         assert t.kmc_step == 16
         assert (t.lattice() == m.species_ids()["CO"]).all()
+
+
+@pytest.mark.parametrize("config", [2, 3, 4])
+def test_serial_and_fast_paths_agree(config):
+    """The gather / replay / scatter step and the serial interpreter give the same
+    tables, step by step counts and clocks."""
+    wl = configs.build(config, n=6, steps=0, sides=[16, 32])
+    out = []
+    for fast in (False, True):
+        pool = E.Pool(arena_bytes=512 << 20, max_slots=16)
+        pool.set_fast_path(fast)
+        mid = pool.add_model(wl.program)
+        slots = pool.admit_many([mid] * wl.n, wl.sizes, wl.rates, seeds=wl.seeds, rng=E.RNG_PHILOX, trajs=wl.trajs)
+        pool.run(slots, 4000)
+        out.append([(pool.tables(s), pool.procstat(s), pool.clock(s))
+                    for i, s in enumerate(slots)])
+        pool.close()
+    for (ta, pa, ca), (tb, pb, cb) in zip(*out):
+        np.testing.assert_array_equal(ta[0], tb[0])
+        np.testing.assert_array_equal(ta[1], tb[1])
+        np.testing.assert_array_equal(pa, pb)
+        assert ca == cb
