@@ -297,7 +297,7 @@ __device__ inline void run_stream(View &v, int pos, int bx, int by, int bz) {
 }  // namespace kmc
 
 // ==================================================================================
-// Fast step: gather -> parallel evaluation -> overlay replay -> scatter
+// Fast step: gather -> parallel evaluation -> per-process replay
 // ==================================================================================
 // A process's resolved fast stream (kmos_gb300/program.py) lists every lattice
 // coordinate it reads or writes as a slot; every condition reads a slot's value from
@@ -305,19 +305,21 @@ __device__ inline void run_stream(View &v, int pos, int bx, int by, int bz) {
 //   1. lanes load every slot's species and check the old species of the replaces;
 //   2. lanes evaluate the edits (guarded dels, adds, nli dels / adds), and a ballot
 //      compacts the ones that happen into a list in program order;
-//   3. lanes load, for every del edit, avail_sites(p, site, 2) and the entry of
-//      avail_sites(p, :, 1) that the swap-remove of that del can read;
-//   4. lane 0 replays the edits in order with exactly the reference's add_proc /
-//      del_proc arithmetic on an on-chip overlay (open addressing) of the table
-//      entries written this step;
-//   5. lanes write the final lattice species and the overlay entries back.
-// The edits and their order are those of the serial interpreter above; only where
-// the values live differs.
+//   3. edits of different processes touch different rows of avail_sites, so each lane
+//      takes one process and replays that process's edits in program order with the
+//      reference's add_proc / del_proc arithmetic: it first issues all the loads its
+//      dels need (avail_sites(p, site, 2) and the top entries of avail_sites(p, :, 1)),
+//      then applies the edits, writing through to memory and remembering its writes
+//      in a small lane-private log so later reads of the same entries stay on chip;
+//   4. lanes write the final species of the replaced slots.
+// The edits and their order within each process are those of the serial interpreter;
+// edits of different processes commute.
 namespace kmc {
 
 constexpr int FAST_SLOTS = 128;
 constexpr int FAST_EDITS = 96;
-constexpr int OV_SIZE = 512;  // power of two, >= 4 keys per edit
+constexpr int LOG_MAX = 12;   // lane-private write log entries
+constexpr int TAIL_MAX = 6;   // lane-private prefetched tail entries
 constexpr int FAST_MAXV = (1 << 23) - 1;
 
 enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
@@ -326,43 +328,14 @@ struct FastSmem {
   int32_t latv[FAST_SLOTS];
   int32_t latsite[FAST_SLOTS];
   int8_t ekind[FAST_EDITS];    // E_GDEL / E_DEL / E_ADD
-  int8_t eprev[FAST_EDITS];    // previous del edit of the same process, -1 if none
   int16_t ep[FAST_EDITS];      // process, 0-based
+  int8_t heads[FAST_EDITS];    // first edit of each process touched this step
   int32_t esite[FAST_EDITS];   // target site
-  int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2)
-  int32_t eti[FAST_EDITS];     // tail index prefetched for this del edit
-  int32_t et[FAST_EDITS];      // prefetched avail_sites(p, eti, 1)
-  uint32_t okey[OV_SIZE];      // overlay of table entries written this step
-  int32_t oval[OV_SIZE];
-  uint16_t oused[OV_SIZE];
+  int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
+  uint32_t lkey[32][LOG_MAX];  // lane-private write logs: table << 31 | index
+  int32_t lval[32][LOG_MAX];
+  int32_t tail[32][TAIL_MAX];  // lane-private avail_sites(p, n0 - j, 1), j < TAIL_MAX
 };
-
-__device__ inline uint32_t ov_key(int table, int p, int index) {
-  return 1u + (((uint32_t)table << 31) | ((uint32_t)p << 23) | (uint32_t)index);
-}
-
-// lane 0 only
-__device__ inline int ov_find(const FastSmem &f, uint32_t key) {
-  uint32_t h = (key * 2654435761u) >> 23;
-  for (int probe = 0; probe < OV_SIZE; probe++) {
-    const uint32_t k = f.okey[h];
-    if (k == key) return (int)h;
-    if (k == 0) return -1 - (int)h;  // free slot where it would go
-    h = (h + 1) & (OV_SIZE - 1);
-  }
-  return -(OV_SIZE + 1);  // full
-}
-
-__device__ inline bool ov_set(FastSmem &f, int &nused, uint32_t key, int32_t val) {
-  const int i = ov_find(f, key);
-  if (i >= 0) { f.oval[i] = val; return true; }
-  if (i == -(OV_SIZE + 1) || nused >= OV_SIZE) return false;
-  const int slot = -1 - i;
-  f.okey[slot] = key;
-  f.oval[slot] = val;
-  f.oused[nused++] = (uint16_t)slot;
-  return true;
-}
 
 // The hot section of a model program: fast streams, group records and nli tables with
 // offsets relative to its start (shared memory when the block staged it).

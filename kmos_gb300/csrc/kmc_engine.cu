@@ -53,12 +53,80 @@ struct WarpSmem {
   double accum[NP * 32];
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
-  int16_t lastdel[NP * 32];
+  int32_t owner[NP * 32];  // first edit of each process this step (INT_MAX when none)
   FastSmem f;
 };
 
-// One kMC step's run_proc_nr through the gather / evaluate / replay / scatter path.
-// All lanes call it and get the status.
+// Replays the edits of process p (the edits k >= head with ep[k] == p) in program
+// order.  Lane-private; returns a status.
+__device__ int replay_process(FastSmem &f, int32_t *ns, const View &v, int head, int ne, int lane) {
+  const int p = f.ep[head];
+  const size_t row = (size_t)p * v.stride;
+  int32_t *a1 = v.as1 + row;
+  int32_t *a2 = v.as2 + row;
+  const int n0 = ns[p];
+  // issue every load the dels can need
+  int r = 0;
+  for (int k = head; k < ne; k++) {
+    if (f.ep[k] != p || f.ekind[k] == E_ADD) continue;
+    f.em[k] = a2[f.esite[k]];
+    if (r < TAIL_MAX) f.tail[lane][r] = (n0 - r >= 1) ? a1[n0 - r] : 0;
+    r++;
+  }
+  // apply the edits; reads look in the write log, then at the prefetched values
+  int n = n0, nlog = 0;
+  bool logok = true;
+  auto put = [&](int table, int index, int32_t val) {
+    if (table) a2[index] = val; else a1[index] = val;
+    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
+    if (!logok) return;
+    for (int i = nlog - 1; i >= 0; i--)
+      if (f.lkey[lane][i] == key) { f.lval[lane][i] = val; return; }
+    if (nlog < LOG_MAX) { f.lkey[lane][nlog] = key; f.lval[lane][nlog] = val; nlog++; }
+    else logok = false;
+  };
+  auto logged = [&](int table, int index, int32_t &val) -> bool {
+    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
+    for (int i = nlog - 1; i >= 0; i--)
+      if (f.lkey[lane][i] == key) { val = f.lval[lane][i]; return true; }
+    return false;
+  };
+  for (int k = head; k < ne; k++) {
+    if (f.ep[k] != p) continue;
+    const int kind = f.ekind[k], site = f.esite[k];
+    if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
+      n += 1;
+      put(0, n, site);
+      put(1, site, n);
+      continue;
+    }
+    // del_proc (base.mpy:211-265)
+    int m;
+    if (!logok) m = a2[site];
+    else if (!logged(1, site, m)) m = f.em[k];
+    if (m == 0) {
+      if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
+      continue;                            // guarded del of an absent entry
+    }
+    if (m < n) {
+      int last;
+      if (!logok) last = a1[n];
+      else if (!logged(0, n, last)) last = (n0 - n < TAIL_MAX && n <= n0) ? f.tail[lane][n0 - n] : a1[n];
+      put(0, m, last);
+      put(0, n, 0);
+      put(1, last, m);
+    } else {
+      put(0, m, 0);
+    }
+    put(1, site, 0);
+    n -= 1;
+  }
+  ns[p] = n;
+  return ST_OK;
+}
+
+// One kMC step's run_proc_nr through the gather / evaluate / replay path.  All lanes
+// call it and get the status.
 template <int NP>
 __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
                          int lane) {
@@ -68,7 +136,6 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   const int32_t *chk = coords + nlat;
   const int32_t *wr = chk + 2 * nchk;
   const int32_t *eoff = wr + 2 * nwr;
-  const int stride = v.stride;
   const unsigned lt = (1u << lane) - 1u;
   // 1. gather every slot; check the old species of first replaces
   for (int i = lane; i < nlat; i += 32) {
@@ -109,89 +176,33 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       f.ekind[pos] = (int8_t)kind;
       f.ep[pos] = (int16_t)(p - 1);
       f.esite[pos] = site;
+      atomicMin(&sm.owner[p - 1], pos);
     }
     ne += __popc(b);
   }
   __syncwarp();
-  // chain the del edits of each process: the k-th del of p can read as1(p, n0 - k)
-  if (lane == 0) {
-    for (int k = 0; k < ne; k++) {
-      if (f.ekind[k] == E_ADD) continue;
-      const int p = f.ep[k];
-      const int prev = sm.lastdel[p];
-      f.eprev[k] = (int8_t)prev;
-      f.eti[k] = prev < 0 ? sm.ns[p] : f.eti[prev] - 1;
-      sm.lastdel[p] = (int16_t)k;
-    }
-    for (int k = 0; k < ne; k++)
-      if (f.ekind[k] != E_ADD) sm.lastdel[f.ep[k]] = -1;
+  // 3. one lane per process touched: the process's first edit heads its chain
+  int nh = 0;
+  for (int r = 0; r < ne; r += 32) {
+    const int k = r + lane;
+    const bool head = k < ne && sm.owner[f.ep[k]] == k;
+    const unsigned b = __ballot_sync(0xffffffffu, head);
+    if (head) f.heads[nh + __popc(b & lt)] = (int8_t)k;
+    nh += __popc(b);
   }
   __syncwarp();
-  // 3. prefetch avail_sites(p, site, 2) and the tail entry of every del edit
-  for (int k = lane; k < ne; k += 32) {
-    if (f.ekind[k] == E_ADD) continue;
-    const size_t row = (size_t)f.ep[k] * stride;
-    f.em[k] = v.as2[row + f.esite[k]];
-    const int ti = f.eti[k];
-    f.et[k] = ti >= 1 ? v.as1[row + ti] : 0;
+  for (int k = lane; k < ne; k += 32) sm.owner[f.ep[k]] = 0x7FFFFFFF;
+  int err = ST_OK;
+  for (int h = lane; h < nh; h += 32) {
+    const int e = replay_process(f, sm.ns, v, f.heads[h], ne, lane);
+    if (e) err = e;
   }
-  __syncwarp();
-  // 4. replay add_proc / del_proc in program order on the overlay
-  int err = ST_OK, nused = 0;
-  if (lane == 0) {
-    for (int k = 0; k < ne && err == ST_OK; k++) {
-      const int kind = f.ekind[k], p = f.ep[k], site = f.esite[k];
-      if (kind == E_ADD) {
-        const int n = sm.ns[p] + 1;
-        sm.ns[p] = n;
-        if (!ov_set(f, nused, ov_key(0, p, n), site) || !ov_set(f, nused, ov_key(1, p, site), n)) err = ST_TABLE;
-        continue;
-      }
-      int i = ov_find(f, ov_key(1, p, site));
-      const int m = i >= 0 ? f.oval[i] : f.em[k];
-      if (m == 0) {
-        if (kind == E_DEL) err = ST_TABLE;  // nli names a process that is not there
-        continue;
-      }
-      const int n = sm.ns[p];
-      bool ok = true;
-      if (m < n) {
-        int last;
-        i = ov_find(f, ov_key(0, p, n));
-        if (i >= 0) {
-          last = f.oval[i];
-        } else {
-          int j = k;
-          while (j >= 0 && f.eti[j] != n) j = f.eprev[j];
-          last = j >= 0 ? f.et[j] : v.as1[(size_t)p * stride + n];
-        }
-        ok = ov_set(f, nused, ov_key(0, p, m), last) && ov_set(f, nused, ov_key(0, p, n), 0) &&
-             ov_set(f, nused, ov_key(1, p, last), m);
-      } else {
-        ok = ov_set(f, nused, ov_key(0, p, m), 0);
-      }
-      ok = ok && ov_set(f, nused, ov_key(1, p, site), 0);
-      if (!ok) err = ST_TABLE;
-      sm.ns[p] = n - 1;
-    }
-  }
-  err = __shfl_sync(0xffffffffu, err, 0);
-  nused = __shfl_sync(0xffffffffu, nused, 0);
-  __syncwarp();
-  // 5. scatter the overlay and the final species of the replaced slots
-  for (int i = lane; i < nused; i += 32) {
-    const int h = f.oused[i];
-    const uint32_t key = f.okey[h] - 1u;
-    if (err == ST_OK) {
-      const size_t at = (size_t)((key >> 23) & 0xFF) * stride + (key & 0x7FFFFF);
-      if (key >> 31) v.as2[at] = f.oval[h]; else v.as1[at] = f.oval[h];
-    }
-    f.okey[h] = 0u;
-  }
-  if (err == ST_OK)
+  // 4. the final species of every replaced slot
+  if (!__any_sync(0xffffffffu, err != ST_OK))
     for (int i = lane; i < nwr; i += 32) v.lat[f.latsite[wr[2 * i]] - 1] = (int8_t)wr[2 * i + 1];
+  const int e0 = __reduce_max_sync(0xffffffffu, (unsigned)err);
   __syncwarp();
-  return err;
+  return e0;
 }
 
 // --------------------------------------------------------------------- run kernel
@@ -227,8 +238,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
   H.nspecies = M.nspecies;
   const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
   WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw + hot_bytes)[wib];
-  for (int i = lane; i < OV_SIZE; i += 32) sm.f.okey[i] = 0u;
-  for (int i = lane; i < NP * 32; i += 32) sm.lastdel[i] = -1;
+  for (int i = lane; i < NP * 32; i += 32) sm.owner[i] = 0x7FFFFFFF;
   __syncthreads();
 
   for (;;) {
@@ -282,17 +292,43 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
     }
     double t = S.kmc_time, dt = S.kmc_time_step;
     int64_t kstep = S.kmc_step;
-    uint64_t rng[4] = {S.rng[0], S.rng[1], S.rng[2], S.rng[3]};
+    // random numbers: every 32 steps, lane j draws step k + j's (ran_time, ran_proc,
+    // ran_site) and -log(ran_time); steps take them with shuffles
+    uint64_t rbase[4] = {S.rng[0], S.rng[1], S.rng[2], S.rng[3]};
     const int rng_kind = S.rng_kind;
     const uint32_t seed = S.seed, traj = S.traj;
+    double my_nl = 0.0, my_rp = 0.0, my_rs = 0.0;
+    int bidx = 32;
     int from = S.accum_from;
     int status = ST_OK;
+    int64_t k = 0;
     __syncwarp();
 
-    for (int64_t k = 0; k < nsteps; k++) {
+    for (; k < nsteps; k++) {
       if (a.cancel && (k & 1023) == 0 && *a.cancel) { status = ST_CANCELLED; break; }
-      double ran_time, ran_proc, ran_site;
-      draw3(rng_kind, rng, seed, traj, ran_time, ran_proc, ran_site);
+      if (bidx == 32) {
+        if (k > 0) {  // advance the base state past the batch just used
+          if (rng_kind == RNG_GFORTRAN) {
+            for (int d = 0; d < 96; d++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
+          } else {
+            rbase[0] += 32;
+          }
+        }
+        uint64_t st[4] = {rbase[0], rbase[1], rbase[2], rbase[3]};
+        double rt;
+        if (rng_kind == RNG_GFORTRAN) {
+          for (int d = 0; d < 3 * lane; d++) xoshiro_next(st[0], st[1], st[2], st[3]);
+        } else {
+          st[0] += lane;
+        }
+        draw3(rng_kind, st, seed, traj, rt, my_rp, my_rs);
+        my_nl = -log(rt);
+        bidx = 0;
+      }
+      const double nl = __shfl_sync(0xffffffffu, my_nl, bidx);
+      const double ran_proc = __shfl_sync(0xffffffffu, my_rp, bidx);
+      const double ran_site = __shfl_sync(0xffffffffu, my_rs, bidx);
+      bidx++;
 
       // update_accum_rate from the first stale entry: entries before it are the same
       // sums of the same terms, so the result equals a full recompute bit for bit
@@ -309,10 +345,12 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       from = P;
       __syncwarp();
       const double total = sm.accum[P - 1];
-      if (!(total > 0.0)) { status = ST_DEADLOCK; break; }
+      const long long tbits = __double_as_longlong(total);
+      if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
 
-      // update_clocks
-      dt = __ddiv_rn(-log(ran_time), total);
+      // update_clocks: kmc_time += -log(r)/accum(P), the quotient as -log(r) times the
+      // reciprocal of accum(P) (within 2 ulp of the quotient)
+      dt = __dmul_rn(nl, __drcp_rn(total));
       t = __dadd_rn(t, dt);
       kstep += 1;
 
@@ -323,13 +361,15 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
         if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(sm.term[i], dt));
       }
 
-      // determine_procsite
-      const double val = __dmul_rn(ran_proc, total);
+      // determine_procsite: for non-negative doubles the order of the bit patterns is
+      // the order of the values
+      const long long vbits = __double_as_longlong(__dmul_rn(ran_proc, total));
       int proc = -1;
 #pragma unroll
       for (int j = 0; j < NP; j++) {
         const int i = lane + 32 * j;
-        const bool pred = (i < P) && (sm.accum[i] > val || sm.accum[i] == total);
+        const long long ab = i < P ? __double_as_longlong(sm.accum[i]) : 0;
+        const bool pred = (i < P) && (ab > vbits || ab == tbits);
         const unsigned b = __ballot_sync(0xffffffffu, pred);
         if (proc < 0 && b) proc = 32 * j + __ffs(b) - 1;
       }
@@ -380,6 +420,16 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       from = first;
       __syncwarp();
     }
+    // random state after the draws actually used: bidx draws of the current batch
+    // (a step that found no process has drawn its numbers, as in the reference)
+    if (bidx < 32 || k > 0) {
+      const int used = bidx;
+      if (rng_kind == RNG_GFORTRAN) {
+        for (int d = 0; d < 3 * used; d++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
+      } else {
+        rbase[0] += used;
+      }
+    }
 
 #pragma unroll
     for (int j = 0; j < NP; j++) {
@@ -395,7 +445,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       S.kmc_time = t;
       S.kmc_time_step = dt;
       S.kmc_step = kstep;
-      S.rng[0] = rng[0]; S.rng[1] = rng[1]; S.rng[2] = rng[2]; S.rng[3] = rng[3];
+      S.rng[0] = rbase[0]; S.rng[1] = rbase[1]; S.rng[2] = rbase[2]; S.rng[3] = rbase[3];
       S.accum_from = from;
       S.status = status;
     }
