@@ -181,6 +181,20 @@ KMC_API int kmc_pool_occupation_counts(kmc_pool *pool, const int32_t *slots, int
 KMC_API int kmc_pool_get_results(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride,
                                  int64_t *procstat, double *integ, double *times, int64_t *steps,
                                  int32_t *status);
+/* kmc_pool_occupation_counts for callers that must not allocate device memory: code
+ * running under a fixed device-memory budget that is already spent, or in a stream-ordered
+ * section where a cudaMalloc would synchronise the device or is forbidden (an allocator's
+ * own callback, a real-time serving loop).  It has no counterpart in the reference.  Its
+ * scratch (slot list and counters) is one static device array of about 2 MB that every
+ * call shares: at most KMC_STATIC_OCC_MAX_SLOTS slots and KMC_STATIC_OCC_MAX_STRIDE
+ * counters per slot (larger requests return KMC_ERR_ARG).  The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress), so make that call before any
+ * stream capture.  Calls whose work overlaps on the GPU (other threads, other pools'
+ * streams) race on the array: serialise them. */
+#define KMC_STATIC_OCC_MAX_SLOTS 4096
+#define KMC_STATIC_OCC_MAX_STRIDE 64
+KMC_API int kmc_pool_occupation_counts_static(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride,
+                                              int64_t *out);
 /* Launch configuration used by kmc_pool_run: warps per block (1..32, 0 = automatic). */
 KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
 /* 1 (default): steps whose process has a fast stream run through the gather /

@@ -1557,6 +1557,61 @@ int kmc_pool_get_results(kmc_pool *p, const int32_t *slots, int32_t n, int32_t s
   return KMC_OK;
 }
 
+// ------------------------------------------------- occupation counts without allocating
+// Scratch of kmc_pool_occupation_counts_static: the slot list (int32) followed by the
+// counters (unsigned 64-bit), for at most KMC_STATIC_OCC_MAX_SLOTS slots of at most
+// KMC_STATIC_OCC_MAX_STRIDE counters.  Every GPU that loads the library holds it until
+// the process exits.  Host code may not use the name as an address: the per-device
+// address comes from cudaGetSymbolAddress below.
+constexpr size_t kOccListBytes = sizeof(int32_t) * KMC_STATIC_OCC_MAX_SLOTS;
+constexpr size_t kOccCountBytes = sizeof(unsigned long long) * KMC_STATIC_OCC_MAX_SLOTS * KMC_STATIC_OCC_MAX_STRIDE;
+static __device__ __align__(256) unsigned char g_occ_scratch[kOccListBytes + kOccCountBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_occ_mu;
+void *g_occ_addr[kMaxDevices];  // device address of g_occ_scratch, per device
+}  // namespace
+
+int kmc_pool_occupation_counts_static(kmc_pool *p, const int32_t *slots, int32_t n, int32_t stride, int64_t *out) {
+  if (!p || !slots || !out) return fail(KMC_ERR_ARG, "bad arguments");
+  if (n < 1 || n > KMC_STATIC_OCC_MAX_SLOTS)
+    return fail(KMC_ERR_ARG, "kmc_pool_occupation_counts_static: slot count must be 1.." +
+                                 std::to_string(KMC_STATIC_OCC_MAX_SLOTS));
+  if (stride < 1 || stride > KMC_STATIC_OCC_MAX_STRIDE)
+    return fail(KMC_ERR_ARG, "kmc_pool_occupation_counts_static: stride must be 1.." +
+                                 std::to_string(KMC_STATIC_OCC_MAX_STRIDE));
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+  }
+  if (p->device < 0 || p->device >= kMaxDevices) return fail(KMC_ERR_ARG, "device index beyond the static table");
+  CK(cudaSetDevice(p->device));
+  void *base = nullptr;
+  {
+    // one-time set-up per device, with that device current
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    if (!g_occ_addr[p->device]) {
+      void *addr = nullptr;
+      CK(cudaGetSymbolAddress(&addr, g_occ_scratch));
+      g_occ_addr[p->device] = addr;
+    }
+    base = g_occ_addr[p->device];
+  }
+  int32_t *d_list = reinterpret_cast<int32_t *>(base);
+  unsigned long long *d_out = reinterpret_cast<unsigned long long *>(static_cast<char *>(base) + kOccListBytes);
+  const size_t count_bytes = sizeof(unsigned long long) * (size_t)n * stride;
+  // the counters keep the previous call's values: clear the part this call uses
+  CK(cudaMemsetAsync(d_out, 0, count_bytes, p->stream));
+  CK(cudaMemcpyAsync(d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  kmc_occupation_kernel<<<n, 256, 0, p->stream>>>(p->d_slots, p->d_models, d_list, n, stride, d_out);
+  CK(cudaGetLastError());
+  p->launches++;
+  CK(cudaMemcpyAsync(out, d_out, count_bytes, cudaMemcpyDeviceToHost, p->stream));
+  CK(cudaStreamSynchronize(p->stream));
+  return KMC_OK;
+}
+
 // ---------------------------------------------------------- single trajectory API
 int kmc_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer, int32_t seed,
                int32_t rng_kind, uint32_t traj_id, kmc_handle **out) {

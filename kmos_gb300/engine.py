@@ -83,6 +83,7 @@ SIGNATURES = {
     "kmc_pool_get_lattice": (_i32, [_vp, _i32, _p32]),
     "kmc_pool_get_tables": (_i32, [_vp, _i32, _p32, _p32]),
     "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
+    "kmc_pool_occupation_counts_static": (_i32, [_vp, _p32, _i32, _i32, _p64]),
     "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
     "kmc_pool_set_fast_path": (_i32, [_vp, _i32]),
@@ -455,6 +456,18 @@ class Pool:
         _check(load().kmc_pool_get_results(self.h, _ptr(slots, _i32), n, int(stride), _ptr(ps, _i64), _ptr(ig, _dbl),
                                            _ptr(t, _dbl), _ptr(k, _i64), _ptr(st, _i32)))
         return ps, ig, t, k, st
+
+    def occupation_counts_static(self, slots, stride: int) -> np.ndarray:
+        """occupation_counts through the entry point that allocates no device memory
+        (for callers that cannot allocate: a spent memory budget, or a section where an
+        allocation would synchronise the device).  Its scratch is a fixed static array
+        shared by every call: at most 4096 slots and 64 counters per slot, and calls that
+        overlap on the GPU must be serialised by the caller."""
+        slots = _a32(slots)
+        out = np.zeros(len(slots) * stride, np.int64)
+        _check(load().kmc_pool_occupation_counts_static(self.h, _ptr(slots, _i32), len(slots), int(stride),
+                                                         _ptr(out, _i64)))
+        return out.reshape(len(slots), stride)
 
     def occupation_counts(self, slots, stride: int) -> np.ndarray:
         slots = _a32(slots)
