@@ -12,9 +12,18 @@ Outputs
   ab_model_ref_procs_sites.npy  the 10000 (proc, site) pairs of the reference's golden
                               trajectory tests/test_run/_tmp_export_local_smart/
                               ref_procs_sites_local_smart.log (identical for lat_int and otf).
+  ops/<model>_<backend>.json  the op order of the Fortran the reference's generator writes
+                              for each fixture model (fortran_ops.py reads it): per process
+                              the inlined op list, the touch-ups, and every nli function's
+                              value on every species assignment of its coordinates.  The
+                              .ini models are exported here with the reference generator;
+                              for default.xml and pdopd.xml (the reference's XML reader needs
+                              lxml, absent here) the generated code the reference ships as
+                              its own golden export (tests/export_test/reference_*) is used.
 """
 import ast
 import json
+import re
 import os
 import sys
 import types
@@ -68,8 +77,88 @@ def import_reference():
     return kmos
 
 
+def export_reference(kmos, path, backend, out_dir):
+    import kmos.io
+    pt = kmos.types.Project()
+    pt.import_file(path)
+    os.makedirs(out_dir, exist_ok=True)
+    try:
+        kmos.io.export_source(pt, out_dir, code_generator=backend)
+    except Exception as e:  # write_settings evaluates rates it cannot; the sources are written
+        print("  export:", repr(e)[:80])
+
+
+SHIPPED = {("default_xml", "local_smart"): "tests/export_test/reference_export",
+           ("default_xml", "lat_int"): "tests/export_test/reference_export_lat_int",
+           ("pdopd_xml", "local_smart"): "tests/export_test/reference_pdopd_local_smart",
+           ("pdopd_xml", "lat_int"): "tests/export_test/reference_pdopd_lat_int"}
+
+
+def _jsonable(ops):
+    out = []
+    for op in ops:
+        if op[0] == "add":
+            out.append(["add", op[1], list(op[2]), sorted([list(c), m] for c, m in op[3])])
+        else:
+            out.append([op[0]] + [list(x) if isinstance(x, tuple) else x for x in op[1:]])
+    return out
+
+
+def write_op_goldens(kmos):
+    import itertools
+    import tempfile
+    sys.path.insert(0, HERE)
+    import fortran_ops as F
+
+    os.makedirs(os.path.join(HERE, "ops"), exist_ok=True)
+    rng = np.random.default_rng(0)
+    for name, rel in MODELS.items():
+        for backend in ("local_smart", "lat_int"):
+            if (name, backend) in SHIPPED:
+                d = os.path.join(REF, SHIPPED[(name, backend)])
+            elif rel.endswith(".ini"):
+                d = tempfile.mkdtemp(prefix="kmos_export_")
+                export_reference(kmos, os.path.join(REF, rel), backend, d)
+            else:
+                continue
+            out = {"backend": backend}
+            if backend == "local_smart":
+                procs, touch, const = F.local_smart_ops(d)
+                out["touchups"] = {str(n): _jsonable(ops) for n, ops in touch.items()}
+            else:
+                procs, nlis, groups, const = F.lat_int_ops(d)
+                out["groups"] = groups
+                tables = {}
+                species = sorted(v for k, v in const.items() if False)
+                for g, tree in nlis.items():
+                    coords = F.tree_coords(tree)
+                    ids = sorted({v for v in _species_ids(d, F)})
+                    combos = list(itertools.product(ids, repeat=len(coords)))
+                    if len(combos) > 20000:
+                        combos = [tuple(int(x) for x in rng.choice(ids, size=len(coords))) for _ in range(20000)]
+                    vals = [F.eval_nli(tree, lambda c, a=dict(zip(coords, cb)): a[c]) for cb in combos]
+                    tables[str(g)] = {"coords": [list(c) for c in coords], "combos": [list(c) for c in combos],
+                                      "values": vals}
+                out["nli"] = tables
+            out["procs"] = {str(p): _jsonable(ops) for p, ops in procs.items()}
+            with open(os.path.join(HERE, "ops", "%s_%s.json" % (name, backend)), "w") as fh:
+                json.dump(out, fh, separators=(",", ":"))
+            print("ops", name, backend, len(procs), "processes")
+
+
+def _species_ids(directory, F):
+    import glob
+    for f in glob.glob(os.path.join(directory, "proclist*.f90")):
+        text = open(f).read()
+        m = re.search(r"nr_of_species\s*=\s*(\d+)", text)
+        if m:
+            return range(int(m.group(1)))
+    raise ValueError("no species count in %s" % directory)
+
+
 def main():
     kmos = import_reference()
+    write_op_goldens(kmos)
     from kmos_gb300 import model as M
 
     os.makedirs(os.path.join(HERE, "models"), exist_ok=True)
