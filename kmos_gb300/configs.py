@@ -211,3 +211,37 @@ def build(config: int, n: Optional[int] = None, steps: Optional[int] = None, sid
     else:
         raise ValueError("config must be 1..4")
     return wl
+
+
+def serving_requests(rate: float = 500.0, duration: float = 60.0, seed: int = 5, steps_scale: float = 1.0,
+                     side_range=(10, 200), steps_range=(1e4, 1e7)):
+    """Configuration 5: a Poisson request stream mixing configurations 1-3.
+
+    Arrivals at ``rate`` per second for ``duration`` seconds; model uniform in {1, 2, 3};
+    side uniform in ``side_range``; kMC steps log-uniform in ``steps_range`` times
+    ``steps_scale``; per-request parameters drawn as in the batch configurations.
+    Returns (requests, {model key: program})."""
+    from .serving import Request
+    rng = np.random.Generator(np.random.PCG64(1000 + 5 + seed))
+    progs = {"c1": build(1, n=1, steps=0).program, "c2": build(2, n=1, steps=0).program,
+             "c3": build(3, n=1, steps=0).program}
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        kind = int(rng.integers(1, 4))
+        side = int(rng.integers(side_range[0], side_range[1] + 1))
+        n = int(np.exp(rng.uniform(np.log(steps_range[0]), np.log(steps_range[1]))) * steps_scale)
+        if kind == 1:
+            rates = [100.0, 100.0]
+        elif kind == 2:
+            y = rng.uniform(0.45, 0.60)
+            rates = [y] + [(1.0 - y) / 4.0] * 4 + [1e6] * 4
+        else:
+            kT = K_B_EV * rng.uniform(300.0, 600.0)
+            rates = [1e3] + [1e13 * np.exp(-(1.3 + 0.1 * bin(m).count("1")) / kT) for m in range(16)] + \
+                    [1e13 * np.exp(-0.6 / kT)] * 4
+        reqs.append(Request(model="c%d" % kind, size=(side, side, 1), rates=[float(x) for x in rates],
+                            steps=max(1, n), seed=5, traj_id=len(reqs), rid=len(reqs), arrival=t))
+    return reqs, progs

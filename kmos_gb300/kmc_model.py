@@ -1,0 +1,207 @@
+"""Drop-in for kmos's f2py module ``kmc_model``: ``base``, ``lattice`` and ``proclist``
+with the names, argument conventions and return values of the generated Fortran
+modules, running on the GB300 engine.
+
+kmos builds ``kmc_model`` per model with f2py (kmos/utils/__init__.py:406-521) and
+``kmos.run`` imports ``base, lattice, proclist`` from it (kmos/run/__init__.py:86-114).
+Here one call configures the three namespaces for a model::
+
+    from kmos_gb300 import kmc_model
+    base, lattice, proclist = kmc_model.configure("model.ini", backend="local_smart")
+
+(``kmos_gb300.export`` writes a ``kmc_model.py`` that does this, so ``kmos.run`` imports
+it unchanged).  Without an explicit call, the first access to ``base``, ``lattice`` or
+``proclist`` configures them from the ``kmc_settings`` module of the export directory:
+its ``model_json`` (written by ``kmos_gb300.export``) or the project ``xml`` kmos's own
+export writes there; the backend comes from ``kmc_settings.backend`` or the
+``KMOS_GB300_BACKEND`` environment variable (default local_smart).  f2py lower-cases Fortran names, so process, species and site constants
+are lower-case attributes.  Sites are passed as 4-vectors ``(x, y, z, n)`` where the
+Fortran takes ``integer, dimension(4)``, and as 1-based indices where it takes ``nr``.
+
+State lives on the GPU from ``proclist.init`` to ``lattice.deallocate_system``; getters
+copy what they return.  Where the Fortran would ``stop``, a ``KMCError`` is raised.
+"""
+from __future__ import annotations
+
+import types
+from typing import Optional
+
+import numpy as np
+
+from . import engine as E
+from .model import Model, from_dict, load
+from .program import compile_model
+
+
+class _State:
+    def __init__(self, model: Model, backend: str):
+        self.model = model
+        self.backend = backend
+        self.program = compile_model(model, backend)
+        self.traj: Optional[E.Trajectory] = None
+        self.system_size = np.zeros(3, dtype=np.int32)
+        self.seed = 1
+
+    def t(self) -> E.Trajectory:
+        if self.traj is None:
+            raise E.KMCError(1, "system not allocated: call proclist.init first")
+        return self.traj
+
+    # lattice mapping (lattice.mpy:146-210)
+    def lattice2nr(self, site) -> int:
+        x, y, z, n = (int(v) for v in site)
+        X, Y, Z = (int(v) for v in self.system_size)
+        return self.model.spuck * ((x % X) + X * ((y % Y) + Y * (z % Z))) + n
+
+    def nr2lattice(self, nr: int):
+        sp = self.model.spuck
+        X, Y = int(self.system_size[0]), int(self.system_size[1])
+        c = (int(nr) - 1) // sp
+        return np.array([c % X, (c // X) % Y, c // (X * Y), int(nr) - sp * c], dtype=np.int32)
+
+
+def _base(S: _State) -> types.SimpleNamespace:
+    ns = types.SimpleNamespace()
+    ns.null_species = S.model.null_species()
+    ns.get_null_species = lambda: S.model.null_species()
+    ns.is_allocated = lambda: S.traj is not None
+    ns.set_rate_const = lambda proc, rate: S.t().set_rate_const(int(proc), float(rate))
+    ns.update_accum_rate = lambda: S.t().update_accum_rate()
+    ns.update_integ_rate = lambda: S.t().update_integ_rate()
+    ns.get_kmc_time = lambda: S.t().kmc_time
+    ns.get_kmc_time_step = lambda: S.t().kmc_time_step
+    ns.get_kmc_step = lambda: S.t().kmc_step
+
+    def set_kmc_time(t):
+        S.t().kmc_time = float(t)
+
+    ns.set_kmc_time = set_kmc_time
+    ns.get_procstat = lambda proc: int(S.t().procstat()[int(proc) - 1])
+    ns.get_rate = lambda proc: float(S.t().rates()[int(proc) - 1])
+    ns.get_integ_rate = lambda proc: float(S.t().integ_rates()[int(proc) - 1])
+    ns.get_accum_rate = lambda proc: float(S.t().accum_rates()[int(proc) - 1])
+    ns.get_nrofsites = lambda proc: int(S.t().nr_of_sites()[int(proc) - 1])
+    ns.get_avail_site = lambda proc, idx, sw: S.t().avail_site(int(proc), int(idx), int(sw))
+    ns.get_volume = lambda: S.t().V
+    ns.get_walltime = lambda: 0.0
+    ns.get_species = lambda nr: S.t().get_species(int(nr))
+    ns.replace_species = lambda nr, old, new: S.t().replace_species(int(nr), int(old), int(new))
+    return ns
+
+
+def _lattice(S: _State) -> types.SimpleNamespace:
+    m = S.model
+    ns = types.SimpleNamespace()
+    ns.system_size = S.system_size
+    ns.spuck = m.spuck
+    ns.model_dimension = m.dimension
+    ns.nr_of_layers = len(m.layers)
+    lid = m.layer_ids()
+    for name, i in lid.items():
+        setattr(ns, name.lower(), i)
+    ns.default_layer = lid[m.default_layer]
+    ns.substrate_layer = lid.get(m.substrate_layer, ns.default_layer)
+    ns.unit_cell_size = np.array(m.cell, dtype=np.float64)
+    ns.site_positions = np.array([s.pos for _l, s in m.site_list()], dtype=np.float64).reshape(-1, 3)
+    for (lname, sname), n in m.site_ids().items():
+        setattr(ns, ("%s_%s" % (lname, sname)).lower(), n)
+    ns.calculate_lattice2nr = S.lattice2nr
+    ns.calculate_nr2lattice = S.nr2lattice
+    ns.get_species = lambda site: S.t().get_species(S.lattice2nr(site))
+    ns.replace_species = lambda site, old, new: S.t().replace_species(S.lattice2nr(site), int(old), int(new))
+
+    def deallocate_system():
+        if S.traj is not None:
+            S.traj.close()
+            S.traj = None
+
+    ns.deallocate_system = deallocate_system
+    return ns
+
+
+def _proclist(S: _State) -> types.SimpleNamespace:
+    m = S.model
+    ns = types.SimpleNamespace()
+    ns.nr_of_proc = len(m.processes)
+    ns.nr_of_species = len(m.species) + (0 if len(m.layers) == 1 else 1)
+    for name, i in m.species_ids().items():
+        setattr(ns, name.lower(), i)
+    ns.default_species = m.species_ids()[m.default_species]
+    if len(m.layers) > 1:
+        ns.null_species = m.null_species()
+    for name, i in m.process_ids().items():
+        setattr(ns, name.lower(), i)
+    ns.seed_size = 12
+    ns.seed = S.seed
+    ns.representation_length = max([len(r) for r in m.representations.values()] + [1])
+    if S.backend == "lat_int":
+        ns.backend = "lat_int"
+
+    def init(input_system_size, system_name="kmc_model", layer=None, seed_in=1, no_banner=True):
+        """proclist.init (proclist_generic_subroutines.mpy:166-230)."""
+        size = [int(v) for v in np.atleast_1d(input_system_size)]
+        size = (size + [1, 1, 1])[:3]
+        if S.traj is not None:
+            raise E.KMCError(1, "allocate_system: tried to allocate twice, deallocate first")
+        S.system_size[:] = size
+        S.seed = int(seed_in)
+        ns.seed = S.seed
+        layer = ns_default_layer if layer is None else int(layer)
+        S.traj = E.Trajectory(S.program, size, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
+
+    ns_default_layer = m.layer_ids()[m.default_layer]
+    ns.init = init
+    ns.do_kmc_steps = lambda n: S.t().do_kmc_steps(int(n))
+    ns.do_kmc_step = lambda: S.t().do_kmc_steps(1)
+    ns.get_next_kmc_step = lambda: S.t().get_next_kmc_step()
+    ns.run_proc_nr = lambda proc, site: S.t().run_proc_nr(int(proc), int(site))
+
+    def get_occupation():
+        """(nr_of_species, spuck) site-resolved coverage per unit cell."""
+        occ = S.t().occupation()
+        out = np.zeros((ns.nr_of_species, m.spuck))
+        out[:occ.shape[0]] = occ
+        return out
+
+    ns.get_occupation = get_occupation
+    if S.backend == "lat_int":
+        ns.touchup_cell = lambda cell: S.t().touchup(S.lattice2nr([cell[0], cell[1], cell[2], 1]))
+    else:
+        for (lname, sname), n in m.site_ids().items():
+            setattr(ns, ("touchup_%s_%s" % (lname, sname)).lower(),
+                    lambda site: S.t().touchup(S.lattice2nr(site)))
+    return ns
+
+
+def configure(model, backend: str = "local_smart"):
+    """Builds ``(base, lattice, proclist)`` for ``model`` (a :class:`Model`, a project
+    file path, or a JSON dict of one) on ``backend``; also sets them as attributes of
+    this module so ``from kmos_gb300.kmc_model import base, lattice, proclist`` works
+    after the call."""
+    if isinstance(model, str):
+        model = load(model)
+    elif isinstance(model, dict):
+        model = from_dict(model)
+    S = _State(model, backend)
+    b, l, p = _base(S), _lattice(S), _proclist(S)
+    g = globals()
+    g["base"], g["lattice"], g["proclist"], g["_state"] = b, l, p, S
+    return b, l, p
+
+
+def __getattr__(name):
+    if name in ("base", "lattice", "proclist"):
+        import importlib
+        import os
+        settings = importlib.import_module("kmc_settings")
+        backend = getattr(settings, "backend", os.environ.get("KMOS_GB300_BACKEND", "local_smart"))
+        if hasattr(settings, "model_json"):
+            model = from_dict(settings.model_json)
+        elif hasattr(settings, "xml"):
+            from .model import load_xml
+            model = load_xml(settings.xml)
+        else:
+            raise AttributeError("kmc_settings has neither model_json nor xml to configure %s from" % name)
+        configure(model, backend)
+        return globals()[name]
+    raise AttributeError(name)

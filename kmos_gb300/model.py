@@ -309,7 +309,11 @@ def load_ini(path_or_text: str) -> Model:
 # .xml reader (layout of kmos/types.py:915-1159, project versions (0, 2) and (0, 3))
 # --------------------------------------------------------------------------------------
 def load_xml(path: str) -> Model:
-    root = ET.parse(path).getroot()
+    """Read a kmos ``.xml`` project file, or an XML string (kmc_settings.xml holds one)."""
+    if path.lstrip().startswith("<"):
+        root = ET.fromstring(path.strip())
+    else:
+        root = ET.parse(path).getroot()
     meta: Dict[str, str] = {}
     species: List[str] = []
     representations: Dict[str, str] = {}

@@ -1,0 +1,222 @@
+"""Continuous-batching serving of kMC trajectories on one GPU.
+
+A request asks for N kMC steps of one model on one lattice with given rate constants
+and returns the trajectory's final TOFs (from procstat and from integ_rates),
+coverages, kmc_time and step count.  The server keeps every admitted trajectory
+resident in the pool's HBM arena and advances all of them together, one *quantum* (a
+persistent launch per model, each trajectory taking min(remaining, quantum) steps) at a
+time.  Between quanta it retires finished trajectories (one gathered read-back) and
+admits waiting requests while the arena has room for them — admission by free HBM.
+Requests that arrive while a quantum runs join the next one, so their work overlaps on
+the device with the requests already running.
+
+Each trajectory's random stream is Philox keyed by (seed, trajectory id), so a request's
+result is the same alone and in any mix.
+
+kmos has no counterpart (it runs one model per process; ``ModelRunner``,
+kmos/run/__init__.py:1991-2368, forks one process per parameter set).
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import engine as E
+from .program import Program
+
+
+@dataclass
+class Request:
+    model: str                      # key of a registered model
+    size: Sequence[int]             # system size per axis
+    rates: Sequence[float]          # rate constant per process
+    steps: int                      # kMC steps to run
+    seed: int = 1
+    traj_id: int = 0                # Philox key word: a request's stream identity
+    rid: int = 0
+    arrival: float = 0.0            # seconds, on the server's clock
+    # filled in by the server
+    slot: int = -1
+    remaining: int = 0
+    admitted: float = -1.0
+    done: float = -1.0
+    result: Optional[dict] = None
+    error: Optional[str] = None
+
+
+@dataclass
+class ModelEntry:
+    program: Program
+    model_id: int
+    nproc: int
+    nspecies: int
+    spuck: int
+    tof_matrix: np.ndarray          # [n_tof, nproc]
+    tof_names: List[str] = field(default_factory=list)
+
+
+class Server:
+    """Continuous-batching server over one pool."""
+
+    def __init__(self, arena_bytes: int, max_slots: int = 8192, quantum: int = 20000, device: int = 0):
+        self.pool = E.Pool(arena_bytes=arena_bytes, max_slots=max_slots, device=device)
+        self.max_slots = max_slots
+        self.quantum = int(quantum)
+        self.models: Dict[str, ModelEntry] = {}
+        self.waiting: collections.deque = collections.deque()
+        self.active: Dict[int, Request] = {}
+        self.finished: List[Request] = []
+        self.t0 = time.perf_counter()
+        self.kmc_steps = 0
+        self.quanta = 0
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def add_model(self, key: str, program: Program) -> None:
+        m = program.model
+        tofs = m.tof_names()
+        mat = np.zeros((len(tofs), program.nproc))
+        for j, p in enumerate(m.processes):
+            for name, factor in (p.tof_count or {}).items():
+                mat[tofs.index(name), j] += factor
+        self.models[key] = ModelEntry(program, self.pool.add_model(program), program.nproc,
+                                      len(m.species), m.spuck, mat, tofs)
+
+    def submit(self, req: Request) -> None:
+        if req.model not in self.models:
+            raise KeyError("unknown model %r" % req.model)
+        if len(req.rates) != self.models[req.model].nproc:
+            raise ValueError("request %d: %d rates for %d processes" % (req.rid, len(req.rates),
+                                                                       self.models[req.model].nproc))
+        req.remaining = int(req.steps)
+        self.waiting.append(req)
+
+    # ------------------------------------------------------------------ scheduling
+    def _admit(self) -> int:
+        """Admits waiting requests in arrival order while the arena and the slot table
+        have room (admission by free HBM)."""
+        batch: List[Request] = []
+        free, _largest = self.pool.free_bytes()
+        budget = free
+        while self.waiting and len(self.active) + len(batch) < self.max_slots:
+            req = self.waiting[0]
+            entry = self.models[req.model]
+            need = self.pool.slot_bytes(entry.model_id, req.size)
+            if need > budget:
+                break
+            budget -= need
+            batch.append(self.waiting.popleft())
+        if not batch:
+            return 0
+        try:
+            slots = self.pool.admit_many([self.models[r.model].model_id for r in batch], [r.size for r in batch],
+                                         [r.rates for r in batch], seeds=[r.seed for r in batch],
+                                         rng=E.RNG_PHILOX, trajs=[r.traj_id for r in batch])
+        except E.KMCError as err:
+            if err.code != 6:
+                raise
+            # fragmentation: fall back to one at a time
+            slots = []
+            for r in batch:
+                try:
+                    slots.append(self.pool.admit(self.models[r.model].model_id, r.size, r.rates, seed=r.seed,
+                                                 rng=E.RNG_PHILOX, traj=r.traj_id))
+                except E.KMCError as e2:
+                    if e2.code != 6:
+                        raise
+                    slots.append(None)
+        t = self.now()
+        for r, s in zip(batch, slots):
+            if s is None:
+                self.waiting.appendleft(r)
+                continue
+            r.slot, r.admitted = s, t
+            self.active[s] = r
+        return len([s for s in slots if s is not None])
+
+    def _retire(self, reqs: List[Request]) -> None:
+        if not reqs:
+            return
+        by_model: Dict[str, List[Request]] = collections.defaultdict(list)
+        for r in reqs:
+            by_model[r.model].append(r)
+        t = self.now()
+        for key, rs in by_model.items():
+            entry = self.models[key]
+            slots = [r.slot for r in rs]
+            ps, ig, times, steps, status = self.pool.results(slots, entry.nproc)
+            occ = self.pool.occupation_counts(slots, entry.nspecies * entry.spuck)
+            for i, r in enumerate(rs):
+                cells = int(np.prod(r.size))
+                if status[i] not in (0, 3):
+                    r.error = "status %d" % status[i]
+                tt = times[i] if times[i] > 0 else np.inf
+                r.result = {
+                    "kmc_time": float(times[i]), "kmc_step": int(steps[i]), "status": int(status[i]),
+                    "procstat": ps[i], "integ_rates": ig[i],
+                    "tof": dict(zip(entry.tof_names, entry.tof_matrix @ ps[i] / tt / cells)),
+                    "tof_integ": dict(zip(entry.tof_names, entry.tof_matrix @ ig[i] / tt / cells)),
+                    "coverage": occ[i].reshape(entry.nspecies, entry.spuck) / cells,
+                }
+                r.done = t
+                self.pool.release(r.slot)
+                del self.active[r.slot]
+                self.finished.append(r)
+
+    def run_quantum(self) -> None:
+        """One persistent launch advancing every active trajectory."""
+        if not self.active:
+            return
+        slots = list(self.active)
+        steps = [min(self.active[s].remaining, self.quantum) for s in slots]
+        before = self.pool.results(slots, 1)[3]
+        self.pool.run(slots, steps, sync=True)
+        self.quanta += 1
+        _ps, _ig, _t, after, statuses = self.pool.results(slots, 1)
+        done = []
+        for s, n, k0, k1, st in zip(slots, steps, before, after, statuses):
+            r = self.active[s]
+            self.kmc_steps += int(k1 - k0)
+            r.remaining -= n
+            # a trajectory that found no process (absorbing state) ends early, as the
+            # reference stops there
+            if r.remaining <= 0 or st != 0:
+                r.remaining = 0
+                done.append(r)
+        self._retire(done)
+
+    def serve(self, arrivals: Sequence[Request], until_empty: bool = True, deadline: float = float("inf")):
+        """Feeds ``arrivals`` (sorted by arrival time, server clock) and runs quanta
+        until every request finished (or ``deadline`` seconds passed)."""
+        pending = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
+        self.t0 = time.perf_counter()
+        while pending or self.waiting or self.active:
+            t = self.now()
+            if t > deadline:
+                break
+            while pending and pending[0].arrival <= t:
+                self.submit(pending.popleft())
+            self._admit()
+            if self.active:
+                self.run_quantum()
+            elif pending:
+                time.sleep(max(0.0, min(0.01, pending[0].arrival - self.now())))
+            if not until_empty and not pending:
+                break
+        return self.finished
+
+    def close(self):
+        self.pool.close()
+
+
+def latency_stats(reqs: Sequence[Request]) -> dict:
+    lat = np.array([r.done - r.arrival for r in reqs if r.done >= 0])
+    if len(lat) == 0:
+        return {"completed": 0}
+    return {"completed": int(len(lat)), "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}
