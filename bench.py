@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--cpu-baseline", type=int, default=1)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--bps", type=int, default=0)
+    ap.add_argument("--sides", default="", help="config 3: comma-separated lattice sides to draw from")
+    ap.add_argument("--fast", type=int, default=1, help="gather / replay step path (0: serial interpreter)")
     return ap.parse_args()
 
 
@@ -238,7 +240,8 @@ def run_ours(args, dist: Dist):
     from kmos_gb300 import configs, engine as E
 
     chunk = args.chunk or DEFAULT_CHUNK[args.config]
-    wl = configs.build(args.config, n=args.ntraj or None)
+    sides = [int(x) for x in args.sides.split(",")] if args.sides else None
+    wl = configs.build(args.config, n=args.ntraj or None, sides=sides)
     n = wl.n
     dev = dist.local
     pool_probe = None
@@ -251,6 +254,8 @@ def run_ours(args, dist: Dist):
     pool = E.Pool(arena_bytes=need + (64 << 20), max_slots=n, device=dev)
     if args.warps or args.bps:
         pool.set_launch(args.warps, args.bps)
+    if not args.fast:
+        pool.set_fast_path(False)
     mid = pool.add_model(wl.program)
     trajs = [t + dist.rank * n for t in wl.trajs]
     slots = []

@@ -206,6 +206,11 @@ KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
  * the region to finish and returns its device time in ms. */
 KMC_API int kmc_pool_timer_start(kmc_pool *pool);
 KMC_API int kmc_pool_timer_stop(kmc_pool *pool, float *ms);
+/* Cycles the step kernel spent per phase, summed over warps, in builds compiled with
+ * KMC_PHASE_TIMING (12 entries: draws, accum, clock/integ/bisection, site pick, slot
+ * gather, edit evaluation, process heads, replay, lattice writes, serial interpreter,
+ * term refresh, spare); other builds return KMC_ERR_ARG.  reset != 0 clears the sums. */
+KMC_API int kmc_pool_phase_cycles(kmc_pool *pool, uint64_t *out, int32_t reset);
 /* Kernel launches issued by this pool since creation. */
 KMC_API int kmc_pool_launch_count(kmc_pool *pool, int64_t *count);
 

@@ -32,18 +32,23 @@ def needs_build() -> bool:
     return any(os.path.getmtime(d) > t for d in DEPS)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not needs_build():
+def build(force: bool = False, verbose: bool = False, phase_timing: bool = False) -> str:
+    """Builds the library (``phase_timing``: a separate libkmcgb300_timing.so with the
+    step kernel's per-phase cycle accounting compiled in)."""
+    lib = LIB.replace(".so", "_timing.so") if phase_timing else LIB
+    if not force and not phase_timing and not needs_build():
         return LIB
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib + ".tmp%d" % os.getpid()
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-shared",
            "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
            "-I", os.path.join(ROOT, "include"), "-o", tmp, *SOURCES]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
+    if phase_timing:
+        cmd.insert(1, "-DKMC_PHASE_TIMING")
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

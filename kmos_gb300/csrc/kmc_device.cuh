@@ -320,6 +320,7 @@ constexpr int FAST_SLOTS = 128;
 constexpr int FAST_EDITS = 96;
 constexpr int LOG_MAX = 12;   // lane-private write log entries
 constexpr int TAIL_MAX = 6;   // lane-private prefetched tail entries
+constexpr int FAST_ROUNDS = FAST_EDITS / 32;
 constexpr int FAST_MAXV = (1 << 23) - 1;
 
 enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
@@ -329,12 +330,12 @@ struct FastSmem {
   int32_t latsite[FAST_SLOTS];
   int8_t ekind[FAST_EDITS];    // E_GDEL / E_DEL / E_ADD
   int16_t ep[FAST_EDITS];      // process, 0-based
-  int8_t heads[FAST_EDITS];    // first edit of each process touched this step
+  int16_t heads[FAST_EDITS];   // processes touched this step, in first-edit order
   int32_t esite[FAST_EDITS];   // target site
   int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
-  uint32_t lkey[32][LOG_MAX];  // lane-private write logs: table << 31 | index
-  int32_t lval[32][LOG_MAX];
   int32_t tail[32][TAIL_MAX];  // lane-private avail_sites(p, n0 - j, 1), j < TAIL_MAX
+  uint32_t lkey[LOG_MAX][32];  // lane-private write logs (lane-minor: no bank conflicts)
+  int32_t lval[LOG_MAX][32];
 };
 
 // The hot section of a model program: fast streams, group records and nli tables with
@@ -346,14 +347,13 @@ struct Hot {
 
 __device__ inline int ref_value(int32_t ref, const int32_t *latv) { return ref >= 0 ? latv[ref] : -ref - 2; }
 
-// nli from slot references: table lookup when the program has one, else a member scan
-__device__ inline int nli_refs(const Hot &H, int g, const int32_t *refs, const int32_t *latv) {
-  const int32_t *rec = H.h + H.h[H.grp + g];
-  const int M = rec[0], K = rec[1];
-  const int toff = H.h[H.tab + g];
+// nli of one edit: table lookup when the group has one, else a member scan.  The edit
+// carries the group's table and record offsets (hot-relative) and its K references.
+__device__ inline int nli_refs(const Hot &H, int K, int toff, int roff, const int32_t *refs, const int32_t *latv) {
   if (toff) {
     const int base = H.nspecies + 1;
     int idx = 0, mul = 1;
+#pragma unroll 4
     for (int k = 0; k < K; k++) {
       const int s = ref_value(refs[k], latv);
       idx += (s < 0 ? H.nspecies : s) * mul;
@@ -361,6 +361,8 @@ __device__ inline int nli_refs(const Hot &H, int g, const int32_t *refs, const i
     }
     return H.h[toff + idx];
   }
+  const int32_t *rec = H.h + roff;
+  const int M = rec[0];
   int result = 0;
   const int32_t *mem = rec + 2 + K;
   for (int m = 0; m < M; m++, mem += 1 + K) {

@@ -47,79 +47,119 @@ using namespace kmc;
 
 #define KMC_MAXK 16
 
+// Cycle accounting per step phase (builds with -DKMC_PHASE_TIMING only): lane 0 adds the
+// clock64() time since the previous mark to phase i of its warp.
+#ifdef KMC_PHASE_TIMING
+#define KMC_PHASE(sm, i)                                \
+  do {                                                  \
+    __syncwarp();                                       \
+    if ((threadIdx.x & 31) == 0) {                      \
+      const long long now_ = clock64();                 \
+      (sm).ph[i] += now_ - (sm).tprev;                  \
+      (sm).tprev = now_;                                \
+    }                                                   \
+  } while (0)
+#else
+#define KMC_PHASE(sm, i) \
+  do {                   \
+  } while (0)
+#endif
+constexpr int KMC_NPHASE = 12;
+
 template <int NP>
 struct WarpSmem {
   double rates[NP * 32];
   double accum[NP * 32];
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
-  int32_t owner[NP * 32];  // first edit of each process this step (INT_MAX when none)
+  uint32_t pmask[NP * 32][FAST_ROUNDS];  // edits of each process this step, one bit per edit
+  long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
+  long long tprev;
   FastSmem f;
 };
 
-// Replays the edits of process p (the edits k >= head with ep[k] == p) in program
-// order.  Lane-private; returns a status.
-__device__ int replay_process(FastSmem &f, int32_t *ns, const View &v, int head, int ne, int lane) {
-  const int p = f.ep[head];
+// Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
+// returns a status.  Clears pmask[p].
+template <int NP>
+__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], const View &v, int p,
+                              int rounds, int lane) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
   const int n0 = ns[p];
+  uint32_t bits[FAST_ROUNDS];
+#pragma unroll
+  for (int r = 0; r < FAST_ROUNDS; r++) {
+    bits[r] = r < rounds ? pmask[p][r] : 0u;
+    pmask[p][r] = 0u;
+  }
   // issue every load the dels can need
-  int r = 0;
-  for (int k = head; k < ne; k++) {
-    if (f.ep[k] != p || f.ekind[k] == E_ADD) continue;
-    f.em[k] = a2[f.esite[k]];
-    if (r < TAIL_MAX) f.tail[lane][r] = (n0 - r >= 1) ? a1[n0 - r] : 0;
-    r++;
+  int nd = 0;
+#pragma unroll
+  for (int r = 0; r < FAST_ROUNDS; r++) {
+    uint32_t b = bits[r];
+    while (b) {
+      const int k = 32 * r + __ffs(b) - 1;
+      b &= b - 1;
+      if (f.ekind[k] == E_ADD) continue;
+      f.em[k] = a2[f.esite[k]];
+      if (nd < TAIL_MAX) f.tail[lane][nd] = (n0 - nd >= 1) ? a1[n0 - nd] : 0;
+      nd++;
+    }
   }
   // apply the edits; reads look in the write log, then at the prefetched values
-  int n = n0, nlog = 0;
+  int nlog = 0;
   bool logok = true;
   auto put = [&](int table, int index, int32_t val) {
     if (table) a2[index] = val; else a1[index] = val;
-    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
     if (!logok) return;
+    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
     for (int i = nlog - 1; i >= 0; i--)
-      if (f.lkey[lane][i] == key) { f.lval[lane][i] = val; return; }
-    if (nlog < LOG_MAX) { f.lkey[lane][nlog] = key; f.lval[lane][nlog] = val; nlog++; }
+      if (f.lkey[i][lane] == key) { f.lval[i][lane] = val; return; }
+    if (nlog < LOG_MAX) { f.lkey[nlog][lane] = key; f.lval[nlog][lane] = val; nlog++; }
     else logok = false;
   };
   auto logged = [&](int table, int index, int32_t &val) -> bool {
     const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
     for (int i = nlog - 1; i >= 0; i--)
-      if (f.lkey[lane][i] == key) { val = f.lval[lane][i]; return true; }
+      if (f.lkey[i][lane] == key) { val = f.lval[i][lane]; return true; }
     return false;
   };
-  for (int k = head; k < ne; k++) {
-    if (f.ep[k] != p) continue;
-    const int kind = f.ekind[k], site = f.esite[k];
-    if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
-      n += 1;
-      put(0, n, site);
-      put(1, site, n);
-      continue;
+  int n = n0;
+#pragma unroll
+  for (int r = 0; r < FAST_ROUNDS; r++) {
+    uint32_t b = bits[r];
+    while (b) {
+      const int k = 32 * r + __ffs(b) - 1;
+      b &= b - 1;
+      const int kind = f.ekind[k], site = f.esite[k];
+      if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
+        n += 1;
+        put(0, n, site);
+        put(1, site, n);
+        continue;
+      }
+      // del_proc (base.mpy:211-265)
+      int m;
+      if (!logok) m = a2[site];
+      else if (nlog == 0 || !logged(1, site, m)) m = f.em[k];
+      if (m == 0) {
+        if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
+        continue;                            // guarded del of an absent entry
+      }
+      if (m < n) {
+        int last;
+        if (!logok) last = a1[n];
+        else if (nlog == 0 || !logged(0, n, last)) last = (n0 - n < TAIL_MAX && n <= n0) ? f.tail[lane][n0 - n] : a1[n];
+        put(0, m, last);
+        put(0, n, 0);
+        put(1, last, m);
+      } else {
+        put(0, m, 0);
+      }
+      put(1, site, 0);
+      n -= 1;
     }
-    // del_proc (base.mpy:211-265)
-    int m;
-    if (!logok) m = a2[site];
-    else if (!logged(1, site, m)) m = f.em[k];
-    if (m == 0) {
-      if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
-      continue;                            // guarded del of an absent entry
-    }
-    if (m < n) {
-      int last;
-      if (!logok) last = a1[n];
-      else if (!logged(0, n, last)) last = (n0 - n < TAIL_MAX && n <= n0) ? f.tail[lane][n0 - n] : a1[n];
-      put(0, m, last);
-      put(0, n, 0);
-      put(1, last, m);
-    } else {
-      put(0, m, 0);
-    }
-    put(1, site, 0);
-    n -= 1;
   }
   ns[p] = n;
   return ST_OK;
@@ -147,6 +187,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   bool bad = false;
   for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);
   if (__any_sync(0xffffffffu, bad)) return ST_SPECIES;
+  KMC_PHASE(sm, 4);
   // 2. evaluate every edit in parallel; compact the ones that happen, in order
   int ne = 0;
   for (int r = 0; r < nedit; r += 32) {
@@ -164,7 +205,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], f.latv), e[2 + cnt + c]);
         p = arg; kind = E_ADD;
       } else {
-        p = nli_refs(H, arg, e + 2, f.latv);
+        p = nli_refs(H, cnt, e[2], e[3], e + 4, f.latv);
         on = p != 0;
         kind = op == 4 ? E_DEL : E_ADD;
       }
@@ -176,32 +217,45 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       f.ekind[pos] = (int8_t)kind;
       f.ep[pos] = (int16_t)(p - 1);
       f.esite[pos] = site;
-      atomicMin(&sm.owner[p - 1], pos);
     }
     ne += __popc(b);
   }
   __syncwarp();
-  // 3. one lane per process touched: the process's first edit heads its chain
+  KMC_PHASE(sm, 5);
+  // 3. per process, the bit mask of its edits in each round of 32; a process whose
+  //    first edit this is becomes a head
   int nh = 0;
-  for (int r = 0; r < ne; r += 32) {
-    const int k = r + lane;
-    const bool head = k < ne && sm.owner[f.ep[k]] == k;
-    const unsigned b = __ballot_sync(0xffffffffu, head);
-    if (head) f.heads[nh + __popc(b & lt)] = (int8_t)k;
-    nh += __popc(b);
+  const int rounds = (ne + 31) >> 5;
+  for (int r = 0; r < rounds; r++) {
+    const int k = 32 * r + lane;
+    const int p = k < ne ? f.ep[k] : -1 - lane;
+    const unsigned m = __match_any_sync(0xffffffffu, p);
+    const bool leader = k < ne && (__ffs(m) - 1) == lane;
+    bool head = false;
+    if (leader) {
+      head = true;
+      for (int q = 0; q < r; q++) head = head && sm.pmask[p][q] == 0u;
+    }
+    __syncwarp();
+    if (leader) sm.pmask[p][r] = m;
+    const unsigned hb = __ballot_sync(0xffffffffu, head);
+    if (head) f.heads[nh + __popc(hb & lt)] = (int16_t)p;
+    nh += __popc(hb);
+    __syncwarp();
   }
-  __syncwarp();
-  for (int k = lane; k < ne; k += 32) sm.owner[f.ep[k]] = 0x7FFFFFFF;
+  KMC_PHASE(sm, 6);
   int err = ST_OK;
   for (int h = lane; h < nh; h += 32) {
-    const int e = replay_process(f, sm.ns, v, f.heads[h], ne, lane);
+    const int e = replay_process<NP>(f, sm.ns, sm.pmask, v, f.heads[h], rounds, lane);
     if (e) err = e;
   }
+  KMC_PHASE(sm, 7);
   // 4. the final species of every replaced slot
   if (!__any_sync(0xffffffffu, err != ST_OK))
     for (int i = lane; i < nwr; i += 32) v.lat[f.latsite[wr[2 * i]] - 1] = (int8_t)wr[2 * i + 1];
   const int e0 = __reduce_max_sync(0xffffffffu, (unsigned)err);
   __syncwarp();
+  KMC_PHASE(sm, 8);
   return e0;
 }
 
@@ -218,6 +272,7 @@ struct RunArgs {
   int32_t fast;                   // 1: use the gather / replay path where it applies
   int32_t model;                  // every listed slot runs this model
   int32_t stage_words;            // hot-section words copied to shared memory (0 = read it from global)
+  unsigned long long *phase;      // KMC_NPHASE cycle sums (KMC_PHASE_TIMING builds)
 };
 
 template <int NP>
@@ -238,7 +293,8 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
   H.nspecies = M.nspecies;
   const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
   WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw + hot_bytes)[wib];
-  for (int i = lane; i < NP * 32; i += 32) sm.owner[i] = 0x7FFFFFFF;
+  for (int i = lane; i < NP * 32 * FAST_ROUNDS; i += 32) (&sm.pmask[0][0])[i] = 0u;
+  for (int i = lane; i < KMC_NPHASE; i += 32) sm.ph[i] = 0;
   __syncthreads();
 
   for (;;) {
@@ -303,6 +359,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
     int status = ST_OK;
     int64_t k = 0;
     __syncwarp();
+    if (lane == 0) sm.tprev = clock64();
 
     for (; k < nsteps; k++) {
       if (a.cancel && (k & 1023) == 0 && *a.cancel) { status = ST_CANCELLED; break; }
@@ -329,6 +386,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       const double ran_proc = __shfl_sync(0xffffffffu, my_rp, bidx);
       const double ran_site = __shfl_sync(0xffffffffu, my_rs, bidx);
       bidx++;
+      KMC_PHASE(sm, 0);
 
       // update_accum_rate from the first stale entry: entries before it are the same
       // sums of the same terms, so the result equals a full recompute bit for bit
@@ -336,14 +394,18 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
         double acc = from > 0 ? sm.accum[from - 1] : 0.0;
         int i = from;
         if (i == 0) { acc = sm.term[0]; sm.accum[0] = acc; i = 1; }
-#pragma unroll 4
-        for (; i < P; i++) {
-          acc = __dadd_rn(acc, sm.term[i]);
-          sm.accum[i] = acc;
+        for (; i < P; i += 8) {
+          double t8[8];  // load a chunk of terms before the dependent adds
+#pragma unroll
+          for (int j = 0; j < 8; j++) t8[j] = (i + j < P) ? sm.term[i + j] : 0.0;
+#pragma unroll
+          for (int j = 0; j < 8; j++)
+            if (i + j < P) { acc = __dadd_rn(acc, t8[j]); sm.accum[i + j] = acc; }
         }
       }
       from = P;
       __syncwarp();
+      KMC_PHASE(sm, 1);
       const double total = sm.accum[P - 1];
       const long long tbits = __double_as_longlong(total);
       if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
@@ -382,6 +444,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       for (int j = 0; j < NP; j++)
         if (proc == lane + 32 * j) ps[j] += 1;  // increment_procstat
 
+      KMC_PHASE(sm, 2);
       int err = ST_OK;
       const int fs_off = fast_ok ? H.h[proc] : 0;
       int site = 0;
@@ -392,6 +455,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       site = __shfl_sync(0xffffffffu, site, 0);
       int bx, by, bz, bn;
       v.g.coords(site, bx, by, bz, bn);
+      KMC_PHASE(sm, 3);
       if (fs_off) {
         err = fast_step<NP>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
       } else {
@@ -403,6 +467,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
         }
         err = __shfl_sync(0xffffffffu, err, 0);
         __syncwarp();
+        KMC_PHASE(sm, 9);
       }
       if (err) { status = err; break; }
       // refresh the terms of processes whose nr_of_sites changed; accum restarts at
@@ -419,6 +484,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       }
       from = first;
       __syncwarp();
+      KMC_PHASE(sm, 10);
     }
     // random state after the draws actually used: bidx draws of the current batch
     // (a step that found no process has drawn its numbers, as in the reference)
@@ -451,6 +517,10 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
     }
     __syncwarp();
   }
+#ifdef KMC_PHASE_TIMING
+  if (lane == 0 && a.phase)
+    for (int i = 0; i < KMC_NPHASE; i++) atomicAdd(&a.phase[i], (unsigned long long)sm.ph[i]);
+#endif
 }
 
 // -------------------------------------------------------------------- init kernel
@@ -771,6 +841,7 @@ struct kmc_pool {
   int blocks_per_sm = 0;  // 0 = occupancy maximum
   std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> graphs;
   std::mutex mu;
+  unsigned long long *d_phase = nullptr;  // KMC_NPHASE cycle sums
   char *d_res = nullptr;   // results gather buffers
   char *h_res = nullptr;   // pinned
   size_t res_cap = 0;
@@ -956,9 +1027,10 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
           if (arg < 1 || arg > m->P || e + 2 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad add edit");
           for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad add ref");
         } else if (op == 4 || op == 5) {
-          if (arg >= m->ngroups || e + 2 + cnt > hl || cnt != hot[hot[m->hot_grp + arg] + 1])
+          if (arg >= m->ngroups || e + 4 + cnt > hl || cnt != hot[hot[m->hot_grp + arg] + 1] ||
+              hot[e + 2] != hot[m->hot_tab + arg] || hot[e + 3] != hot[m->hot_grp + arg])
             return fail(KMC_ERR_PROGRAM, "bad nli edit");
-          for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad nli ref");
+          for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 4 + c])) return fail(KMC_ERR_PROGRAM, "bad nli ref");
         } else {
           return fail(KMC_ERR_PROGRAM, "bad edit kind");
         }
@@ -1037,6 +1109,7 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
     a.fast = p->fast_path;
     a.model = model;
     a.stage_words = (md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
+    a.phase = p->d_phase;
     const size_t hot_bytes = ((size_t)a.stage_words * 4 + 15) / 16 * 16;
     int rc;
     if (md.P <= 32) rc = plan_kernel<1>(p, L, hot_bytes);
@@ -1142,6 +1215,8 @@ int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_p
   CK(cudaMalloc(&p->d_steps, sizeof(int64_t) * max_slots));
   CK(cudaMalloc(&p->d_counter, sizeof(int32_t) * p->max_models));
   CK(cudaMalloc(&p->d_cmd_out, sizeof(int32_t) * 4));
+  CK(cudaMalloc(&p->d_phase, sizeof(unsigned long long) * KMC_NPHASE));
+  CK(cudaMemset(p->d_phase, 0, sizeof(unsigned long long) * KMC_NPHASE));
   CK(cudaHostAlloc(&p->h_cancel, sizeof(int32_t), cudaHostAllocMapped));
   *p->h_cancel = 0;
   CK(cudaHostGetDevicePointer(&p->d_cancel, p->h_cancel, 0));
@@ -1169,7 +1244,7 @@ int kmc_pool_destroy(kmc_pool *p) {
   for (auto &m : p->models) cudaFree(m.d_prog);
   cudaFree(p->arena); cudaFree(p->d_slots); cudaFree(p->d_models); cudaFree(p->d_list);
   cudaFree(p->d_steps); cudaFree(p->d_counter); cudaFree(p->d_cmd_out); cudaFreeHost(p->h_cancel);
-  cudaFree(p->d_res); cudaFreeHost(p->h_res);
+  cudaFree(p->d_res); cudaFreeHost(p->h_res); cudaFree(p->d_phase);
   cudaFree(p->d_adm_list); cudaFree(p->d_adm_staged); cudaFree(p->d_adm_rates); cudaFree(p->d_adm_roff);
   cudaEventDestroy(p->ev0); cudaEventDestroy(p->ev1); cudaEventDestroy(p->tev0); cudaEventDestroy(p->tev1);
   cudaStreamDestroy(p->stream);
@@ -1399,6 +1474,18 @@ int kmc_pool_timer_stop(kmc_pool *p, float *ms) {
   CK(cudaEventSynchronize(p->tev1));
   CK(cudaEventElapsedTime(ms, p->tev0, p->tev1));
   return KMC_OK;
+}
+
+int kmc_pool_phase_cycles(kmc_pool *p, uint64_t *out, int32_t reset) {
+  if (!p || !out) return fail(KMC_ERR_ARG, "bad arguments");
+  CK(cudaStreamSynchronize(p->stream));
+  CK(cudaMemcpy(out, p->d_phase, sizeof(unsigned long long) * KMC_NPHASE, cudaMemcpyDeviceToHost));
+  if (reset) CK(cudaMemset(p->d_phase, 0, sizeof(unsigned long long) * KMC_NPHASE));
+#ifdef KMC_PHASE_TIMING
+  return KMC_OK;
+#else
+  return fail(KMC_ERR_ARG, "library built without KMC_PHASE_TIMING");
+#endif
 }
 
 int kmc_pool_launch_count(kmc_pool *p, int64_t *count) {

@@ -91,6 +91,7 @@ SIGNATURES = {
     "kmc_pool_timer_start": (_i32, [_vp]),
     "kmc_pool_timer_stop": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_pool_launch_count": (_i32, [_vp, _p64]),
+    "kmc_pool_phase_cycles": (_i32, [_vp, _P(ctypes.c_uint64), _i32]),
 }
 
 _lib = None
@@ -106,15 +107,17 @@ def library_path() -> str:
     return _build.LIB
 
 
-def load(build_if_missing: bool = True):
-    """Loads the engine library (building it first if it is missing or stale)."""
+def load(build_if_missing: bool = True, path: Optional[str] = None):
+    """Loads the engine library (building it first if it is missing or stale).  ``path``
+    selects another build of the same C-ABI (the phase-timing build)."""
     global _lib
     if _lib is None:
-        if build_if_missing and _build.needs_build():
+        if path is None and build_if_missing and _build.needs_build():
             _build.build()
-        if not os.path.exists(_build.LIB):
-            raise RuntimeError("kmc engine library %s is missing; run kmos_gb300.build.build()" % _build.LIB)
-        L = ctypes.CDLL(_build.LIB)
+        lib = path or _build.LIB
+        if not os.path.exists(lib):
+            raise RuntimeError("kmc engine library %s is missing; run kmos_gb300.build.build()" % lib)
+        L = ctypes.CDLL(lib)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res
@@ -397,6 +400,13 @@ class Pool:
         ms = ctypes.c_float()
         _check(load().kmc_pool_timer_stop(self.h, ctypes.byref(ms)))
         return ms.value
+
+    def phase_cycles(self, reset: bool = True) -> np.ndarray:
+        """Per-phase cycle sums of the step kernel (library built with KMC_PHASE_TIMING)."""
+        out = np.zeros(12, np.uint64)
+        _check(load().kmc_pool_phase_cycles(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                            1 if reset else 0))
+        return out
 
     def launch_count(self) -> int:
         c = _i64()

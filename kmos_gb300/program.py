@@ -68,6 +68,8 @@ had before the step.  All edits of a step can therefore be evaluated in parallel
     [nlat, nchk, nwr, nedit, coord * nlat, (slot, old_mask) * nchk,
      (slot, species) * nwr, edit_offset * nedit, edits...]
     edit  [kind | cnt << 8 | arg << 16, target coord, ref * cnt, (mask * cnt for adds)]
+          nli edits: [h, target coord, table offset, record offset, ref * cnt] with the
+          hot-relative offsets of the group's nli table (0 = none) and member record
     kind  2 = guarded del (arg = proc), 3 = add (arg = proc, cnt conditions),
           4 = nli del, 5 = nli add (arg = group, cnt = the group's K coordinates)
     ref   >= 0: slot index (value before the step); < 0: constant species -ref-2
@@ -562,7 +564,9 @@ class ProgramBuilder:
                 g, o = op[1], op[2]
                 coords, _mems = records[g]
                 refs = [ref(slot((o[0] + c[0], o[1] + c[1], o[2] + c[2], c[3]))) for c in coords]
-                edits.append([op_header(4 if kind == "li_del" else 5, len(coords), g), pack_coord(*o)] + refs)
+                # the group's nli table and record offsets are filled in by build()
+                edits.append([op_header(4 if kind == "li_del" else 5, len(coords), g), pack_coord(*o),
+                              ("tab", g), ("rec", g)] + refs)
                 reach = [max(reach[i], abs(o[i])) for i in range(3)]
             else:
                 return None
@@ -649,6 +653,7 @@ class ProgramBuilder:
             hot[p] = len(hot)
             hot.extend(words)
         hot[P] = len(hot)
+        fixups = [i for i, x in enumerate(hot) if isinstance(x, tuple)]
         grp_off = len(hot)
         hot.extend([0] * max(ngroups, 1))
         tab_off = len(hot)
@@ -680,6 +685,9 @@ class ProgramBuilder:
                 table.append(result)
             hot[tab_off + gi] = len(hot)
             hot.extend(table)
+        for i in fixups:
+            what, gi = hot[i]
+            hot[i] = hot[tab_off + gi] if what == "tab" else hot[grp_off + gi]
         w.emit(*hot)
         header = [MAGIC, VERSION, BACKENDS[self.backend], P, len(m.species), self.null, m.spuck,
                   m.dimension, ngroups, len(m.layers), off_proc, off_touch, off_groups,
