@@ -178,11 +178,9 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   const int32_t *eoff = wr + 2 * nwr;
   const unsigned lt = (1u << lane) - 1u;
   // 1. gather every slot; check the old species of first replaces
-  for (int i = lane; i < nlat; i += 32) {
-    const int s = v.g.site(bx, by, bz, coords[i]);
-    f.latsite[i] = s;
-    f.latv[i] = v.lat[s - 1];
-  }
+  for (int i = lane; i < nlat; i += 32) f.latsite[i] = v.g.site(bx, by, bz, coords[i]);
+  KMC_PHASE(sm, 11);
+  for (int i = lane; i < nlat; i += 32) f.latv[i] = v.lat[f.latsite[i] - 1];
   __syncwarp();
   bool bad = false;
   for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);

@@ -220,3 +220,39 @@ def latency_stats(reqs: Sequence[Request]) -> dict:
         return {"completed": 0}
     return {"completed": int(len(lat)), "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean())}
+
+
+def main(argv=None):
+    """Configuration 5 on one GPU: ``python -m kmos_gb300.serving [--rate R] [--duration S]
+    [--steps-scale F]``; prints one JSON line with p50/p99 latency and steps/s."""
+    import argparse
+    import json
+    from . import configs
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rate", type=float, default=500.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--steps-scale", type=float, default=1.0)
+    ap.add_argument("--quantum", type=int, default=20000)
+    ap.add_argument("--arena-gb", type=float, default=64.0)
+    ap.add_argument("--deadline", type=float, default=float("inf"))
+    a = ap.parse_args(argv)
+    reqs, progs = configs.serving_requests(rate=a.rate, duration=a.duration, steps_scale=a.steps_scale)
+    srv = Server(arena_bytes=int(a.arena_gb * (1 << 30)), max_slots=16384, quantum=a.quantum)
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    t0 = time.perf_counter()
+    done = srv.serve(reqs, deadline=a.deadline)
+    wall = time.perf_counter() - t0
+    stats = latency_stats(done)
+    offered = sum(r.steps for r in reqs)
+    line = {"metric": "serving p50/p99 request latency", "requests": len(reqs), "rate_per_s": a.rate,
+            "duration_s": a.duration, "steps_scale": a.steps_scale, "quantum": a.quantum,
+            "offered_steps": offered, "served_steps": srv.kmc_steps, "wall_s": wall,
+            "steps_per_s": srv.kmc_steps / wall, "quanta": srv.quanta, **stats}
+    srv.close()
+    print(json.dumps(line))
+    return line
+
+
+if __name__ == "__main__":
+    main()
