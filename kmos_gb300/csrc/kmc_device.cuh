@@ -140,6 +140,19 @@ struct Geometry {
     const int n = (int)(u >> 24);
     return spuck * (wrapc(bx + dx, X) + X * (wrapc(by + dy, Y) + Y * wrapc(bz + dz, Z))) + n;
   }
+  // site() for offsets smaller than the lattice in every axis (the fast path's
+  // precondition): one conditional add or subtract per axis instead of a modulo
+  __host__ __device__ inline int site_near(int bx, int by, int bz, int32_t w) const {
+    const uint32_t u = (uint32_t)w;
+    int x = bx + (int8_t)(u & 0xFF), y = by + (int8_t)((u >> 8) & 0xFF), z = bz + (int8_t)((u >> 16) & 0xFF);
+    x += x < 0 ? X : 0;
+    x -= x >= X ? X : 0;
+    y += y < 0 ? Y : 0;
+    y -= y >= Y ? Y : 0;
+    z += z < 0 ? Z : 0;
+    z -= z >= Z ? Z : 0;
+    return spuck * (x + X * (y + Y * z)) + (int)(u >> 24);
+  }
   __host__ __device__ inline void cell(int bx, int by, int bz, int32_t w, int &cx, int &cy, int &cz) const {
     const uint32_t u = (uint32_t)w;
     cx = bx + (int8_t)(u & 0xFF);

@@ -178,7 +178,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   const int32_t *eoff = wr + 2 * nwr;
   const unsigned lt = (1u << lane) - 1u;
   // 1. gather every slot; check the old species of first replaces
-  for (int i = lane; i < nlat; i += 32) f.latsite[i] = v.g.site(bx, by, bz, coords[i]);
+  for (int i = lane; i < nlat; i += 32) f.latsite[i] = v.g.site_near(bx, by, bz, coords[i]);
   KMC_PHASE(sm, 11);
   for (int i = lane; i < nlat; i += 32) f.latv[i] = v.lat[f.latsite[i] - 1];
   __syncwarp();
@@ -207,7 +207,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         on = p != 0;
         kind = op == 4 ? E_DEL : E_ADD;
       }
-      if (on) site = v.g.site(bx, by, bz, e[1]);
+      if (on) site = v.g.site_near(bx, by, bz, e[1]);
     }
     const unsigned b = __ballot_sync(0xffffffffu, on);
     if (on) {
@@ -408,19 +408,6 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       const long long tbits = __double_as_longlong(total);
       if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
 
-      // update_clocks: kmc_time += -log(r)/accum(P), the quotient as -log(r) times the
-      // reciprocal of accum(P) (within 2 ulp of the quotient)
-      dt = __dmul_rn(nl, __drcp_rn(total));
-      t = __dadd_rn(t, dt);
-      kstep += 1;
-
-      // update_integ_rate: integ(i) = integ(i) + n(i)*r(i)*dt
-#pragma unroll
-      for (int j = 0; j < NP; j++) {
-        const int i = lane + 32 * j;
-        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(sm.term[i], dt));
-      }
-
       // determine_procsite: for non-negative doubles the order of the bit patterns is
       // the order of the values
       const long long vbits = __double_as_longlong(__dmul_rn(ran_proc, total));
@@ -446,10 +433,21 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
       int err = ST_OK;
       const int fs_off = fast_ok ? H.h[proc] : 0;
       int site = 0;
-      if (lane == 0) {
-        site = v.as1[(size_t)proc * stride + idx];
-        if (a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
+      if (lane == 0) site = v.as1[(size_t)proc * stride + idx];
+
+      // while the site load is in flight: update_clocks, kmc_time += -log(r)/accum(P)
+      // with the quotient as -log(r) times the reciprocal of accum(P) (within 2 ulp),
+      // and update_integ_rate, integ(i) = integ(i) + n(i)*r(i)*dt
+      dt = __dmul_rn(nl, __drcp_rn(total));
+      t = __dadd_rn(t, dt);
+      kstep += 1;
+#pragma unroll
+      for (int j = 0; j < NP; j++) {
+        const int i = lane + 32 * j;
+        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(sm.term[i], dt));
       }
+
+      if (lane == 0 && a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
       site = __shfl_sync(0xffffffffu, site, 0);
       int bx, by, bz, bn;
       v.g.coords(site, bx, by, bz, bn);
