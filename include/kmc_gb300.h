@@ -214,6 +214,67 @@ KMC_API int kmc_pool_phase_cycles(kmc_pool *pool, uint64_t *out, int32_t reset);
 /* Kernel launches issued by this pool since creation. */
 KMC_API int kmc_pool_launch_count(kmc_pool *pool, int64_t *count);
 
+/* ------------------------------------------------------------------------------
+ * Saving and restoring trajectories (base.save_system / base.reload_system,
+ * base.mpy:363-578)
+ * ------------------------------------------------------------------------------ */
+
+/* Compact binary image of one trajectory: clock, step, random stream, status,
+ * rates / integ_rates / accum_rates / procstat / nr_of_sites, the lattice and the first
+ * nr_of_sites(p) entries of avail_sites(p, :, 1) per process (the rest of the tables is
+ * rebuilt on load).  *bytes receives the image size; with buf NULL nothing else is done,
+ * and a capacity below it returns KMC_ERR_ARG.  Unlike the reference's .reload file the
+ * image keeps integ_rates, kmc_time_step and the random stream, so a restored trajectory
+ * continues bit for bit. */
+KMC_API int kmc_pool_save_state(kmc_pool *pool, int32_t slot, void *buf, size_t capacity, size_t *bytes);
+/* Admits a trajectory from an image saved from the same model program (checked by a
+ * hash); the image is validated (sizes, species, every table index) before it reaches
+ * the device.  The new slot id goes to *slot. */
+KMC_API int kmc_pool_restore_state(kmc_pool *pool, int32_t model_id, const void *buf, size_t bytes, int32_t *slot);
+/* The same on a handle; kmc_load_state needs an image of the handle's model and size. */
+KMC_API int kmc_save_state(kmc_handle *h, void *buf, size_t capacity, size_t *bytes);
+KMC_API int kmc_load_state(kmc_handle *h, const void *buf, size_t bytes);
+/* base.save_system (base.mpy:489-575): writes the reference's <system_name>.reload
+ * layout to `path`, plus "#gb300" comment lines (system size, exact kmc_time, rates and
+ * integ_rates, kmc_time_step, random stream) that the reference's reader skips. */
+KMC_API int kmc_save_reload(kmc_handle *h, const char *path);
+/* First pass of base.reload_system (base.mpy:363-440): nr_of_proc, volume and, from a
+ * "#gb300 system_size" line, the system size (zeros when the file has none). */
+KMC_API int kmc_reload_info(const char *path, int32_t *nr_of_proc, int32_t *volume, int32_t dims[3]);
+/* Second pass of base.reload_system (base.mpy:442-486) into an allocated handle of the
+ * same model and volume: kmc_time, walltime, kmc_step, lattice, nr_of_sites, rates,
+ * procstat, avail_sites and avail_sites_back, checked for consistency (KMC_ERR_TABLE).
+ * Without "#gb300" lines integ_rates and kmc_time_step restart at zero and the handle's
+ * random stream continues, as in the reference. */
+KMC_API int kmc_load_reload(kmc_handle *h, const char *path);
+/* base.get_walltime: host seconds spent in kmc_do_steps (the reference adds CPU_TIME
+ * every step, base.mpy:1123-1161). */
+KMC_API int kmc_get_walltime(kmc_handle *h, double *walltime);
+
+/* ------------------------------------------------------------------------------
+ * On-device sampling (kmos.run.KMC_Model.get_std_sampled_data, run/__init__.py:865-966)
+ * ------------------------------------------------------------------------------ */
+
+/* Starts a sampling record for each listed slot (arena memory; KMC_ERR_NOMEM when full):
+ * kmc_time, kmc_step, procstat and integ_rates now. */
+KMC_API int kmc_pool_sample_begin(kmc_pool *pool, const int32_t *slots, int32_t n);
+/* One sample per listed slot, on the pool stream after the work queued before it: the
+ * occupation (get_occupation) weighted by kmc_time_step is added to the record. */
+KMC_API int kmc_pool_sample(kmc_pool *pool, const int32_t *slots, int32_t n);
+/* Ends the records: per slot i, occ_mean[i][occ_stride] = the kmc_time_step-weighted
+ * mean occupation ([nspecies][spuck], NaN when every weight was zero),
+ * procstat_delta / integ_delta[i][proc_stride] = the change since kmc_pool_sample_begin,
+ * times[i] = {total_time, simulated_time}, steps[i] = kMC steps taken, status[i]. */
+KMC_API int kmc_pool_sample_end(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t occ_stride,
+                                int32_t proc_stride, double *occ_mean, int64_t *procstat_delta,
+                                double *integ_delta, double *times, int64_t *steps, int32_t *status);
+/* begin, then `samples` times (run steps_per_sample kMC steps on every listed slot,
+ * sample), then end -- all queued on the device without a host round trip. */
+KMC_API int kmc_pool_sample_run(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t samples,
+                                int64_t steps_per_sample, int32_t occ_stride, int32_t proc_stride,
+                                double *occ_mean, int64_t *procstat_delta, double *integ_delta, double *times,
+                                int64_t *steps, int32_t *status);
+
 #ifdef __cplusplus
 }
 #endif

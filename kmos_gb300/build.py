@@ -8,13 +8,15 @@ from __future__ import annotations
 import os
 import shutil
 import subprocess
+import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libkmcgb300.so")
-SOURCES = [os.path.join(CSRC, "kmc_engine.cu")]
-DEPS = SOURCES + [os.path.join(CSRC, "kmc_device.cuh"), os.path.join(ROOT, "include", "kmc_gb300.h")]
+SOURCES = [os.path.join(CSRC, "kmc_engine.cu"), os.path.join(CSRC, "kmc_state.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, "kmc_device.cuh"), os.path.join(CSRC, "kmc_host.h"),
+                  os.path.join(ROOT, "include", "kmc_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -34,19 +36,28 @@ def needs_build() -> bool:
 
 def build(force: bool = False, verbose: bool = False, phase_timing: bool = False) -> str:
     """Builds the library (``phase_timing``: a separate libkmcgb300_timing.so with the
-    step kernel's per-phase cycle accounting compiled in)."""
+    step kernel's per-phase cycle accounting compiled in).  Translation units compile in
+    parallel, then link into one shared object."""
     lib = LIB.replace(".so", "_timing.so") if phase_timing else LIB
     if not force and not phase_timing and not needs_build():
         return LIB
-    tmp = lib + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-shared",
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-           "-I", os.path.join(ROOT, "include"), "-o", tmp, *SOURCES]
+    flags = [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+             "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
+        flags.insert(0, "-Xptxas=-v")
     if phase_timing:
-        cmd.insert(1, "-DKMC_PHASE_TIMING")
-    subprocess.check_call(cmd)
+        flags.insert(0, "-DKMC_PHASE_TIMING")
+    with tempfile.TemporaryDirectory(prefix="kmcgb300_") as tmpdir:
+        objs, procs = [], []
+        for src in SOURCES:
+            obj = os.path.join(tmpdir, os.path.basename(src) + ".o")
+            objs.append(obj)
+            procs.append(subprocess.Popen([nvcc(), *flags, "-c", "-o", obj, src]))
+        codes = [pr.wait() for pr in procs]
+        if any(codes):
+            raise subprocess.CalledProcessError(max(codes), "nvcc -c")
+        tmp = lib + ".tmp%d" % os.getpid()
+        subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
     os.replace(tmp, lib)
     return lib
 

@@ -197,6 +197,9 @@ __device__ inline void add_proc(View &v, int p, int site) {
   int32_t *a2 = v.as2 + (size_t)(p - 1) * v.stride;
   if (v.collect) { a2[site] = 1; return; }
   const int n = v.ns[p - 1] + 1;
+  // a list can hold every site once; more entries mean the tables no longer match the
+  // lattice (a species replaced without a touch-up): stop instead of leaving the row
+  if (n >= v.stride) { v.err = ST_TABLE; return; }
   v.ns[p - 1] = n;
   a1[n] = site;
   a2[site] = n;

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,8 +43,10 @@
 
 #include "../../include/kmc_gb300.h"
 #include "kmc_device.cuh"
+#include "kmc_host.h"
 
 using namespace kmc;
+using namespace kmc_host;
 
 #define KMC_MAXK 16
 
@@ -134,6 +137,7 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
       b &= b - 1;
       const int kind = f.ekind[k], site = f.esite[k];
       if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
+        if (n + 1 >= v.stride) return ST_TABLE;  // full list: tables out of step with the lattice
         n += 1;
         put(0, n, site);
         put(1, site, n);
@@ -754,8 +758,7 @@ __global__ void kmc_results_kernel(const SlotDev *slots, const int32_t *list, in
 }
 
 // ================================================================== host side
-namespace {
-
+namespace kmc_host {
 thread_local std::string g_err;
 
 int fail(int code, const std::string &msg) {
@@ -763,96 +766,6 @@ int fail(int code, const std::string &msg) {
   return code;
 }
 
-#define CK(call)                                                                           \
-  do {                                                                                     \
-    cudaError_t e_ = (call);                                                               \
-    if (e_ != cudaSuccess) return fail(KMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-struct ModelHost {
-  std::vector<int32_t> prog;
-  int32_t *d_prog = nullptr;
-  ModelDev dev{};
-};
-
-struct SlotHost {
-  bool used = false;
-  size_t off = 0, bytes = 0;
-  SlotDev dev{};
-};
-
-struct GraphKey {
-  int64_t steps;
-  std::vector<int32_t> slots;
-  bool operator==(const GraphKey &o) const { return steps == o.steps && slots == o.slots; }
-};
-struct GraphKeyHash {
-  size_t operator()(const GraphKey &k) const {
-    size_t h = std::hash<int64_t>()(k.steps);
-    for (int32_t s : k.slots) h = h * 1000003u ^ (size_t)s;
-    return h;
-  }
-};
-struct GraphEntry {
-  int64_t nlaunch = 0;
-  cudaGraphExec_t exec = nullptr;
-  cudaGraph_t graph = nullptr;
-  int32_t *d_list = nullptr;
-  int64_t *d_steps = nullptr;
-};
-
-size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
-}  // namespace
-
-struct kmc_pool {
-  int device = 0;
-  int num_sms = 1;
-  cudaStream_t stream = nullptr;
-  char *arena = nullptr;
-  size_t arena_bytes = 0;
-  std::map<size_t, size_t> free_blocks;  // offset -> size
-  std::vector<SlotHost> slots;
-  SlotDev *d_slots = nullptr;
-  std::vector<ModelHost> models;
-  ModelDev *d_models = nullptr;
-  int max_models = 256;
-  int32_t *d_list = nullptr;
-  int64_t *d_steps = nullptr;
-  int32_t *d_counter = nullptr;
-  int32_t *d_cmd_out = nullptr;
-  int32_t *h_cancel = nullptr;   // host-mapped
-  int32_t *d_cancel = nullptr;
-  // admission staging
-  int32_t *d_adm_list = nullptr;
-  SlotDev *d_adm_staged = nullptr;
-  double *d_adm_rates = nullptr;
-  int32_t *d_adm_roff = nullptr;
-  size_t adm_rates_cap = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
-  bool timed = false;
-  int64_t launches = 0;
-  int warps_per_block = 4;
-  int fast_path = 1;
-  int blocks_per_sm = 0;  // 0 = occupancy maximum
-  std::unordered_map<GraphKey, GraphEntry, GraphKeyHash> graphs;
-  std::mutex mu;
-  unsigned long long *d_phase = nullptr;  // KMC_NPHASE cycle sums
-  char *d_res = nullptr;   // results gather buffers
-  char *h_res = nullptr;   // pinned
-  size_t res_cap = 0;
-};
-
-struct kmc_handle {
-  kmc_pool *pool = nullptr;
-  int slot = -1;
-  int model = -1;
-  int P = 0, V = 0, spuck = 1, nspecies = 0;
-  int32_t *d_trace = nullptr;
-  int64_t trace_cap = 0;
-};
-
-namespace {
 
 int alloc_block(kmc_pool *p, size_t bytes, size_t *off) {
   bytes = align_up(bytes, 256);
@@ -886,25 +799,6 @@ void free_block(kmc_pool *p, size_t off, size_t bytes) {
   }
 }
 
-// Byte layout of one slot block.
-struct Layout {
-  size_t lat, as1, as2, rates, integ, accum, nsites, procstat, total;
-};
-
-Layout slot_layout(int P, int V) {
-  Layout L;
-  size_t o = 0;
-  L.lat = o; o = align_up(o + (size_t)V, 16);
-  L.as1 = o; o = align_up(o + (size_t)P * (V + 1) * 4, 16);
-  L.as2 = o; o = align_up(o + (size_t)P * (V + 1) * 4, 16);
-  L.rates = o; o += (size_t)P * 8;
-  L.integ = o; o += (size_t)P * 8;
-  L.accum = o; o += (size_t)P * 8;
-  L.procstat = o; o += (size_t)P * 8;
-  L.nsites = o; o = align_up(o + (size_t)P * 4, 16);
-  L.total = o;
-  return L;
-}
 
 int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
   if (!prog || len < 20) return fail(KMC_ERR_PROGRAM, "program too short");
@@ -1154,6 +1048,25 @@ int launch_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, i
   return issue_run(p, plans, d_list, d_steps, d_trace);
 }
 
+int run_rounds(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, int rounds,
+               const std::function<int(int)> &after) {
+  std::vector<int32_t> ls;
+  std::vector<int64_t> st;
+  std::vector<LaunchPlan> plans;
+  int rc = plan_run(p, slots, steps, n, ls, st, plans);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(p->d_list, ls.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  CK(cudaMemcpyAsync(p->d_steps, st.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, p->stream));
+  *p->h_cancel = 0;
+  for (int r = 0; r < rounds; r++) {
+    rc = issue_run(p, plans, p->d_list, p->d_steps, nullptr);
+    if (rc) return rc;
+    rc = after(r);
+    if (rc) return rc;
+  }
+  return KMC_OK;
+}
+
 int read_slot(kmc_pool *p, int slot, SlotDev *out) {
   CK(cudaStreamSynchronize(p->stream));
   CK(cudaMemcpy(out, p->d_slots + slot, sizeof(SlotDev), cudaMemcpyDeviceToHost));
@@ -1181,7 +1094,7 @@ int run_command(kmc_pool *p, int slot, int cmd, int a0, int a1, int a2, int32_t 
   return KMC_OK;
 }
 
-}  // namespace
+}  // namespace kmc_host
 
 // ===================================================================== C-ABI
 extern "C" {
@@ -1373,6 +1286,7 @@ int kmc_pool_release(kmc_pool *p, int32_t slot) {
   std::lock_guard<std::mutex> lock(p->mu);
   CK(cudaStreamSynchronize(p->stream));
   free_block(p, p->slots[slot].off, p->slots[slot].bytes);
+  if (p->slots[slot].samp_bytes) free_block(p, p->slots[slot].samp_off, p->slots[slot].samp_bytes);
   p->slots[slot] = SlotHost();
   return KMC_OK;
 }
@@ -1771,9 +1685,19 @@ static int finish_run(kmc_handle *h) {
 int kmc_do_steps(kmc_handle *h, int64_t n) {
   HCHECK(h);
   if (n < 0) return fail(KMC_ERR_ARG, "negative step count");
+  const auto t0 = std::chrono::steady_clock::now();
   int rc = kmc_pool_run(h->pool, &h->slot, &n, 1);
   if (rc) return rc;
-  return finish_run(h);
+  rc = finish_run(h);
+  h->walltime += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+int kmc_get_walltime(kmc_handle *h, double *t) {
+  HCHECK(h);
+  if (!t) return fail(KMC_ERR_ARG, "bad arguments");
+  *t = h->walltime;
+  return KMC_OK;
 }
 
 int kmc_trace_steps(kmc_handle *h, int64_t n, int32_t *out) {

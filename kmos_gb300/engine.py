@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import struct
 from typing import Iterable, List, Optional, Sequence
 
 import numpy as np
@@ -92,6 +93,18 @@ SIGNATURES = {
     "kmc_pool_timer_stop": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_pool_launch_count": (_i32, [_vp, _p64]),
     "kmc_pool_phase_cycles": (_i32, [_vp, _P(ctypes.c_uint64), _i32]),
+    "kmc_pool_save_state": (_i32, [_vp, _i32, _vp, _sz, _P(_sz)]),
+    "kmc_pool_restore_state": (_i32, [_vp, _i32, _vp, _sz, _p32]),
+    "kmc_save_state": (_i32, [_vp, _vp, _sz, _P(_sz)]),
+    "kmc_load_state": (_i32, [_vp, _vp, _sz]),
+    "kmc_save_reload": (_i32, [_vp, ctypes.c_char_p]),
+    "kmc_reload_info": (_i32, [ctypes.c_char_p, _p32, _p32, _p32]),
+    "kmc_load_reload": (_i32, [_vp, ctypes.c_char_p]),
+    "kmc_get_walltime": (_i32, [_vp, _pd]),
+    "kmc_pool_sample_begin": (_i32, [_vp, _p32, _i32]),
+    "kmc_pool_sample": (_i32, [_vp, _p32, _i32]),
+    "kmc_pool_sample_end": (_i32, [_vp, _p32, _i32, _i32, _i32, _pd, _p64, _pd, _pd, _p64, _p32]),
+    "kmc_pool_sample_run": (_i32, [_vp, _p32, _i32, _i32, _i64, _i32, _i32, _pd, _p64, _pd, _pd, _p64, _p32]),
 }
 
 _lib = None
@@ -285,6 +298,41 @@ class Trajectory:
         out = np.zeros(self.nspecies * self.spuck)
         _check(load().kmc_get_occupation(self.h, _ptr(out, _dbl)))
         return out.reshape(self.nspecies, self.spuck)
+
+    @property
+    def walltime(self) -> float:
+        t = _dbl()
+        _check(load().kmc_get_walltime(self.h, ctypes.byref(t)))
+        return t.value
+
+    # --- saving and restoring ---
+    def save_state(self) -> bytes:
+        """Compact binary image of the trajectory (``kmc_save_state``)."""
+        n = ctypes.c_size_t()
+        _check(load().kmc_save_state(self.h, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(load().kmc_save_state(self.h, buf, n.value, ctypes.byref(n)))
+        return buf.raw[:n.value]
+
+    def load_state(self, image: bytes):
+        """Loads an image of the same model and system size (``kmc_load_state``)."""
+        _check(load().kmc_load_state(self.h, image, len(image)))
+
+    def save_reload(self, path: str):
+        """base.save_system: writes ``path`` in the reference's .reload layout."""
+        _check(load().kmc_save_reload(self.h, os.fsencode(path)))
+
+    def load_reload(self, path: str):
+        """Second pass of base.reload_system into this trajectory."""
+        _check(load().kmc_load_reload(self.h, os.fsencode(path)))
+
+
+def reload_info(path: str):
+    """(nr_of_proc, volume, system size or None) of a .reload file (``kmc_reload_info``)."""
+    P, V = _i32(), _i32()
+    dims = np.zeros(3, np.int32)
+    _check(load().kmc_reload_info(os.fsencode(path), ctypes.byref(P), ctypes.byref(V), _ptr(dims, _i32)))
+    return P.value, V.value, (None if dims[0] == 0 else [int(d) for d in dims])
 
 
 class Pool:
@@ -484,3 +532,61 @@ class Pool:
         out = np.zeros(len(slots) * stride, np.int64)
         _check(load().kmc_pool_occupation_counts(self.h, _ptr(slots, _i32), len(slots), int(stride), _ptr(out, _i64)))
         return out.reshape(len(slots), stride)
+
+    # --- saving and restoring (base.save_system / reload_system) ---
+    def save_state(self, slot: int) -> bytes:
+        """Compact binary image of a resident trajectory (``kmc_pool_save_state``)."""
+        n = ctypes.c_size_t()
+        _check(load().kmc_pool_save_state(self.h, int(slot), None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(load().kmc_pool_save_state(self.h, int(slot), buf, n.value, ctypes.byref(n)))
+        return buf.raw[:n.value]
+
+    def restore_state(self, model_id: int, image: bytes) -> int:
+        """Admits a trajectory from an image of model ``model_id``; returns its slot."""
+        slot = _i32()
+        _check(load().kmc_pool_restore_state(self.h, int(model_id), image, len(image), ctypes.byref(slot)))
+        s = slot.value
+        self.slot_model[s] = int(model_id)
+        self.slot_volume[s] = struct.unpack_from("<i", image, 44)[0]
+        return s
+
+    # --- on-device sampling (get_std_sampled_data) ---
+    def sample_begin(self, slots):
+        slots = _a32(slots)
+        _check(load().kmc_pool_sample_begin(self.h, _ptr(slots, _i32), len(slots)))
+
+    def sample(self, slots):
+        slots = _a32(slots)
+        _check(load().kmc_pool_sample(self.h, _ptr(slots, _i32), len(slots)))
+
+    def _sample_out(self, slots):
+        n = len(slots)
+        occ_stride = max(int(self.models[self.slot_model[int(s)]][4]) * int(self.models[self.slot_model[int(s)]][6])
+                         for s in slots)
+        proc_stride = max(self.nproc(self.slot_model[int(s)]) for s in slots)
+        return dict(occ=np.zeros((n, occ_stride)), dprocstat=np.zeros((n, proc_stride), np.int64),
+                    dinteg=np.zeros((n, proc_stride)), times=np.zeros((n, 2)), steps=np.zeros(n, np.int64),
+                    status=np.zeros(n, np.int32)), occ_stride, proc_stride
+
+    def _out_args(self, out):
+        return (_ptr(out["occ"], _dbl), _ptr(out["dprocstat"], _i64), _ptr(out["dinteg"], _dbl),
+                _ptr(out["times"], _dbl), _ptr(out["steps"], _i64), _ptr(out["status"], _i32))
+
+    def sample_end(self, slots) -> dict:
+        """Ends the sampling records: per slot the kmc_time_step-weighted mean occupation
+        ``occ`` ([nspecies*spuck]), ``dprocstat`` / ``dinteg`` since sample_begin,
+        ``times`` (total_time, simulated_time), ``steps`` and ``status``."""
+        slots = _a32(slots)
+        out, os_, ps_ = self._sample_out(slots)
+        _check(load().kmc_pool_sample_end(self.h, _ptr(slots, _i32), len(slots), os_, ps_, *self._out_args(out)))
+        return out
+
+    def sample_run(self, slots, samples: int, steps_per_sample: int) -> dict:
+        """sample_begin, ``samples`` x (run ``steps_per_sample`` steps, sample), sample_end,
+        queued on the device in one call."""
+        slots = _a32(slots)
+        out, os_, ps_ = self._sample_out(slots)
+        _check(load().kmc_pool_sample_run(self.h, _ptr(slots, _i32), len(slots), int(samples), int(steps_per_sample),
+                                          os_, ps_, *self._out_args(out)))
+        return out

@@ -41,6 +41,7 @@ class _State:
         self.traj: Optional[E.Trajectory] = None
         self.system_size = np.zeros(3, dtype=np.int32)
         self.seed = 1
+        self.system_name = "kmc_model"
 
     def t(self) -> E.Trajectory:
         if self.traj is None:
@@ -83,10 +84,46 @@ def _base(S: _State) -> types.SimpleNamespace:
     ns.get_nrofsites = lambda proc: int(S.t().nr_of_sites()[int(proc) - 1])
     ns.get_avail_site = lambda proc, idx, sw: S.t().avail_site(int(proc), int(idx), int(sw))
     ns.get_volume = lambda: S.t().V
-    ns.get_walltime = lambda: 0.0
+    ns.get_walltime = lambda: S.t().walltime
     ns.get_species = lambda nr: S.t().get_species(int(nr))
     ns.replace_species = lambda nr, old, new: S.t().replace_species(int(nr), int(old), int(new))
+    ns.save_system = lambda: _save_system(S)
+    ns.reload_system = lambda input_system_name: _reload_system(S, input_system_name)
     return ns
+
+
+def _save_system(S: _State) -> None:
+    """base.save_system (base.mpy:489-575): ``<system_name>.reload`` in the working
+    directory, in the reference's layout."""
+    S.t().save_reload(S.system_name.strip() + ".reload")
+
+
+def _reload_system(S: _State, input_system_name) -> bool:
+    """base.reload_system (base.mpy:363-486): returns whether ``<name>.reload`` existed
+    and was loaded.  Like the reference it allocates the system; the system size comes
+    from the file's ``#gb300 system_size`` line, else from ``lattice.system_size`` when
+    that was set to a size of the file's volume."""
+    import os
+    name = str(input_system_name).strip()
+    S.system_name = name
+    path = name + ".reload"
+    if not os.path.exists(path):
+        return False
+    if S.traj is not None:
+        raise E.KMCError(1, "allocate_system: tried to allocate twice, deallocate first")
+    nproc, volume, dims = E.reload_info(path)
+    if nproc != len(S.model.processes):
+        raise E.KMCError(1, "%s holds %d processes, the model has %d" % (path, nproc, len(S.model.processes)))
+    if dims is None:
+        dims = [int(v) for v in S.system_size]
+        if min(dims) < 1 or int(np.prod(dims)) * S.model.spuck != volume:
+            raise E.KMCError(1, "%s has no system size line: set lattice.system_size to a size with volume %d "
+                                "first" % (path, volume))
+    S.system_size[:] = dims
+    layer = S.model.layer_ids()[S.model.default_layer]
+    S.traj = E.Trajectory(S.program, dims, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
+    S.traj.load_reload(path)
+    return True
 
 
 def _lattice(S: _State) -> types.SimpleNamespace:
@@ -116,6 +153,8 @@ def _lattice(S: _State) -> types.SimpleNamespace:
             S.traj = None
 
     ns.deallocate_system = deallocate_system
+    ns.save_system = lambda: _save_system(S)
+    ns.reload_system = lambda input_system_name: _reload_system(S, input_system_name)
     return ns
 
 
@@ -145,6 +184,7 @@ def _proclist(S: _State) -> types.SimpleNamespace:
             raise E.KMCError(1, "allocate_system: tried to allocate twice, deallocate first")
         S.system_size[:] = size
         S.seed = int(seed_in)
+        S.system_name = str(system_name)
         ns.seed = S.seed
         layer = ns_default_layer if layer is None else int(layer)
         S.traj = E.Trajectory(S.program, size, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
@@ -157,11 +197,10 @@ def _proclist(S: _State) -> types.SimpleNamespace:
     ns.run_proc_nr = lambda proc, site: S.t().run_proc_nr(int(proc), int(site))
 
     def get_occupation():
-        """(nr_of_species, spuck) site-resolved coverage per unit cell."""
-        occ = S.t().occupation()
-        out = np.zeros((ns.nr_of_species, m.spuck))
-        out[:occ.shape[0]] = occ
-        return out
+        """(species, spuck) site-resolved coverage per unit cell: one row per species
+        of the model, the null species of multi-lattice models not counted
+        (proclist_generic_subroutines.mpy:113-158 declares occupation(0:nspecies-1, 1:spuck))."""
+        return S.t().occupation()
 
     ns.get_occupation = get_occupation
     if S.backend == "lat_int":

@@ -167,6 +167,9 @@ class Oracle:
     def integ_rates(self):
         return np.array([lib().oracle_get_integ_rate(self.h, p) for p in range(1, self.P + 1)])
 
+    def rates(self):
+        return np.array([lib().oracle_get_rate(self.h, p) for p in range(1, self.P + 1)])
+
     def accum_rates(self):
         return np.array([lib().oracle_get_accum_rate(self.h, p) for p in range(1, self.P + 1)])
 

@@ -1,0 +1,46 @@
+"""The checker's .reload writer and reader (oracle/reload.py) on the CPU: Fortran edit
+descriptors of base.mpy:528-575 on known values, and a write / read round trip of an
+oracle trajectory's state."""
+import numpy as np
+
+from conftest import fixture_model
+from kmos_gb300 import program as PG
+from oracle import oracle as O, reload as RL
+
+
+def test_edit_descriptors():
+    assert RL.es(1.0, 22, 15) == " 1.000000000000000E+00"
+    assert RL.es(0.0, 22, 15) == " 0.000000000000000E+00"
+    assert RL.es(-2.5e-7, 22, 15) == "-2.500000000000000E-07"
+    assert RL.es(1e13, 14, 7) == " 1.0000000E+13"
+    assert RL.es(123456789.0, 14, 7) == " 1.2345679E+08"
+    assert RL.es(1.5e-120, 14, 7) == " 1.5000000-120"
+    assert RL.es(3.0e200, 14, 7) == " 3.0000000+200"
+    assert RL.es(0.0, 13, 7) == "0.0000000E+00"
+    assert RL.es(-1.0, 13, 7) == "*************"
+    assert RL.iw(-1, 9) == "       -1"
+    assert RL.iw(12345, 22) == " " * 17 + "12345"
+    assert RL.iw(10 ** 9, 9) == "*" * 9
+    assert RL._real("1.5000000-120") == 1.5e-120
+    assert RL._real("2.0D+03") == 2000.0
+
+
+def test_round_trip(tmp_path):
+    prog = PG.compile_model(fixture_model("CO_oxidation_Ruo2"), "local_smart")
+    o = O.Oracle(prog, (6, 5), seed=3, rng=O.RNG_PHILOX, traj=1)
+    o.set_rates(np.linspace(1.0, 50.0, prog.nproc))
+    o.update_accum_rate()
+    o.do_kmc_steps(3000)
+    path = str(tmp_path / "t.reload")
+    RL.write_oracle_reload(path, o, walltime=1.25)
+    r = RL.read_reload(path)
+    ex = o.export()
+    assert r["nr_of_proc"] == prog.nproc and r["volume"] == o.V and r["kmc_step"] == o.kmc_step
+    assert abs(r["kmc_time"] - o.kmc_time) <= 1e-15 * o.kmc_time and r["walltime"] == 1.25
+    np.testing.assert_array_equal(r["lattice"], ex["lattice"])
+    np.testing.assert_array_equal(r["procstat"], ex["procstat"])
+    np.testing.assert_array_equal(r["nr_of_sites"], ex["nsites"])
+    np.testing.assert_allclose(r["rates"], o.rates(), rtol=1e-7)
+    for p in range(prog.nproc):
+        np.testing.assert_array_equal(r["as1"][p + 1], ex["as1"][p][1:])
+        np.testing.assert_array_equal(r["as2"][p + 1], ex["as2"][p][1:])
