@@ -961,7 +961,17 @@ int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   L.threads = 32 * wpb;
   L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
   L.np = NP;
-  CK(cudaFuncSetAttribute(kmc_run_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  // The attribute is a per-function cap shared by every plan (and pool) on the device:
+  // raise it to the device's limit once rather than to this plan's size, which would
+  // lower it under a plan made before this one.
+  cudaFuncAttributes fa;
+  CK(cudaFuncGetAttributes(&fa, kmc_run_kernel<NP>));
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+  const int cap = optin - (int)fa.sharedSizeBytes;
+  if ((int64_t)L.smem > cap) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
+  if (fa.maxDynamicSharedSizeBytes < cap)
+    CK(cudaFuncSetAttribute(kmc_run_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
   int bps = p->blocks_per_sm;
   if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP>, L.threads, L.smem));
   if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
