@@ -349,7 +349,7 @@ struct FastSmem {
   int16_t heads[FAST_EDITS];   // processes touched this step, in first-edit order
   int32_t esite[FAST_EDITS];   // target site
   int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
-  int32_t tail[32][TAIL_MAX];  // lane-private avail_sites(p, n0 - j, 1), j < TAIL_MAX
+  int32_t tail[32][TAIL_MAX];  // per head h < 32: avail_sites(p, n0 - j, 1), j < TAIL_MAX
   uint32_t lkey[LOG_MAX][32];  // lane-private write logs (lane-minor: no bank conflicts)
   int32_t lval[LOG_MAX][32];
 };

@@ -76,40 +76,32 @@ struct WarpSmem {
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
   uint32_t pmask[NP * 32][FAST_ROUNDS];  // edits of each process this step, one bit per edit
+  int8_t hidx[NP * 32];                  // head index of each process touched this step
+  uint8_t ndel[NP * 32];                 // its del edits this step
   long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
   long long tprev;
   FastSmem f;
 };
 
 // Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
-// returns a status.  Clears pmask[p].
+// returns a status.  Clears pmask[p].  The loads it needs were issued warp-parallel
+// before: em[k] = avail_sites(p, site_k, 2) for every del edit k, and for head h < 32
+// tail[h][j] = avail_sites(p, n0 - j, 1) for j < min(nd, TAIL_MAX), nd = its del edits.
 template <int NP>
 __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], const View &v, int p,
-                              int rounds, int lane) {
+                              int rounds, int h) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
   const int n0 = ns[p];
+  const int lane = threadIdx.x & 31;
   uint32_t bits[FAST_ROUNDS];
 #pragma unroll
   for (int r = 0; r < FAST_ROUNDS; r++) {
     bits[r] = r < rounds ? pmask[p][r] : 0u;
     pmask[p][r] = 0u;
   }
-  // issue every load the dels can need
-  int nd = 0;
-#pragma unroll
-  for (int r = 0; r < FAST_ROUNDS; r++) {
-    uint32_t b = bits[r];
-    while (b) {
-      const int k = 32 * r + __ffs(b) - 1;
-      b &= b - 1;
-      if (f.ekind[k] == E_ADD) continue;
-      f.em[k] = a2[f.esite[k]];
-      if (nd < TAIL_MAX) f.tail[lane][nd] = (n0 - nd >= 1) ? a1[n0 - nd] : 0;
-      nd++;
-    }
-  }
+  const bool has_tail = h < 32;
   // apply the edits; reads look in the write log, then at the prefetched values
   int nlog = 0;
   bool logok = true;
@@ -154,7 +146,8 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
       if (m < n) {
         int last;
         if (!logok) last = a1[n];
-        else if (nlog == 0 || !logged(0, n, last)) last = (n0 - n < TAIL_MAX && n <= n0) ? f.tail[lane][n0 - n] : a1[n];
+        else if (nlog == 0 || !logged(0, n, last))
+          last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[h][n0 - n] : a1[n];
         put(0, m, last);
         put(0, n, 0);
         put(1, last, m);
@@ -181,19 +174,39 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   const int32_t *wr = chk + 2 * nchk;
   const int32_t *eoff = wr + 2 * nwr;
   const unsigned lt = (1u << lane) - 1u;
-  // 1. gather every slot; check the old species of first replaces
-  for (int i = lane; i < nlat; i += 32) f.latsite[i] = v.g.site_near(bx, by, bz, coords[i]);
+  // 1. gather every slot (all lattice loads in flight together); check the old species
+  //    of first replaces
+  int32_t lvv[FAST_SLOTS / 32];
+#pragma unroll
+  for (int rr = 0; rr < FAST_SLOTS / 32; rr++) {
+    const int i = lane + 32 * rr;
+    lvv[rr] = 0;
+    if (i < nlat) {
+      const int site = v.g.site_near(bx, by, bz, coords[i]);
+      f.latsite[i] = site;
+      lvv[rr] = v.lat[site - 1];
+    }
+  }
   KMC_PHASE(sm, 11);
-  for (int i = lane; i < nlat; i += 32) f.latv[i] = v.lat[f.latsite[i] - 1];
+#pragma unroll
+  for (int rr = 0; rr < FAST_SLOTS / 32; rr++)
+    if (lane + 32 * rr < nlat) f.latv[lane + 32 * rr] = lvv[rr];
   __syncwarp();
   bool bad = false;
   for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);
   if (__any_sync(0xffffffffu, bad)) return ST_SPECIES;
   KMC_PHASE(sm, 4);
-  // 2. evaluate every edit in parallel; compact the ones that happen, in order
+  // 2. evaluate every edit in parallel; compact the ones that happen, in order.  A del
+  //    edit's avail_sites(p, site, 2) load is issued here and lands in em[] afterwards.
   int ne = 0;
-  for (int r = 0; r < nedit; r += 32) {
-    const int k = r + lane;
+  int32_t emv[FAST_ROUNDS];
+  int empos[FAST_ROUNDS];
+#pragma unroll
+  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
+    emv[rr] = 0;
+    empos[rr] = -1;
+    if (32 * rr >= nedit) continue;
+    const int k = 32 * rr + lane;
     bool on = false;
     int kind = E_GDEL, p = 0, site = 0;
     if (k < nedit) {
@@ -211,7 +224,10 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         on = p != 0;
         kind = op == 4 ? E_DEL : E_ADD;
       }
-      if (on) site = v.g.site_near(bx, by, bz, e[1]);
+      if (on) {
+        site = v.g.site_near(bx, by, bz, e[1]);
+        if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
+      }
     }
     const unsigned b = __ballot_sync(0xffffffffu, on);
     if (on) {
@@ -219,9 +235,13 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       f.ekind[pos] = (int8_t)kind;
       f.ep[pos] = (int16_t)(p - 1);
       f.esite[pos] = site;
+      if (kind != E_ADD) empos[rr] = pos;
     }
     ne += __popc(b);
   }
+#pragma unroll
+  for (int rr = 0; rr < FAST_ROUNDS; rr++)
+    if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
   __syncwarp();
   KMC_PHASE(sm, 5);
   // 3. per process, the bit mask of its edits in each round of 32; a process whose
@@ -241,14 +261,49 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
     __syncwarp();
     if (leader) sm.pmask[p][r] = m;
     const unsigned hb = __ballot_sync(0xffffffffu, head);
-    if (head) f.heads[nh + __popc(hb & lt)] = (int16_t)p;
+    if (head) {
+      const int hh = nh + __popc(hb & lt);
+      f.heads[hh] = (int16_t)p;
+      sm.hidx[p] = (int8_t)min(hh, 127);
+      sm.ndel[p] = 0;
+    }
     nh += __popc(hb);
     __syncwarp();
   }
+  // 3b. the avail_sites(p, n0 - j, 1) entries the dels of each process can move, one
+  //     load per del edit (its rank j among the process's dels), all in flight together
+  int32_t tv[FAST_ROUNDS];
+  int tslot[FAST_ROUNDS];
+#pragma unroll
+  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
+    tv[rr] = 0;
+    tslot[rr] = -1;
+    if (rr >= rounds) continue;
+    const int k = 32 * rr + lane;
+    const bool del = k < ne && f.ekind[k] != E_ADD;
+    const int p = del ? f.ep[k] : -1 - lane;
+    const unsigned m = __match_any_sync(0xffffffffu, p);
+    if (del) {
+      const int rank = sm.ndel[p] + __popc(m & lt);
+      const int hh = sm.hidx[p];
+      const int n0 = sm.ns[p];
+      if (rank < TAIL_MAX && hh < 32) {
+        tslot[rr] = hh * TAIL_MAX + rank;
+        if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)p * v.stride + n0 - rank];
+      }
+    }
+    __syncwarp();
+    if (del && (__ffs(m) - 1) == lane) sm.ndel[p] += (uint8_t)__popc(m);
+    __syncwarp();
+  }
+#pragma unroll
+  for (int rr = 0; rr < FAST_ROUNDS; rr++)
+    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
+  __syncwarp();
   KMC_PHASE(sm, 6);
   int err = ST_OK;
   for (int h = lane; h < nh; h += 32) {
-    const int e = replay_process<NP>(f, sm.ns, sm.pmask, v, f.heads[h], rounds, lane);
+    const int e = replay_process<NP>(f, sm.ns, sm.pmask, v, f.heads[h], rounds, h);
     if (e) err = e;
   }
   KMC_PHASE(sm, 7);
