@@ -335,7 +335,8 @@ namespace kmc {
 constexpr int FAST_SLOTS = 128;
 constexpr int FAST_EDITS = 96;
 constexpr int LOG_MAX = 12;   // lane-private write log entries
-constexpr int TAIL_MAX = 6;   // lane-private prefetched tail entries
+constexpr int TAIL_MAX = 6;   // prefetched list-tail entries per process
+constexpr int TAIL_PROCS = 64; // processes 0..63 get prefetched tails
 constexpr int FAST_ROUNDS = FAST_EDITS / 32;
 constexpr int FAST_MAXV = (1 << 23) - 1;
 
@@ -349,7 +350,7 @@ struct FastSmem {
   int16_t heads[FAST_EDITS];   // processes touched this step, in first-edit order
   int32_t esite[FAST_EDITS];   // target site
   int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
-  int32_t tail[32][TAIL_MAX];  // per head h < 32: avail_sites(p, n0 - j, 1), j < TAIL_MAX
+  int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS
   uint32_t lkey[LOG_MAX][32];  // lane-private write logs (lane-minor: no bank conflicts)
   int32_t lval[LOG_MAX][32];
 };

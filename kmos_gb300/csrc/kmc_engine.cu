@@ -76,20 +76,20 @@ struct WarpSmem {
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
   uint32_t pmask[NP * 32][FAST_ROUNDS];  // edits of each process this step, one bit per edit
-  int8_t hidx[NP * 32];                  // head index of each process touched this step
-  uint8_t ndel[NP * 32];                 // its del edits this step
+  uint8_t ndel[NP * 32];                 // del edits of each process so far this step (0 between steps)
   long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
   long long tprev;
   FastSmem f;
 };
 
 // Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
-// returns a status.  Clears pmask[p].  The loads it needs were issued warp-parallel
-// before: em[k] = avail_sites(p, site_k, 2) for every del edit k, and for head h < 32
-// tail[h][j] = avail_sites(p, n0 - j, 1) for j < min(nd, TAIL_MAX), nd = its del edits.
+// returns a status.  Clears pmask[p] and ndel[p].  The loads it needs were issued
+// warp-parallel while the edits were evaluated: em[k] = avail_sites(p, site_k, 2) for
+// every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
+// j < min(nd, TAIL_MAX), nd = its del edits.
 template <int NP>
-__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], const View &v, int p,
-                              int rounds, int h) {
+__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], uint8_t *ndel,
+                              const View &v, int p, int rounds) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
@@ -101,7 +101,8 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
     bits[r] = r < rounds ? pmask[p][r] : 0u;
     pmask[p][r] = 0u;
   }
-  const bool has_tail = h < 32;
+  ndel[p] = 0;
+  const bool has_tail = p < TAIL_PROCS;
   // apply the edits; reads look in the write log, then at the prefetched values
   int nlog = 0;
   bool logok = true;
@@ -147,7 +148,7 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
         int last;
         if (!logok) last = a1[n];
         else if (nlog == 0 || !logged(0, n, last))
-          last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[h][n0 - n] : a1[n];
+          last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
         put(0, m, last);
         put(0, n, 0);
         put(1, last, m);
@@ -196,15 +197,19 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);
   if (__any_sync(0xffffffffu, bad)) return ST_SPECIES;
   KMC_PHASE(sm, 4);
-  // 2. evaluate every edit in parallel; compact the ones that happen, in order.  A del
-  //    edit's avail_sites(p, site, 2) load is issued here and lands in em[] afterwards.
+  // 2. evaluate every edit in parallel; compact the ones that happen, in order.  The
+  //    loads the replay needs are issued here and land in shared memory afterwards: a
+  //    del edit's avail_sites(p, site, 2), and the list entry avail_sites(p, n0 - j, 1)
+  //    its swap-remove can move, j = its rank among the process's dels this step.
   int ne = 0;
-  int32_t emv[FAST_ROUNDS];
-  int empos[FAST_ROUNDS];
+  int32_t emv[FAST_ROUNDS], tv[FAST_ROUNDS];
+  int empos[FAST_ROUNDS], tslot[FAST_ROUNDS];
 #pragma unroll
   for (int rr = 0; rr < FAST_ROUNDS; rr++) {
     emv[rr] = 0;
     empos[rr] = -1;
+    tv[rr] = 0;
+    tslot[rr] = -1;
     if (32 * rr >= nedit) continue;
     const int k = 32 * rr + lane;
     bool on = false;
@@ -229,6 +234,17 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
       }
     }
+    const bool del = on && kind != E_ADD;
+    const int q = del ? p - 1 : -1 - lane;
+    const unsigned dm = __match_any_sync(0xffffffffu, q);
+    if (del) {
+      const int rank = sm.ndel[q] + __popc(dm & lt);
+      if (rank < TAIL_MAX && q < TAIL_PROCS) {
+        const int n0 = sm.ns[q];
+        tslot[rr] = q * TAIL_MAX + rank;
+        if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)q * v.stride + n0 - rank];
+      }
+    }
     const unsigned b = __ballot_sync(0xffffffffu, on);
     if (on) {
       const int pos = ne + __popc(b & lt);
@@ -238,10 +254,14 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       if (kind != E_ADD) empos[rr] = pos;
     }
     ne += __popc(b);
+    if (del && (__ffs(dm) - 1) == lane) sm.ndel[q] += (uint8_t)__popc(dm);
+    __syncwarp();
   }
 #pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++)
+  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
     if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
+    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
+  }
   __syncwarp();
   KMC_PHASE(sm, 5);
   // 3. per process, the bit mask of its edits in each round of 32; a process whose
@@ -261,49 +281,14 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
     __syncwarp();
     if (leader) sm.pmask[p][r] = m;
     const unsigned hb = __ballot_sync(0xffffffffu, head);
-    if (head) {
-      const int hh = nh + __popc(hb & lt);
-      f.heads[hh] = (int16_t)p;
-      sm.hidx[p] = (int8_t)min(hh, 127);
-      sm.ndel[p] = 0;
-    }
+    if (head) f.heads[nh + __popc(hb & lt)] = (int16_t)p;
     nh += __popc(hb);
     __syncwarp();
   }
-  // 3b. the avail_sites(p, n0 - j, 1) entries the dels of each process can move, one
-  //     load per del edit (its rank j among the process's dels), all in flight together
-  int32_t tv[FAST_ROUNDS];
-  int tslot[FAST_ROUNDS];
-#pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
-    tv[rr] = 0;
-    tslot[rr] = -1;
-    if (rr >= rounds) continue;
-    const int k = 32 * rr + lane;
-    const bool del = k < ne && f.ekind[k] != E_ADD;
-    const int p = del ? f.ep[k] : -1 - lane;
-    const unsigned m = __match_any_sync(0xffffffffu, p);
-    if (del) {
-      const int rank = sm.ndel[p] + __popc(m & lt);
-      const int hh = sm.hidx[p];
-      const int n0 = sm.ns[p];
-      if (rank < TAIL_MAX && hh < 32) {
-        tslot[rr] = hh * TAIL_MAX + rank;
-        if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)p * v.stride + n0 - rank];
-      }
-    }
-    __syncwarp();
-    if (del && (__ffs(m) - 1) == lane) sm.ndel[p] += (uint8_t)__popc(m);
-    __syncwarp();
-  }
-#pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++)
-    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
-  __syncwarp();
   KMC_PHASE(sm, 6);
   int err = ST_OK;
   for (int h = lane; h < nh; h += 32) {
-    const int e = replay_process<NP>(f, sm.ns, sm.pmask, v, f.heads[h], rounds, h);
+    const int e = replay_process<NP>(f, sm.ns, sm.pmask, sm.ndel, v, f.heads[h], rounds);
     if (e) err = e;
   }
   KMC_PHASE(sm, 7);
@@ -351,6 +336,7 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
   const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
   WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw + hot_bytes)[wib];
   for (int i = lane; i < NP * 32 * FAST_ROUNDS; i += 32) (&sm.pmask[0][0])[i] = 0u;
+  for (int i = lane; i < NP * 32; i += 32) sm.ndel[i] = 0;
   for (int i = lane; i < KMC_NPHASE; i += 32) sm.ph[i] = 0;
   __syncthreads();
 
