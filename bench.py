@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--ntraj", type=int, default=0, help="override the trajectory count")
     ap.add_argument("--graph", type=int, default=1, help="replay the launch from a CUDA graph")
     ap.add_argument("--cpu-baseline", type=int, default=1)
-    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=-1,
+                    help="warps per block (0: balanced, one block per SM); default: autotune or the pool's")
     ap.add_argument("--bps", type=int, default=0)
     ap.add_argument("--sides", default="", help="config 3: comma-separated lattice sides to draw from")
     ap.add_argument("--fast", type=int, default=1, help="gather / replay step path (0: serial interpreter)")
@@ -254,7 +255,7 @@ def run_ours(args, dist: Dist):
     need = sum(per)
     pool.close()
     pool = E.Pool(arena_bytes=need + (64 << 20), max_slots=n, device=dev)
-    if args.warps or args.bps:
+    if args.warps >= 0:
         pool.set_launch(args.warps, args.bps)
     if not args.fast:
         pool.set_fast_path(False)
@@ -277,7 +278,7 @@ def run_ours(args, dist: Dist):
             pool.run(slots, chunk, sync=False)
 
     tuned = None
-    if args.autotune and not (args.warps or args.bps or not args.fast):
+    if args.autotune and not (args.warps >= 0 or args.bps or not args.fast):
         # part of the warm-up: probes advance the real trajectories (results do not
         # depend on the launch shape)
         from kmos_gb300 import autotune

@@ -195,7 +195,9 @@ KMC_API int kmc_pool_get_results(kmc_pool *pool, const int32_t *slots, int32_t n
 #define KMC_STATIC_OCC_MAX_STRIDE 64
 KMC_API int kmc_pool_occupation_counts_static(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride,
                                               int64_t *out);
-/* Launch configuration used by kmc_pool_run: warps per block (1..32, 0 = automatic). */
+/* Launch configuration used by kmc_pool_run: warps per block (1..16) with blocks_per_sm
+ * blocks per SM (0 = as many as fit), or warps_per_block 0 = balanced: one block per SM,
+ * the run's trajectories split evenly over the SMs in the fewest rounds per warp. */
 KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
 /* 1 (default): steps whose process has a fast stream run through the gather /
  * replay / scatter path; 0: every step runs the serial interpreter (same results). */

@@ -3,7 +3,8 @@
 The step results do not depend on the launch shape (each trajectory's steps are the
 same whatever warp runs them), so tuning runs short launches on the *real* trajectories:
 each probe advances them by ``probe_steps`` steps, which the caller counts as warm-up or
-as part of the requested steps.  It picks warps per block (1, 2, 4 or 8) and the step
+as part of the requested steps.  It picks the launch shape (the balanced one-block-per-SM
+shape, or 2, 4 or 8 warps per block with as many blocks as fit) and the step
 path (gather / replay or serial interpreter) with the highest measured steps/s, sets
 them on the pool, and returns steps per launch for about ``target_ms`` per launch.
 """
@@ -15,7 +16,7 @@ from . import engine as E
 
 
 def tune(pool: E.Pool, slots: Sequence[int], probe_steps: int = 500, target_ms: float = 100.0,
-         warps=(1, 2, 4, 8), paths=(True, False)) -> Dict:
+         warps=(0, 2, 4, 8), paths=(True, False)) -> Dict:
     results: List[Dict] = []
     for fast in paths:
         for w in warps:

@@ -318,7 +318,7 @@ struct RunArgs {
 };
 
 template <int NP>
-__global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
+__global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -340,10 +340,16 @@ __global__ void __launch_bounds__(256) kmc_run_kernel(RunArgs a) {
   for (int i = lane; i < KMC_NPHASE; i += 32) sm.ph[i] = 0;
   __syncthreads();
 
-  for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(a.counter, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
+  // Work: every warp first takes item (warp in block) * gridDim.x + block -- the list
+  // is sorted by cost, so each block gets an even share of long and short trajectories
+  // -- then pulls further items from the counter.
+  const int nstatic = gridDim.x * (blockDim.x >> 5);
+  for (int round = 0;; round++) {
+    int item = wib * gridDim.x + blockIdx.x;
+    if (round > 0) {
+      if (lane == 0) item = nstatic + atomicAdd(a.counter, 1);
+      item = __shfl_sync(0xffffffffu, item, 0);
+    }
     if (item >= a.n) break;
     const int slot = a.list[item];
     const int64_t nsteps = a.steps[item];
@@ -998,9 +1004,6 @@ struct LaunchPlan {
 
 template <int NP>
 int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
-  const int wpb = p->warps_per_block;
-  L.threads = 32 * wpb;
-  L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
   L.np = NP;
   // The attribute is a per-function cap shared by every plan (and pool) on the device:
   // raise it to the device's limit once rather than to this plan's size, which would
@@ -1010,13 +1013,33 @@ int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   int optin = 0;
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
   const int cap = optin - (int)fa.sharedSizeBytes;
-  if ((int64_t)L.smem > cap) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
   if (fa.maxDynamicSharedSizeBytes < cap)
     CK(cudaFuncSetAttribute(kmc_run_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-  int bps = p->blocks_per_sm;
-  if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP>, L.threads, L.smem));
-  if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
-  L.blocks = std::max(1, std::min((L.count + wpb - 1) / wpb, p->num_sms * bps));
+  if (p->warps_per_block > 0) {
+    const int wpb = p->warps_per_block;
+    L.threads = 32 * wpb;
+    L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
+    if ((int64_t)L.smem > cap) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
+    int bps = p->blocks_per_sm;
+    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP>, L.threads, L.smem));
+    if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
+    L.blocks = std::max(1, std::min((L.count + wpb - 1) / wpb, p->num_sms * bps));
+    return KMC_OK;
+  }
+  // balanced: one block per SM, as many warps per block as fit (registers: 16 at 128
+  // per thread; shared memory), and the fewest rounds of items per warp with the warps
+  // split evenly over the SMs
+  const int regs = std::max(1, fa.numRegs);
+  int maxw = std::min(16, 65536 / (regs * 32));
+  maxw = std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / (int64_t)sizeof(WarpSmem<NP>));
+  if (maxw < 1) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
+  const int blocks = std::max(1, std::min(p->num_sms, L.count));
+  const int rounds = (L.count + blocks * maxw - 1) / (blocks * maxw);
+  const int warps = (L.count + rounds - 1) / rounds;
+  const int wpb = std::min(maxw, (warps + blocks - 1) / blocks);
+  L.threads = 32 * wpb;
+  L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
+  L.blocks = blocks;
   return KMC_OK;
 }
 
@@ -1025,8 +1048,14 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
              std::vector<int64_t> &st, std::vector<LaunchPlan> &plans) {
   std::vector<int32_t> order(n);
   for (int i = 0; i < n; i++) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return p->slots[slots[x]].dev.model < p->slots[slots[y]].dev.model; });
+  // by model, then longest first (steps, then lattice size), so that the kernel's strided
+  // first assignment spreads the long trajectories over the blocks
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const SlotDev &a = p->slots[slots[x]].dev, &b = p->slots[slots[y]].dev;
+    if (a.model != b.model) return a.model < b.model;
+    if (steps[x] != steps[y]) return steps[x] > steps[y];
+    return a.V > b.V;
+  });
   ls.resize(n);
   st.resize(n);
   for (int i = 0; i < n; i++) { ls[i] = slots[order[i]]; st[i] = steps[order[i]]; }
@@ -1456,8 +1485,8 @@ int kmc_pool_launch_count(kmc_pool *p, int64_t *count) {
 }
 
 int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per_sm) {
-  if (!p || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
-  p->warps_per_block = warps_per_block ? warps_per_block : 4;
+  if (!p || warps_per_block < 0 || warps_per_block > 16 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
+  p->warps_per_block = warps_per_block;
   p->blocks_per_sm = blocks_per_sm;
   for (auto &kv : p->graphs) {
     cudaGraphExecDestroy(kv.second.exec);
