@@ -334,7 +334,7 @@ namespace kmc {
 
 constexpr int FAST_SLOTS = 128;
 constexpr int FAST_EDITS = 96;
-constexpr int LOG_MAX = 12;   // lane-private write log entries
+constexpr int LOG_MAX = 16;   // lane-private write log entries (a multiple of 4)
 constexpr int TAIL_MAX = 6;   // prefetched list-tail entries per process
 constexpr int TAIL_PROCS = 64; // processes 0..63 get prefetched tails
 constexpr int FAST_ROUNDS = FAST_EDITS / 32;
@@ -351,7 +351,7 @@ struct FastSmem {
   int32_t esite[FAST_EDITS];   // target site
   int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
   int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS
-  uint32_t lkey[LOG_MAX][32];  // lane-private write logs (lane-minor: no bank conflicts)
+  uint4 lkey4[LOG_MAX / 4][32];  // lane-private write logs, four keys per 16 bytes (lane-minor)
   int32_t lval[LOG_MAX][32];
 };
 

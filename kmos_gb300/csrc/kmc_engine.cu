@@ -103,22 +103,35 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
   }
   ndel[p] = 0;
   const bool has_tail = p < TAIL_PROCS;
-  // apply the edits; reads look in the write log, then at the prefetched values
+  // apply the edits; reads look in the write log, then at the prefetched values.  The
+  // log is append-only (a later entry for a key shadows earlier ones) and is searched
+  // newest first, four keys per shared-memory load; once full, reads go to HBM, which
+  // every write reaches too.
   int nlog = 0;
   bool logok = true;
   auto put = [&](int table, int index, int32_t val) {
     if (table) a2[index] = val; else a1[index] = val;
     if (!logok) return;
-    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
-    for (int i = nlog - 1; i >= 0; i--)
-      if (f.lkey[i][lane] == key) { f.lval[i][lane] = val; return; }
-    if (nlog < LOG_MAX) { f.lkey[nlog][lane] = key; f.lval[nlog][lane] = val; nlog++; }
-    else logok = false;
+    if (nlog < LOG_MAX) {
+      reinterpret_cast<uint32_t *>(&f.lkey4[nlog >> 2][lane])[nlog & 3] = ((uint32_t)table << 31) | (uint32_t)index;
+      f.lval[nlog][lane] = val;
+      nlog++;
+    } else {
+      logok = false;
+    }
   };
   auto logged = [&](int table, int index, int32_t &val) -> bool {
     const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
-    for (int i = nlog - 1; i >= 0; i--)
-      if (f.lkey[i][lane] == key) { val = f.lval[i][lane]; return true; }
+    for (int g = (nlog - 1) >> 2; g >= 0; g--) {
+      const uint4 k4 = f.lkey4[g][lane];
+      const int b = 4 * g;
+      int i = -1;
+      if (b + 3 < nlog && k4.w == key) i = b + 3;
+      else if (b + 2 < nlog && k4.z == key) i = b + 2;
+      else if (b + 1 < nlog && k4.y == key) i = b + 1;
+      else if (k4.x == key) i = b;
+      if (i >= 0) { val = f.lval[i][lane]; return true; }
+    }
     return false;
   };
   int n = n0;
@@ -257,11 +270,6 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
     if (del && (__ffs(dm) - 1) == lane) sm.ndel[q] += (uint8_t)__popc(dm);
     __syncwarp();
   }
-#pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
-    if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
-    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
-  }
   __syncwarp();
   KMC_PHASE(sm, 5);
   // 3. per process, the bit mask of its edits in each round of 32; a process whose
@@ -285,6 +293,13 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
     nh += __popc(hb);
     __syncwarp();
   }
+  // the loads issued during evaluation land now, after the head search overlapped them
+#pragma unroll
+  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
+    if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
+    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
+  }
+  __syncwarp();
   KMC_PHASE(sm, 6);
   int err = ST_OK;
   for (int h = lane; h < nh; h += 32) {
