@@ -347,7 +347,6 @@ struct FastSmem {
   int32_t latsite[FAST_SLOTS];
   int8_t ekind[FAST_EDITS];    // E_GDEL / E_DEL / E_ADD
   int16_t ep[FAST_EDITS];      // process, 0-based
-  int16_t heads[FAST_EDITS];   // processes touched this step, in first-edit order
   int32_t esite[FAST_EDITS];   // target site
   int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
   int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS

@@ -76,7 +76,7 @@ struct WarpSmem {
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
   uint32_t pmask[NP * 32][FAST_ROUNDS];  // edits of each process this step, one bit per edit
-  uint8_t ndel[NP * 32];                 // del edits of each process so far this step (0 between steps)
+  int32_t ndel[NP * 32];                 // del edits of each process so far this step (0 between steps)
   long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
   long long tprev;
   FastSmem f;
@@ -88,7 +88,7 @@ struct WarpSmem {
 // every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
 // j < min(nd, TAIL_MAX), nd = its del edits.
 template <int NP>
-__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], uint8_t *ndel,
+__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], int32_t *ndel,
                               const View &v, int p, int rounds) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
@@ -247,11 +247,11 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
       }
     }
-    const bool del = on && kind != E_ADD;
-    const int q = del ? p - 1 : -1 - lane;
-    const unsigned dm = __match_any_sync(0xffffffffu, q);
-    if (del) {
-      const int rank = sm.ndel[q] + __popc(dm & lt);
+    // a del's rank among its process's dels picks which list entry it loads; the ranks
+    // only have to be distinct, so a shared-memory counter gives them in any order
+    if (on && kind != E_ADD) {
+      const int q = p - 1;
+      const int rank = atomicAdd(&sm.ndel[q], 1);
       if (rank < TAIL_MAX && q < TAIL_PROCS) {
         const int n0 = sm.ns[q];
         tslot[rr] = q * TAIL_MAX + rank;
@@ -264,36 +264,14 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       f.ekind[pos] = (int8_t)kind;
       f.ep[pos] = (int16_t)(p - 1);
       f.esite[pos] = site;
+      atomicOr(&sm.pmask[p - 1][pos >> 5], 1u << (pos & 31));  // the process's edit mask
       if (kind != E_ADD) empos[rr] = pos;
     }
     ne += __popc(b);
-    if (del && (__ffs(dm) - 1) == lane) sm.ndel[q] += (uint8_t)__popc(dm);
-    __syncwarp();
   }
-  __syncwarp();
-  KMC_PHASE(sm, 5);
-  // 3. per process, the bit mask of its edits in each round of 32; a process whose
-  //    first edit this is becomes a head
-  int nh = 0;
   const int rounds = (ne + 31) >> 5;
-  for (int r = 0; r < rounds; r++) {
-    const int k = 32 * r + lane;
-    const int p = k < ne ? f.ep[k] : -1 - lane;
-    const unsigned m = __match_any_sync(0xffffffffu, p);
-    const bool leader = k < ne && (__ffs(m) - 1) == lane;
-    bool head = false;
-    if (leader) {
-      head = true;
-      for (int q = 0; q < r; q++) head = head && sm.pmask[p][q] == 0u;
-    }
-    __syncwarp();
-    if (leader) sm.pmask[p][r] = m;
-    const unsigned hb = __ballot_sync(0xffffffffu, head);
-    if (head) f.heads[nh + __popc(hb & lt)] = (int16_t)p;
-    nh += __popc(hb);
-    __syncwarp();
-  }
-  // the loads issued during evaluation land now, after the head search overlapped them
+  KMC_PHASE(sm, 5);
+  // the loads issued during evaluation land now
 #pragma unroll
   for (int rr = 0; rr < FAST_ROUNDS; rr++) {
     if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
@@ -301,10 +279,16 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   }
   __syncwarp();
   KMC_PHASE(sm, 6);
+  // 3. every process with edits replays them on its own lane (process j on lane j % 32)
   int err = ST_OK;
-  for (int h = lane; h < nh; h += 32) {
-    const int e = replay_process<NP>(f, sm.ns, sm.pmask, sm.ndel, v, f.heads[h], rounds);
-    if (e) err = e;
+  for (int j = lane; j < v.P; j += 32) {
+    uint32_t any = 0;
+#pragma unroll
+    for (int r = 0; r < FAST_ROUNDS; r++) any |= r < rounds ? sm.pmask[j][r] : 0u;
+    if (any) {
+      const int e = replay_process<NP>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds);
+      if (e) err = e;
+    }
   }
   KMC_PHASE(sm, 7);
   // 4. the final species of every replaced slot
