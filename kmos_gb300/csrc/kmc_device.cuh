@@ -363,6 +363,11 @@ struct Hot {
 
 __device__ inline int ref_value(int32_t ref, const int32_t *latv) { return ref >= 0 ? latv[ref] : -ref - 2; }
 
+// nli table code of a species: the species, or ns for the null species (-1); a value
+// above ns (a lattice holding no valid species) maps to ns too, so a table index built
+// from codes stays inside its table.
+__device__ inline int species_code(int s, int ns) { return (int)min((unsigned)s, (unsigned)ns); }
+
 // nli of one edit: table lookup when the group has one, else a member scan.  The edit
 // carries the group's table and record offsets (hot-relative) and its K references.
 __device__ inline int nli_refs(const Hot &H, int K, int toff, int roff, const int32_t *refs, const int32_t *latv) {
@@ -371,8 +376,7 @@ __device__ inline int nli_refs(const Hot &H, int K, int toff, int roff, const in
     int idx = 0, mul = 1;
 #pragma unroll 4
     for (int k = 0; k < K; k++) {
-      const int s = ref_value(refs[k], latv);
-      idx += (s < 0 ? H.nspecies : s) * mul;
+      idx += species_code(ref_value(refs[k], latv), H.nspecies) * mul;
       mul *= base;
     }
     return H.h[toff + idx];

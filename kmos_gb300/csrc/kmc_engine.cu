@@ -231,7 +231,13 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       const int32_t *e = fs + eoff[k];
       const uint32_t h = (uint32_t)e[0];
       const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-      if (op == 2) {
+      if (op >= 6) {  // nli through its table: index_base + sum(code(slot) * mul)
+        int idx = e[2];
+        for (int c = 0; c < cnt; c++) idx += species_code(f.latv[e[3 + c]], H.nspecies) * e[3 + cnt + c];
+        p = H.h[idx];
+        on = p != 0;
+        kind = op == 6 ? E_DEL : E_ADD;
+      } else if (op == 2) {
         on = true; p = arg;
       } else if (op == 3) {
         on = true;
@@ -243,7 +249,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         kind = op == 4 ? E_DEL : E_ADD;
       }
       if (on) {
-        site = v.g.site_near(bx, by, bz, e[1]);
+        site = f.latsite[e[1]];
         if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
       }
     }
@@ -956,15 +962,29 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
         if (eo[k] < head || e + 2 > hl) return fail(KMC_ERR_PROGRAM, "bad edit offset");
         const uint32_t h = (uint32_t)hot[e];
         const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-        if (!coord_ok(hot[e + 1])) return fail(KMC_ERR_PROGRAM, "bad edit target");
-        if (op == 2) {
+        if (hot[e + 1] < 0 || hot[e + 1] >= nlat) return fail(KMC_ERR_PROGRAM, "bad edit target");
+        if (op == 6 || op == 7) {
+          // every index the table form can produce lies inside the group's table
+          if (arg >= m->ngroups || e + 3 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad nli table edit");
+          const int toff = hot[m->hot_tab + arg];
+          const int K = hot[hot[m->hot_grp + arg] + 1];
+          int64_t size = 1;
+          for (int k = 0; k < K; k++) size *= (m->nspecies + 1);
+          int64_t lo = hot[e + 2], hi = hot[e + 2];
+          for (int c = 0; c < cnt; c++) {
+            if (hot[e + 3 + c] < 0 || hot[e + 3 + c] >= nlat || hot[e + 3 + cnt + c] < 0)
+              return fail(KMC_ERR_PROGRAM, "bad nli table edit");
+            hi += (int64_t)m->nspecies * hot[e + 3 + cnt + c];
+          }
+          if (toff <= 0 || lo < toff || hi >= toff + size) return fail(KMC_ERR_PROGRAM, "nli table edit outside its table");
+        } else if (op == 2) {
           if (arg < 1 || arg > m->P) return fail(KMC_ERR_PROGRAM, "bad edit process");
         } else if (op == 3) {
           if (arg < 1 || arg > m->P || e + 2 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad add edit");
           for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad add ref");
         } else if (op == 4 || op == 5) {
           if (arg >= m->ngroups || e + 4 + cnt > hl || cnt != hot[hot[m->hot_grp + arg] + 1] ||
-              hot[e + 2] != hot[m->hot_tab + arg] || hot[e + 3] != hot[m->hot_grp + arg])
+              hot[e + 2] != 0 || hot[e + 3] != hot[m->hot_grp + arg])
             return fail(KMC_ERR_PROGRAM, "bad nli edit");
           for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 4 + c])) return fail(KMC_ERR_PROGRAM, "bad nli ref");
         } else {

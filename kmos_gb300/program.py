@@ -67,12 +67,17 @@ had before the step.  All edits of a step can therefore be evaluated in parallel
 
     [nlat, nchk, nwr, nedit, coord * nlat, (slot, old_mask) * nchk,
      (slot, species) * nwr, edit_offset * nedit, edits...]
-    edit  [kind | cnt << 8 | arg << 16, target coord, ref * cnt, (mask * cnt for adds)]
-          nli edits: [h, target coord, table offset, record offset, ref * cnt] with the
-          hot-relative offsets of the group's nli table (0 = none) and member record
+    edit  [kind | cnt << 8 | arg << 16, target slot, ref * cnt, (mask * cnt for adds)]
+          nli edits through a member scan: [h, target slot, 0, record offset, ref * cnt]
+          with the hot-relative offset of the group's member record;
+          nli edits through a table: [h, target slot, index base, slot * cnt, mul * cnt]:
+          the table entry is index_base + sum(code(slot_c) * mul_c), the constant
+          references and the table's own offset folded into index_base
     kind  2 = guarded del (arg = proc), 3 = add (arg = proc, cnt conditions),
-          4 = nli del, 5 = nli add (arg = group, cnt = the group's K coordinates)
+          4 = nli del, 5 = nli add (member scan; arg = group, cnt = the group's K),
+          6 = nli del, 7 = nli add (table; arg = group, cnt = its non-constant refs)
     ref   >= 0: slot index (value before the step); < 0: constant species -ref-2
+    Every edit's target coordinate is a slot, so its site is gathered with the others.
 
 ``chk`` are the old-species checks of first replaces (later ones are checked here),
 ``wr`` the final species of every replaced slot.  Edit offsets are relative to the
@@ -510,9 +515,10 @@ class ProgramBuilder:
         return len(ops)
 
     @staticmethod
-    def _fast_stream(stream, records):
+    def _fast_stream(stream, records, tabled=(), ns=0):
         """Resolved slot form of one process stream (see the module docstring); None
-        when it exceeds the on-chip limits."""
+        when it exceeds the on-chip limits.  ``tabled``: groups with an nli table over
+        ``ns`` species (their edits take the table form)."""
         slots: Dict[RelCoord, int] = {}
 
         def slot(c):
@@ -542,7 +548,7 @@ class ProgramBuilder:
                     chk.append((sl, op[2]))
                 static[sl] = op[3]
             elif kind == "gdel":
-                edits.append([op_header(2, 0, op[1]), pack_coord(*op[2])])
+                edits.append([op_header(2, 0, op[1]), slot(op[2])])
                 t = op[2]
                 reach = [max(reach[i], abs(t[i])) for i in range(3)]
             elif kind == "add":
@@ -559,14 +565,30 @@ class ProgramBuilder:
                 reach = [max(reach[i], abs(t[i])) for i in range(3)]
                 if dead:
                     continue  # this add_proc can never fire after the writes before it
-                edits.append([op_header(3, len(refs), op[1]), pack_coord(*op[2])] + refs + masks)
+                edits.append([op_header(3, len(refs), op[1]), slot(op[2])] + refs + masks)
             elif kind in ("li_del", "li_add"):
                 g, o = op[1], op[2]
                 coords, _mems = records[g]
                 refs = [ref(slot((o[0] + c[0], o[1] + c[1], o[2] + c[2], c[3]))) for c in coords]
-                # the group's nli table and record offsets are filled in by build()
-                edits.append([op_header(4 if kind == "li_del" else 5, len(coords), g), pack_coord(*o),
-                              ("tab", g), ("rec", g)] + refs)
+                target = slot(o)
+                if g in tabled:
+                    # table index = sum(code_k * (ns+1)^k), code = species or ns for null
+                    const, vslots, muls = 0, [], []
+                    for k, r in enumerate(refs):
+                        mul = (ns + 1) ** k
+                        if r < 0:
+                            sp = -r - 2
+                            const += (ns if sp < 0 else sp) * mul
+                        else:
+                            vslots.append(r)
+                            muls.append(mul)
+                    # the table offset is added by build()
+                    edits.append([op_header(6 if kind == "li_del" else 7, len(vslots), g), target,
+                                  ("tabc", g, const)] + vslots + muls)
+                else:
+                    # the group's record offset is filled in by build()
+                    edits.append([op_header(4 if kind == "li_del" else 5, len(coords), g), target,
+                                  0, ("rec", g)] + refs)
                 reach = [max(reach[i], abs(o[i])) for i in range(3)]
             else:
                 return None
@@ -644,8 +666,10 @@ class ProgramBuilder:
         off_hot = len(w.words)
         hot: List[int] = [0] * (P + 1)
         reach = [0, 0, 0]
+        base = len(m.species) + 1
+        tabled = {gi for gi, (coords, _mems) in enumerate(records) if base ** len(coords) <= NLI_TABLE_MAX}
         for p, stream in enumerate(proc_streams):
-            fast = self._fast_stream(stream, records)
+            fast = self._fast_stream(stream, records, tabled, len(m.species))
             if fast is None:
                 continue
             words, rch = fast
@@ -663,10 +687,9 @@ class ProgramBuilder:
             hot.extend([len(mems), len(coords)] + [pack_coord(*c) for c in coords])
             for proc, masks in mems:
                 hot.extend([proc] + list(masks))
-        base = len(m.species) + 1
         for gi, (coords, mems) in enumerate(records):
             K = len(coords)
-            if base ** K > NLI_TABLE_MAX:
+            if gi not in tabled:
                 continue
             table = []
             for idx in range(base ** K):
@@ -686,8 +709,8 @@ class ProgramBuilder:
             hot[tab_off + gi] = len(hot)
             hot.extend(table)
         for i in fixups:
-            what, gi = hot[i]
-            hot[i] = hot[tab_off + gi] if what == "tab" else hot[grp_off + gi]
+            what, gi = hot[i][0], hot[i][1]
+            hot[i] = hot[tab_off + gi] + hot[i][2] if what == "tabc" else hot[grp_off + gi]
         w.emit(*hot)
         header = [MAGIC, VERSION, BACKENDS[self.backend], P, len(m.species), self.null, m.spuck,
                   m.dimension, ngroups, len(m.layers), off_proc, off_touch, off_groups,
