@@ -400,6 +400,15 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
         ps[j] = 0;
       }
     }
+    // with every rate >= +0 every term n*r is >= +0, so is every partial sum, and adding
+    // a +0 term leaves a sum >= +0 unchanged bit for bit: the chain skips those adds
+    bool neg_rate = false;
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+      const int i = lane + 32 * j;
+      neg_rate |= i < P && (__double_as_longlong(sm.rates[i]) < 0);
+    }
+    const bool skip_zero = !__any_sync(0xffffffffu, neg_rate);
     double t = S.kmc_time, dt = S.kmc_time_step;
     int64_t kstep = S.kmc_step;
     // random numbers: every 32 steps, lane j draws step k + j's (ran_time, ran_proc,
@@ -454,7 +463,10 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
           for (int j = 0; j < 8; j++) t8[j] = (i + j < P) ? sm.term[i + j] : 0.0;
 #pragma unroll
           for (int j = 0; j < 8; j++)
-            if (i + j < P) { acc = __dadd_rn(acc, t8[j]); sm.accum[i + j] = acc; }
+            if (i + j < P) {
+              if (!(skip_zero && __double_as_longlong(t8[j]) == 0)) acc = __dadd_rn(acc, t8[j]);
+              sm.accum[i + j] = acc;
+            }
         }
       }
       from = P;
