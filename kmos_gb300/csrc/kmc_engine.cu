@@ -1074,6 +1074,8 @@ int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   return KMC_OK;
 }
 
+int ensure_aux(kmc_pool *p, size_t n);
+
 // Sorts the run list by model (stable) into ls / st and plans one launch per model.
 int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std::vector<int32_t> &ls,
              std::vector<int64_t> &st, std::vector<LaunchPlan> &plans) {
@@ -1122,26 +1124,51 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
     i = j;
   }
   if ((int)plans.size() > p->max_models) return fail(KMC_ERR_ARG, "too many models in one run");
-  return KMC_OK;
+  return ensure_aux(p, plans.size());
 }
 
 // Issues the planned launches on the pool stream (capturable: no host copies).
+// Streams and events for n concurrent per-model launches (created outside any capture).
+int ensure_aux(kmc_pool *p, size_t n) {
+  if (n > 1 && !p->fork_ev) CK(cudaEventCreateWithFlags(&p->fork_ev, cudaEventDisableTiming));
+  while (n > 1 && p->aux.size() < n) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    p->aux.push_back(st);
+    p->aux_ev.push_back(ev);
+  }
+  return KMC_OK;
+}
+
 int issue_run(kmc_pool *p, std::vector<LaunchPlan> &plans, const int32_t *d_list, const int64_t *d_steps,
               int32_t *d_trace) {
   CK(cudaMemsetAsync(p->d_counter, 0, sizeof(int32_t) * plans.size(), p->stream));
-  for (auto &L : plans) {
+  const bool fork = plans.size() > 1 && p->aux.size() >= plans.size();
+  if (fork) CK(cudaEventRecord(p->fork_ev, p->stream));
+  for (size_t i = 0; i < plans.size(); i++) {
+    LaunchPlan &L = plans[i];
     L.a.list = d_list + L.first;
     L.a.steps = d_steps + L.first;
     L.a.trace = d_trace;
+    cudaStream_t st = p->stream;
+    if (fork) {
+      st = p->aux[i];
+      CK(cudaStreamWaitEvent(st, p->fork_ev, 0));
+    }
     switch (L.np) {
-      case 1: kmc_run_kernel<1><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
-      case 2: kmc_run_kernel<2><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
-      case 4: kmc_run_kernel<4><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
-      default: kmc_run_kernel<8><<<L.blocks, L.threads, L.smem, p->stream>>>(L.a); break;
+      case 1: kmc_run_kernel<1><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 2: kmc_run_kernel<2><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 4: kmc_run_kernel<4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      default: kmc_run_kernel<8><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
     }
     CK(cudaGetLastError());
     p->launches++;
+    if (fork) CK(cudaEventRecord(p->aux_ev[i], st));
   }
+  if (fork)
+    for (size_t i = 0; i < plans.size(); i++) CK(cudaStreamWaitEvent(p->stream, p->aux_ev[i], 0));
   return KMC_OK;
 }
 
@@ -1267,6 +1294,11 @@ int kmc_pool_destroy(kmc_pool *p) {
   cudaFree(p->d_res); cudaFreeHost(p->h_res); cudaFree(p->d_phase);
   cudaFree(p->d_adm_list); cudaFree(p->d_adm_staged); cudaFree(p->d_adm_rates); cudaFree(p->d_adm_roff);
   cudaEventDestroy(p->ev0); cudaEventDestroy(p->ev1); cudaEventDestroy(p->tev0); cudaEventDestroy(p->tev1);
+  for (size_t i = 0; i < p->aux.size(); i++) {
+    cudaStreamDestroy(p->aux[i]);
+    cudaEventDestroy(p->aux_ev[i]);
+  }
+  if (p->fork_ev) cudaEventDestroy(p->fork_ev);
   cudaStreamDestroy(p->stream);
   delete p;
   return KMC_OK;

@@ -121,6 +121,11 @@ struct kmc_pool {
   unsigned long long *d_phase = nullptr;  // KMC_NPHASE cycle sums
   char *d_res = nullptr;   // results gather buffers
   char *h_res = nullptr;   // pinned
+  // per-model launches of one run go to these streams (forked from and joined back to
+  // `stream` with events) so one model's launch tail overlaps the others' work
+  std::vector<cudaStream_t> aux;
+  std::vector<cudaEvent_t> aux_ev;
+  cudaEvent_t fork_ev = nullptr;
   size_t res_cap = 0;
 };
 

@@ -13,12 +13,22 @@ the device with the requests already running.
 Each trajectory's random stream is Philox keyed by (seed, trajectory id), so a request's
 result is the same alone and in any mix.
 
+Scheduling policy: "fifo" admits in arrival order.  "srpt" (shortest remaining
+processing time) admits the waiting request with the fewest remaining steps first and,
+when the arena or the slot table is full, evicts the resident trajectory with the most
+remaining steps if it has more than ``evict_ratio`` times the head's: its state image
+(kmc_pool_save_state, a compact copy of lattice, tables, counters, clock and random
+stream) goes to host memory and the request back to the queue, to be restored
+(kmc_pool_restore_state) and continued bit for bit later.  Short requests then no longer
+wait behind long ones.
+
 kmos has no counterpart (it runs one model per process; ``ModelRunner``,
 kmos/run/__init__.py:1991-2368, forks one process per parameter set).
 """
 from __future__ import annotations
 
 import collections
+import heapq
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence
@@ -46,6 +56,8 @@ class Request:
     done: float = -1.0
     result: Optional[dict] = None
     error: Optional[str] = None
+    image: Optional[bytes] = None   # state while evicted to host memory
+    evictions: int = 0
 
 
 @dataclass
@@ -62,17 +74,24 @@ class ModelEntry:
 class Server:
     """Continuous-batching server over one pool."""
 
-    def __init__(self, arena_bytes: int, max_slots: int = 8192, quantum: int = 20000, device: int = 0):
+    def __init__(self, arena_bytes: int, max_slots: int = 8192, quantum: int = 20000, device: int = 0,
+                 policy: str = "fifo", evict_ratio: float = 4.0, max_evict: int = 64):
+        if policy not in ("fifo", "srpt"):
+            raise ValueError("policy must be fifo or srpt")
         self.pool = E.Pool(arena_bytes=arena_bytes, max_slots=max_slots, device=device)
         self.max_slots = max_slots
         self.quantum = int(quantum)
+        self.policy = policy
+        self.evict_ratio = float(evict_ratio)
+        self.max_evict = int(max_evict)
         self.models: Dict[str, ModelEntry] = {}
-        self.waiting: collections.deque = collections.deque()
+        self.waiting = _Queue(policy)
         self.active: Dict[int, Request] = {}
         self.finished: List[Request] = []
         self.t0 = time.perf_counter()
         self.kmc_steps = 0
         self.quanta = 0
+        self.evicted = 0
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -94,25 +113,70 @@ class Server:
             raise ValueError("request %d: %d rates for %d processes" % (req.rid, len(req.rates),
                                                                        self.models[req.model].nproc))
         req.remaining = int(req.steps)
-        self.waiting.append(req)
+        self.waiting.push(req)
 
     # ------------------------------------------------------------------ scheduling
+    def _need(self, req: Request) -> int:
+        return self.pool.slot_bytes(self.models[req.model].model_id, req.size)
+
+    def _evict(self) -> int:
+        """srpt: while the queue's head does not fit and a resident trajectory has far
+        more steps left, move that trajectory's state to host memory."""
+        if self.policy != "srpt" or not self.waiting or not self.active:
+            return 0
+        n = 0
+        victims = sorted(self.active.values(), key=lambda r: -r.remaining)
+        free = self.pool.free_bytes()[0]
+        head = self.waiting.peek()
+        need = self._need(head)
+        for v in victims:
+            if n >= self.max_evict:
+                break
+            fits = len(self.active) < self.max_slots and need <= free
+            if fits or v.remaining <= self.evict_ratio * head.remaining:
+                break
+            v.image = self.pool.save_state(v.slot)
+            free += self._need(v)
+            self.pool.release(v.slot)
+            del self.active[v.slot]
+            v.slot = -1
+            v.evictions += 1
+            self.waiting.push(v)
+            n += 1
+        self.evicted += n
+        return n
+
     def _admit(self) -> int:
-        """Admits waiting requests in arrival order while the arena and the slot table
-        have room (admission by free HBM)."""
+        """Admits waiting requests in policy order while the arena and the slot table
+        have room (admission by free HBM); evicted requests are restored from their
+        images."""
         batch: List[Request] = []
+        restored = 0
         free, _largest = self.pool.free_bytes()
         budget = free
         while self.waiting and len(self.active) + len(batch) < self.max_slots:
-            req = self.waiting[0]
-            entry = self.models[req.model]
-            need = self.pool.slot_bytes(entry.model_id, req.size)
+            req = self.waiting.peek()
+            need = self._need(req)
             if need > budget:
                 break
+            self.waiting.pop()
+            if req.image is not None:
+                try:
+                    s = self.pool.restore_state(self.models[req.model].model_id, req.image)
+                except E.KMCError as err:
+                    if err.code != 6:
+                        raise
+                    self.waiting.push(req)  # fragmentation: try again next quantum
+                    break
+                req.image, req.slot = None, s
+                self.active[s] = req
+                restored += 1
+                budget = self.pool.free_bytes()[0]
+                continue
             budget -= need
-            batch.append(self.waiting.popleft())
+            batch.append(req)
         if not batch:
-            return 0
+            return restored
         try:
             slots = self.pool.admit_many([self.models[r.model].model_id for r in batch], [r.size for r in batch],
                                          [r.rates for r in batch], seeds=[r.seed for r in batch],
@@ -133,11 +197,11 @@ class Server:
         t = self.now()
         for r, s in zip(batch, slots):
             if s is None:
-                self.waiting.appendleft(r)
+                self.waiting.push(r)
                 continue
             r.slot, r.admitted = s, t
             self.active[s] = r
-        return len([s for s in slots if s is not None])
+        return restored + len([s for s in slots if s is not None])
 
     def _retire(self, reqs: List[Request]) -> None:
         if not reqs:
@@ -201,6 +265,7 @@ class Server:
                 break
             while pending and pending[0].arrival <= t:
                 self.submit(pending.popleft())
+            self._evict()
             self._admit()
             if self.active:
                 self.run_quantum()
@@ -212,6 +277,35 @@ class Server:
 
     def close(self):
         self.pool.close()
+
+
+class _Queue:
+    """Waiting requests: arrival order (fifo) or fewest remaining steps first (srpt)."""
+
+    def __init__(self, policy: str):
+        self.policy = policy
+        self.items: list = []
+        self.fifo: collections.deque = collections.deque()
+        self.n = 0
+
+    def push(self, r: Request) -> None:
+        if self.policy == "srpt":
+            heapq.heappush(self.items, (r.remaining, r.arrival, r.rid, self.n, r))
+            self.n += 1
+        else:
+            self.fifo.append(r)
+
+    def peek(self) -> Request:
+        return self.items[0][-1] if self.policy == "srpt" else self.fifo[0]
+
+    def pop(self) -> Request:
+        return heapq.heappop(self.items)[-1] if self.policy == "srpt" else self.fifo.popleft()
+
+    def __len__(self) -> int:
+        return len(self.items) if self.policy == "srpt" else len(self.fifo)
+
+    def __bool__(self) -> bool:
+        return len(self) > 0
 
 
 def latency_stats(reqs: Sequence[Request]) -> dict:
@@ -235,9 +329,12 @@ def main(argv=None):
     ap.add_argument("--quantum", type=int, default=20000)
     ap.add_argument("--arena-gb", type=float, default=64.0)
     ap.add_argument("--deadline", type=float, default=float("inf"))
+    ap.add_argument("--policy", default="fifo", choices=["fifo", "srpt"])
+    ap.add_argument("--max-slots", type=int, default=16384)
     a = ap.parse_args(argv)
     reqs, progs = configs.serving_requests(rate=a.rate, duration=a.duration, steps_scale=a.steps_scale)
-    srv = Server(arena_bytes=int(a.arena_gb * (1 << 30)), max_slots=16384, quantum=a.quantum)
+    srv = Server(arena_bytes=int(a.arena_gb * (1 << 30)), max_slots=a.max_slots, quantum=a.quantum,
+                 policy=a.policy)
     for k, p in progs.items():
         srv.add_model(k, p)
     t0 = time.perf_counter()
@@ -248,7 +345,8 @@ def main(argv=None):
     line = {"metric": "serving p50/p99 request latency", "requests": len(reqs), "rate_per_s": a.rate,
             "duration_s": a.duration, "steps_scale": a.steps_scale, "quantum": a.quantum,
             "offered_steps": offered, "served_steps": srv.kmc_steps, "wall_s": wall,
-            "steps_per_s": srv.kmc_steps / wall, "quanta": srv.quanta, **stats}
+            "steps_per_s": srv.kmc_steps / wall, "quanta": srv.quanta, "policy": a.policy,
+            "max_slots": a.max_slots, "evictions": srv.evicted, **stats}
     srv.close()
     print(json.dumps(line))
     return line

@@ -64,3 +64,40 @@ def test_quantum_size_does_not_change_results():
     for rid in a:
         np.testing.assert_array_equal(a[rid].result["procstat"], b[rid].result["procstat"])
         assert a[rid].result["kmc_time"] == b[rid].result["kmc_time"]
+
+
+def test_srpt_evicts_and_results_do_not_change():
+    """Shortest-remaining-first with eviction: two long trajectories fill the arena, then
+    short requests arrive; a long one is saved to host memory, the short ones run, and the
+    long one is restored later.  Every result equals the request run alone (state images
+    restore bit for bit)."""
+    reqs, progs = small_stream(n=40)
+    tmpl = next(r for r in reqs if r.model == "c3")
+    longs = [serving.Request(model="c3", size=(40, 40), rates=tmpl.rates, steps=20000, seed=3, traj_id=i,
+                             rid=100 + i, arrival=0.0) for i in range(2)]
+    shorts = [serving.Request(model="c3", size=(16, 16), rates=tmpl.rates, steps=600, seed=4, traj_id=10 + i,
+                              rid=200 + i, arrival=0.05) for i in range(6)]
+    probe = serving.Server(arena_bytes=1 << 20, max_slots=4)
+    for k, p in progs.items():
+        probe.add_model(k, p)
+    need_long = probe.pool.slot_bytes(probe.models["c3"].model_id, (40, 40))
+    need_short = probe.pool.slot_bytes(probe.models["c3"].model_id, (16, 16))
+    probe.close()
+    assert need_short > 4096
+    srv = serving.Server(arena_bytes=2 * need_long + 1024, max_slots=64, quantum=300, policy="srpt")
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    out = {r.rid: r for r in srv.serve(longs + shorts)}
+    evicted = srv.evicted
+    srv.close()
+    assert len(out) == len(longs) + len(shorts) and evicted > 0
+    assert any(out[r.rid].evictions > 0 for r in longs)
+    # the short requests finished before the long ones
+    assert max(out[r.rid].done for r in shorts) < max(out[r.rid].done for r in longs)
+    for r in longs + shorts[:2]:
+        alone = serve([clone(r)], progs, arena=need_long + 4096, quantum=300)[r.rid]
+        a, b = alone.result, out[r.rid].result
+        assert a["kmc_step"] == b["kmc_step"] and a["kmc_time"] == b["kmc_time"]
+        np.testing.assert_array_equal(a["procstat"], b["procstat"])
+        np.testing.assert_array_equal(a["integ_rates"], b["integ_rates"])
+        np.testing.assert_array_equal(a["coverage"], b["coverage"])
