@@ -170,6 +170,31 @@ struct Geometry {
   }
 };
 
+// n / d by a multiply and a shift for 0 <= n < 2^31 (Granlund & Montgomery, "Division by
+// invariant integers using multiplication", PLDI 1994): with p = 32 + ceil(log2 d) and
+// m = ceil(2^p / d), m*d - 2^p < d <= 2^(p-32), so floor(n*m / 2^p) = floor(n / d) for
+// every n < 2^32; n < 2^31 keeps n*m below 2^64.
+struct FastDiv {
+  unsigned long long m;
+  int p;
+  __host__ __device__ inline void init(unsigned d) {
+    int l = 0;
+    while (l < 31 && (1u << l) < d) l++;
+    p = 32 + l;
+    m = ((1ull << p) + d - 1) / d;
+  }
+  __host__ __device__ inline unsigned div(unsigned n) const { return (unsigned)(((unsigned long long)n * m) >> p); }
+};
+
+// (double)n for 0 <= n < 2^31 from its bit pattern: integer instructions only, so the
+// conversion takes no slot of the FP64 pipe.
+__device__ inline double int_to_double(int n) {
+  if (n <= 0) return 0.0;
+  const int e = 31 - __clz(n);
+  return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) |
+                                          (((unsigned long long)n << (52 - e)) & 0xFFFFFFFFFFFFFull)));
+}
+
 __host__ __device__ inline bool in_mask(int species, int32_t mask) {
   const int bit = species < 0 ? 31 : species;
   return ((uint32_t)mask >> bit) & 1u;

@@ -369,6 +369,10 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
     v.ns = sm.ns;
     v.prog = M.prog;
     v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
+    FastDiv div_spuck, div_x, div_y;  // calculate_nr2lattice without hardware division
+    div_spuck.init(M.spuck);
+    div_x.init(S.X);
+    div_y.init(S.Y);
     v.stride = stride;
     v.backend = M.backend;
     v.P = P;
@@ -490,7 +494,12 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
       }
       const int n = sm.ns[proc];
       if (n <= 0) { status = ST_DEADLOCK; break; }
-      int idx = (int)__dadd_rn(1.0, __dmul_rn(ran_site, (double)n));
+      // idx = int(1 + ran_site * n): the int -> double and the truncation by bit
+      // manipulation (exact for 1 <= n < 2^31 and 1 <= q < 2^32), the product and the sum
+      // in FP64 as the reference rounds them
+      const long long qb = __double_as_longlong(__dadd_rn(1.0, __dmul_rn(ran_site, int_to_double(n))));
+      const int qe = (int)(qb >> 52) - 1023;
+      int idx = (int)((((unsigned long long)qb & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - qe));
       if (idx > n) idx = n;
 
 #pragma unroll
@@ -517,8 +526,17 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
 
       if (lane == 0 && a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
       site = __shfl_sync(0xffffffffu, site, 0);
+      if (site < 1 || site > S.V) { status = ST_TABLE; break; }  // list entry outside the lattice
       int bx, by, bz, bn;
-      v.g.coords(site, bx, by, bz, bn);
+      {  // calculate_nr2lattice (lattice.mpy:177-210)
+        const unsigned c = div_spuck.div((unsigned)(site - 1));
+        bn = site - M.spuck * (int)c;
+        const unsigned r = div_x.div(c);
+        bx = (int)(c - (unsigned)S.X * r);
+        const unsigned zq = div_y.div(r);
+        by = (int)(r - (unsigned)S.Y * zq);
+        bz = (int)zq;
+      }
       KMC_PHASE(sm, 3);
       if (fs_off) {
         err = fast_step<NP>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
@@ -542,7 +560,7 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
         const int i = lane + 32 * j;
         const int nn = i < P ? sm.ns[i] : 0;
         const bool ch = i < P && nn != n0[j];
-        if (ch) { sm.term[i] = __dmul_rn((double)nn, sm.rates[i]); n0[j] = nn; }
+        if (ch) { sm.term[i] = __dmul_rn(int_to_double(nn), sm.rates[i]); n0[j] = nn; }
         const unsigned b = __ballot_sync(0xffffffffu, ch);
         if (first == P && b) first = 32 * j + __ffs(b) - 1;
       }
