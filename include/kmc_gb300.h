@@ -209,9 +209,11 @@ KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
 KMC_API int kmc_pool_timer_start(kmc_pool *pool);
 KMC_API int kmc_pool_timer_stop(kmc_pool *pool, float *ms);
 /* Cycles the step kernel spent per phase, summed over warps, in builds compiled with
- * KMC_PHASE_TIMING (12 entries: draws, accum, clock/integ/bisection, site pick, slot
- * gather, edit evaluation, process heads, replay, lattice writes, serial interpreter,
- * term refresh, spare); other builds return KMC_ERR_ARG.  reset != 0 clears the sums. */
+ * KMC_PHASE_TIMING (16 entries: draws, accum, clock/integ/bisection, site pick, slot
+ * gather, end of edit evaluation, table-load stores, replay, lattice writes, serial
+ * interpreter, term refresh, slot sites, then per evaluation round: edit decode and nli,
+ * del-position load, del rank and list-entry load, compaction); other builds return
+ * KMC_ERR_ARG.  reset != 0 clears the sums. */
 KMC_API int kmc_pool_phase_cycles(kmc_pool *pool, uint64_t *out, int32_t reset);
 /* Kernel launches issued by this pool since creation. */
 KMC_API int kmc_pool_launch_count(kmc_pool *pool, int64_t *count);

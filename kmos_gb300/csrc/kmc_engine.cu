@@ -67,7 +67,7 @@ using namespace kmc_host;
   do {                   \
   } while (0)
 #endif
-constexpr int KMC_NPHASE = 12;
+constexpr int KMC_NPHASE = 16;
 
 template <int NP>
 struct WarpSmem {
@@ -233,7 +233,20 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
       if (op >= 6) {  // nli through its table: index_base + sum(code(slot) * mul)
         int idx = e[2];
-        for (int c = 0; c < cnt; c++) idx += species_code(f.latv[e[3 + c]], H.nspecies) * e[3 + cnt + c];
+        if (cnt > 0 && cnt <= 8) {
+          // eight independent reads, clamped to the record, so they issue together
+          const int cm = cnt - 1;
+          int sl[8], mu[8];
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            sl[c] = e[3 + min(c, cm)];
+            mu[c] = e[3 + cnt + min(c, cm)];
+          }
+#pragma unroll
+          for (int c = 0; c < 8; c++) idx += c < cnt ? species_code(f.latv[sl[c]], H.nspecies) * mu[c] : 0;
+        } else {
+          for (int c = 0; c < cnt; c++) idx += species_code(f.latv[e[3 + c]], H.nspecies) * e[3 + cnt + c];
+        }
         p = H.h[idx];
         on = p != 0;
         kind = op == 6 ? E_DEL : E_ADD;
@@ -248,11 +261,13 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         on = p != 0;
         kind = op == 4 ? E_DEL : E_ADD;
       }
-      if (on) {
-        site = f.latsite[e[1]];
-        if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
-      }
     }
+    KMC_PHASE(sm, 12);
+    if (on) {
+      site = f.latsite[fs[eoff[k] + 1]];
+      if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
+    }
+    KMC_PHASE(sm, 13);
     // a del's rank among its process's dels picks which list entry it loads; the ranks
     // only have to be distinct, so a shared-memory counter gives them in any order
     if (on && kind != E_ADD) {
@@ -264,6 +279,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
         if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)q * v.stride + n0 - rank];
       }
     }
+    KMC_PHASE(sm, 14);
     const unsigned b = __ballot_sync(0xffffffffu, on);
     if (on) {
       const int pos = ne + __popc(b & lt);
@@ -274,6 +290,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
       if (kind != E_ADD) empos[rr] = pos;
     }
     ne += __popc(b);
+    KMC_PHASE(sm, 15);
   }
   const int rounds = (ne + 31) >> 5;
   KMC_PHASE(sm, 5);

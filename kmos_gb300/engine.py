@@ -451,7 +451,7 @@ class Pool:
 
     def phase_cycles(self, reset: bool = True) -> np.ndarray:
         """Per-phase cycle sums of the step kernel (library built with KMC_PHASE_TIMING)."""
-        out = np.zeros(12, np.uint64)
+        out = np.zeros(16, np.uint64)
         _check(load().kmc_pool_phase_cycles(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                                             1 if reset else 0))
         return out

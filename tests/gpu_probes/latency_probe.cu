@@ -24,6 +24,21 @@ __global__ void chase_smem(int iters, unsigned *out, long long *cyc) {
   if (threadIdx.x == 0) { out[0] = p; cyc[0] = (t1 - t0) / iters; }
 }
 
+// The same chase through a generic pointer to the shared array (the address space is
+// hidden from the compiler by selecting it at run time), as the engine reads a model's
+// hot section that may sit in shared or global memory.
+__global__ void chase_smem_generic(const unsigned *gbuf, int use_global, int iters, unsigned *out, long long *cyc) {
+  __shared__ unsigned nx[1024];
+  for (int i = threadIdx.x; i < 1024; i += blockDim.x) nx[i] = (i * 97 + 13) & 1023;
+  __syncthreads();
+  const unsigned *src = use_global ? gbuf : nx;
+  unsigned p = threadIdx.x;
+  long long t0 = clock64();
+  for (int i = 0; i < iters; i++) p = src[p];
+  long long t1 = clock64();
+  if (threadIdx.x == 0) { out[0] = p; cyc[0] = (t1 - t0) / iters; }
+}
+
 __global__ void store_load(unsigned *buf, int iters, unsigned *out, long long *cyc) {
   unsigned v = threadIdx.x;
   long long t0 = clock64();
@@ -88,6 +103,9 @@ int main() {
   chase_smem<<<1, 32>>>(4000, out, cyc);
   long long c; cudaMemcpy(&c, cyc, 8, cudaMemcpyDeviceToHost);
   printf("dependent shared-memory load           : %lld cycles\n", c);
+  chase_smem_generic<<<1, 32>>>(out, 0, 4000, out, cyc);
+  cudaMemcpy(&c, cyc, 8, cudaMemcpyDeviceToHost);
+  printf("dependent shared-memory load, generic  : %lld cycles\n", c);
   unsigned *buf; cudaMalloc(&buf, 1 << 20);
   store_load<<<1, 32>>>(buf, 100, out, cyc);
   store_load<<<1, 32>>>(buf, 4000, out, cyc);
