@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--sides", default="", help="config 3: comma-separated lattice sides to draw from")
     ap.add_argument("--fast", type=int, default=1, help="gather / replay step path (0: serial interpreter)")
     ap.add_argument("--autotune", type=int, default=1, help="pick the launch shape on scratch trajectories first")
+    ap.add_argument("--cpu-steps", type=int, default=0,
+                    help="kMC steps per trajectory of the CPU sample (default: a 10-30 s sample per config)")
     return ap.parse_args()
 
 
@@ -175,13 +177,13 @@ def _cpu_worker(args):
 CPU_STEPS = {1: 2_000_000, 2: 1_000_000, 3: 300_000, 4: 1_000_000}
 
 
-def cpu_sample(config: int, rounds: int = 1):
+def cpu_sample(config: int, rounds: int = 1, steps: int = 0):
     """The oracle (the CPU restatement of the reference loop, one process per core, each
     on its own trajectory) on all host cores.  Returns (steps/s aggregate, cores, sample)."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    steps = CPU_STEPS[config]
+    steps = steps or CPU_STEPS[config]
     ctx = mp.get_context("spawn")
     total, wall = 0, 0.0
     with ctx.Pool(cores) as pool:
@@ -192,6 +194,13 @@ def cpu_sample(config: int, rounds: int = 1):
             total += sum(s for s, _ in res)
     sample = "%d trajectories x %d kMC steps of config %d, one process per core" % (cores * rounds, steps, config)
     return total / wall, cores, sample
+
+
+def replica_trajs(trajs, rank: int):
+    """Philox trajectory ids of one rank's replica batch: the same workload with ids
+    offset by rank * batch size, so ranks run disjoint, reproducible trajectories."""
+    n = len(trajs)
+    return [int(t) + rank * n for t in trajs]
 
 
 def step_bytes(config: int, chunk: int = 50000):
@@ -217,8 +226,8 @@ def run_reference(args, dist: Dist):
     if dist.rank != 0:
         dist.close()
         return
-    warm = [cpu_sample(args.config) for _ in range(min(args.warmup, 1))]
-    vals = [cpu_sample(args.config) for _ in range(max(1, min(args.steps, 3)))]
+    warm = [cpu_sample(args.config, steps=args.cpu_steps) for _ in range(min(args.warmup, 1))]
+    vals = [cpu_sample(args.config, steps=args.cpu_steps) for _ in range(max(1, min(args.steps, 3)))]
     value = statistics.median(v for v, _c, _s in vals)
     _v, cores, sample = vals[0]
     from kmos_gb300 import configs
@@ -260,7 +269,7 @@ def run_ours(args, dist: Dist):
     if not args.fast:
         pool.set_fast_path(False)
     mid = pool.add_model(wl.program)
-    trajs = [t + dist.rank * n for t in wl.trajs]
+    trajs = replica_trajs(wl.trajs, dist.rank)
     slots = []
     B = 1024
     for i in range(0, n, B):
@@ -345,7 +354,7 @@ def run_ours(args, dist: Dist):
             traffic = tr.get("bytes_per_kmc_step", 0) * kmc_steps_rank / args.steps
         cpu = None
         if args.cpu_baseline:
-            v, cores, sample = cpu_sample(args.config)
+            v, cores, sample = cpu_sample(args.config, steps=args.cpu_steps)
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
