@@ -172,6 +172,10 @@ KMC_API int kmc_pool_get_integ_rates(kmc_pool *pool, int32_t slot, double *out);
 KMC_API int kmc_pool_get_nr_of_sites(kmc_pool *pool, int32_t slot, int32_t *out);
 KMC_API int kmc_pool_get_lattice(kmc_pool *pool, int32_t slot, int32_t *out);
 KMC_API int kmc_pool_get_tables(kmc_pool *pool, int32_t slot, int32_t *as1, int32_t *as2);
+/* base.set_rate_const for every process of a resident trajectory (rates[P], base.mpy:
+ * 581-601) followed by update_accum_rate before its next step: new parameters (T,
+ * partial pressures) for a trajectory that keeps its lattice, tables and clock. */
+KMC_API int kmc_pool_set_rates(kmc_pool *pool, int32_t slot, const double *rates);
 /* Occupation counts of many slots at once, reduced on the device: out[i] holds the
  * [nspecies][spuck] counts of slots[i] (int64), with stride `stride` int64 per slot. */
 KMC_API int kmc_pool_occupation_counts(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride, int64_t *out);

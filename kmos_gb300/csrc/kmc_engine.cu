@@ -1654,6 +1654,22 @@ int kmc_pool_get_lattice(kmc_pool *p, int32_t slot, int32_t *out) {
   return KMC_OK;
 }
 
+int kmc_pool_set_rates(kmc_pool *p, int32_t slot, const double *rates) {
+  int rc = check_slot(p, slot);
+  if (rc) return rc;
+  if (!rates) return fail(KMC_ERR_ARG, "bad arguments");
+  std::lock_guard<std::mutex> lock(p->mu);
+  CK(cudaSetDevice(p->device));
+  CK(cudaStreamSynchronize(p->stream));
+  SlotHost &sh = p->slots[slot];
+  CK(cudaMemcpy(sh.dev.rates, rates, sizeof(double) * sh.dev.P, cudaMemcpyHostToDevice));
+  // the next step recomputes every n*r term and the whole prefix sum (update_accum_rate)
+  const int32_t zero = 0;
+  CK(cudaMemcpy(&p->d_slots[slot].accum_from, &zero, sizeof(int32_t), cudaMemcpyHostToDevice));
+  sh.dev.accum_from = 0;
+  return KMC_OK;
+}
+
 int kmc_pool_get_tables(kmc_pool *p, int32_t slot, int32_t *as1, int32_t *as2) {
   int rc = check_slot(p, slot);
   if (rc) return rc;

@@ -83,6 +83,7 @@ SIGNATURES = {
     "kmc_pool_get_nr_of_sites": (_i32, [_vp, _i32, _p32]),
     "kmc_pool_get_lattice": (_i32, [_vp, _i32, _p32]),
     "kmc_pool_get_tables": (_i32, [_vp, _i32, _p32, _p32]),
+    "kmc_pool_set_rates": (_i32, [_vp, _i32, _pd]),
     "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
     "kmc_pool_occupation_counts_static": (_i32, [_vp, _p32, _i32, _i32, _p64]),
     "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
@@ -500,6 +501,13 @@ class Pool:
         as2 = np.zeros(P * (volume + 1), np.int32)
         _check(load().kmc_pool_get_tables(self.h, int(slot), _ptr(as1, _i32), _ptr(as2, _i32)))
         return as1.reshape(P, volume + 1), as2.reshape(P, volume + 1)
+
+    def set_rates(self, slot: int, rates):
+        """New rate constants for a resident trajectory (``kmc_pool_set_rates``)."""
+        r = np.ascontiguousarray(rates, dtype=np.float64)
+        if len(r) != self.nproc(self.slot_model[int(slot)]):
+            raise ValueError("one rate per process")
+        _check(load().kmc_pool_set_rates(self.h, int(slot), _ptr(r, _dbl)))
 
     def results(self, slots, stride: int):
         """procstat [n, stride], integ [n, stride], kmc_time [n], kmc_step [n], status [n]

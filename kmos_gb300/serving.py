@@ -13,6 +13,15 @@ the device with the requests already running.
 Each trajectory's random stream is Philox keyed by (seed, trajectory id), so a request's
 result is the same alone and in any mix.
 
+Sessions: requests naming the same ``session`` continue one trajectory.  After a
+session's request finishes, its trajectory stays resident (lattice, tables, rates, clock
+and random stream) for the next request of that session, which may bring new rate
+constants (a new temperature or pressure: ``kmc_pool_set_rates``) and runs on from the
+same state; a session's requests run one after the other.  Idle sessions are the first
+moved to host memory when admission needs room.  A request with ``keep=False`` ends its
+session.  Results report the request's own interval (TOFs from the procstat and
+integ_rates differences over its kmc_time) beside the trajectory's totals.
+
 Scheduling policy: "fifo" admits in arrival order.  "srpt" (shortest remaining
 processing time) admits the waiting request with the fewest remaining steps first and,
 when the arena or the slot table is full, evicts the resident trajectory with the most
@@ -31,7 +40,7 @@ import collections
 import heapq
 import time
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -43,7 +52,7 @@ from .program import Program
 class Request:
     model: str                      # key of a registered model
     size: Sequence[int]             # system size per axis
-    rates: Sequence[float]          # rate constant per process
+    rates: Optional[Sequence[float]]  # rate constant per process (None: a session's current rates)
     steps: int                      # kMC steps to run
     seed: int = 1
     traj_id: int = 0                # Philox key word: a request's stream identity
@@ -58,6 +67,20 @@ class Request:
     error: Optional[str] = None
     image: Optional[bytes] = None   # state while evicted to host memory
     evictions: int = 0
+    session: Optional[str] = None   # requests of one session continue one trajectory
+    keep: bool = True               # with a session: keep its trajectory after this request
+    start: Optional[tuple] = None   # (procstat, integ_rates, kmc_time) when the request began
+
+
+@dataclass
+class Session:
+    model: str
+    size: Tuple[int, ...]
+    slot: int = -1                  # resident and idle when >= 0 and not busy
+    image: Optional[bytes] = None   # state while evicted to host memory
+    busy: bool = False              # a request of this session is queued or running
+    queue: collections.deque = field(default_factory=collections.deque)
+    last_used: float = 0.0
 
 
 @dataclass
@@ -92,6 +115,7 @@ class Server:
         self.kmc_steps = 0
         self.quanta = 0
         self.evicted = 0
+        self.sessions: Dict[str, Session] = {}
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -109,15 +133,58 @@ class Server:
     def submit(self, req: Request) -> None:
         if req.model not in self.models:
             raise KeyError("unknown model %r" % req.model)
-        if len(req.rates) != self.models[req.model].nproc:
+        continuing = req.session is not None and req.session in self.sessions
+        if req.rates is None and not continuing:
+            raise ValueError("request %d: rates are needed to start a trajectory" % req.rid)
+        if req.rates is not None and len(req.rates) != self.models[req.model].nproc:
             raise ValueError("request %d: %d rates for %d processes" % (req.rid, len(req.rates),
                                                                        self.models[req.model].nproc))
         req.remaining = int(req.steps)
+        if req.session is not None:
+            sess = self.sessions.get(req.session)
+            if sess is None:
+                self.sessions[req.session] = Session(req.model, tuple(req.size), busy=True)
+            else:
+                if sess.model != req.model or tuple(sess.size) != tuple(req.size):
+                    raise ValueError("request %d: session %r runs model %r on %s" % (req.rid, req.session, sess.model,
+                                                                                    sess.size))
+                if sess.busy:
+                    sess.queue.append(req)  # after the session's current request
+                    return
+                sess.busy = True
         self.waiting.push(req)
+
+    def close_session(self, name: str) -> None:
+        """Drops a session's trajectory (resident or in host memory)."""
+        sess = self.sessions.pop(name, None)
+        if sess is not None and sess.slot >= 0 and not sess.busy:
+            self.pool.release(sess.slot)
 
     # ------------------------------------------------------------------ scheduling
     def _need(self, req: Request) -> int:
+        sess = self.sessions.get(req.session) if req.session is not None else None
+        if sess is not None and sess.slot >= 0:
+            return 0  # continues a resident trajectory
         return self.pool.slot_bytes(self.models[req.model].model_id, req.size)
+
+    def _resident(self) -> int:
+        """Slots in use: running requests and resident session trajectories waiting for
+        their next request."""
+        return len(self.active) + sum(1 for x in self.sessions.values() if x.slot >= 0)
+
+    def _evict_idle(self, need: int) -> None:
+        """Moves idle resident sessions (least recently used first) to host memory until
+        ``need`` bytes are free or none is left."""
+        idle = sorted((s for s in self.sessions.values() if s.slot >= 0 and not s.busy), key=lambda s: s.last_used)
+        free = self.pool.free_bytes()[0]
+        for sess in idle:
+            if need <= free and self._resident() < self.max_slots:
+                break
+            sess.image = self.pool.save_state(sess.slot)
+            free += self.pool.slot_bytes(self.models[sess.model].model_id, sess.size)
+            self.pool.release(sess.slot)
+            sess.slot = -1
+            self.evicted += 1
 
     def _evict(self) -> int:
         """srpt: while the queue's head does not fit and a resident trajectory has far
@@ -152,14 +219,39 @@ class Server:
         images."""
         batch: List[Request] = []
         restored = 0
+        started: List[Request] = []
+        if self.waiting:
+            head = self.waiting.peek()
+            self._evict_idle(self._need(head))
         free, _largest = self.pool.free_bytes()
         budget = free
-        while self.waiting and len(self.active) + len(batch) < self.max_slots:
+        while self.waiting and self._resident() + len(batch) < self.max_slots:
             req = self.waiting.peek()
             need = self._need(req)
             if need > budget:
                 break
             self.waiting.pop()
+            sess = self.sessions.get(req.session) if req.session is not None else None
+            if sess is not None and (sess.slot >= 0 or sess.image is not None):
+                # a session's next request: its trajectory runs on, with the new rates
+                if sess.slot < 0:
+                    try:
+                        sess.slot = self.pool.restore_state(self.models[req.model].model_id, sess.image)
+                    except E.KMCError as err:
+                        if err.code != 6:
+                            raise
+                        self.waiting.push(req)
+                        break
+                    sess.image = None
+                    budget = self.pool.free_bytes()[0]
+                if req.rates is not None:
+                    self.pool.set_rates(sess.slot, req.rates)
+                req.slot, req.admitted = sess.slot, self.now()
+                sess.slot = -1  # the running request owns the trajectory until it retires
+                self.active[req.slot] = req
+                started.append(req)
+                restored += 1
+                continue
             if req.image is not None:
                 try:
                     s = self.pool.restore_state(self.models[req.model].model_id, req.image)
@@ -175,6 +267,7 @@ class Server:
                 continue
             budget -= need
             batch.append(req)
+        self._snapshot(started)
         if not batch:
             return restored
         try:
@@ -200,8 +293,19 @@ class Server:
                 self.waiting.push(r)
                 continue
             r.slot, r.admitted = s, t
+            r.start = None  # a fresh trajectory starts from zero counters
             self.active[s] = r
         return restored + len([s for s in slots if s is not None])
+
+    def _snapshot(self, reqs: List[Request]) -> None:
+        """Counters and clock of continued trajectories when their request begins."""
+        by_model: Dict[str, List[Request]] = collections.defaultdict(list)
+        for r in reqs:
+            by_model[r.model].append(r)
+        for key, rs in by_model.items():
+            ps, ig, times, _k, _st = self.pool.results([r.slot for r in rs], self.models[key].nproc)
+            for i, r in enumerate(rs):
+                r.start = (ps[i].copy(), ig[i].copy(), float(times[i]))
 
     def _retire(self, reqs: List[Request]) -> None:
         if not reqs:
@@ -219,18 +323,33 @@ class Server:
                 cells = int(np.prod(r.size))
                 if status[i] not in (0, 3):
                     r.error = "status %d" % status[i]
-                tt = times[i] if times[i] > 0 else np.inf
+                ps0, ig0, t0 = r.start if r.start is not None else (0, 0.0, 0.0)
+                dt = times[i] - t0
+                tt = dt if dt > 0 else np.inf
                 r.result = {
                     "kmc_time": float(times[i]), "kmc_step": int(steps[i]), "status": int(status[i]),
-                    "procstat": ps[i], "integ_rates": ig[i],
-                    "tof": dict(zip(entry.tof_names, entry.tof_matrix @ ps[i] / tt / cells)),
-                    "tof_integ": dict(zip(entry.tof_names, entry.tof_matrix @ ig[i] / tt / cells)),
+                    "procstat": ps[i], "integ_rates": ig[i], "interval_time": float(dt),
+                    "tof": dict(zip(entry.tof_names, entry.tof_matrix @ (ps[i] - ps0) / tt / cells)),
+                    "tof_integ": dict(zip(entry.tof_names, entry.tof_matrix @ (ig[i] - ig0) / tt / cells)),
                     "coverage": occ[i].reshape(entry.nspecies, entry.spuck) / cells,
                 }
                 r.done = t
-                self.pool.release(r.slot)
                 del self.active[r.slot]
                 self.finished.append(r)
+                sess = self.sessions.get(r.session) if r.session is not None else None
+                if sess is not None and r.keep and status[i] in (0, 3):
+                    sess.slot, sess.busy, sess.last_used = r.slot, False, t
+                    if sess.queue:  # the session's next request
+                        nxt = sess.queue.popleft()
+                        sess.busy = True
+                        self.waiting.push(nxt)
+                    continue
+                if sess is not None:
+                    self.sessions.pop(r.session, None)
+                    for nxt in sess.queue:
+                        nxt.error = "session %r ended" % r.session
+                        self.finished.append(nxt)
+                self.pool.release(r.slot)
 
     def run_quantum(self) -> None:
         """One persistent launch advancing every active trajectory."""
@@ -259,7 +378,7 @@ class Server:
         until every request finished (or ``deadline`` seconds passed)."""
         pending = collections.deque(sorted(arrivals, key=lambda r: r.arrival))
         self.t0 = time.perf_counter()
-        while pending or self.waiting or self.active:
+        while pending or self.waiting or self.active or any(s.queue for s in self.sessions.values()):
             t = self.now()
             if t > deadline:
                 break

@@ -3,7 +3,7 @@ mix, admission waits for free arena memory, and dead-locked trajectories retire.
 import numpy as np
 import pytest
 
-from kmos_gb300 import configs, serving
+from kmos_gb300 import configs, engine as E, serving
 
 pytestmark = pytest.mark.gpu
 
@@ -101,3 +101,75 @@ def test_srpt_evicts_and_results_do_not_change():
         np.testing.assert_array_equal(a["procstat"], b["procstat"])
         np.testing.assert_array_equal(a["integ_rates"], b["integ_rates"])
         np.testing.assert_array_equal(a["coverage"], b["coverage"])
+
+
+def test_session_continues_one_trajectory():
+    """Two requests of one session (the second with new rates) end in the state of one
+    trajectory run straight through with the rates changed at the same step, and the
+    second request's TOF covers its own interval."""
+    reqs, progs = small_stream(n=40)
+    tmpl = next(r for r in reqs if r.model == "c2")
+    r2 = [x * 1.5 for x in tmpl.rates]
+    a = serving.Request(model="c2", size=(16, 16), rates=tmpl.rates, steps=1200, seed=9, traj_id=3, rid=1,
+                        session="s1")
+    b = serving.Request(model="c2", size=(16, 16), rates=r2, steps=1800, seed=9, traj_id=3, rid=2, session="s1",
+                        keep=False, arrival=0.0)
+    srv = serving.Server(arena_bytes=64 << 20, max_slots=16, quantum=500)
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    out = {r.rid: r for r in srv.serve([a, b])}
+    assert not srv.sessions  # keep=False ended the session
+    srv.close()
+    # the same trajectory straight through, rates changed after 1200 steps
+    pool = E.Pool(arena_bytes=64 << 20, max_slots=2)
+    mid = pool.add_model(progs["c2"])
+    s = pool.admit(mid, (16, 16), tmpl.rates, seed=9, rng=E.RNG_PHILOX, traj=3)
+    pool.run([s], 1200)
+    ps1, _ig1, t1, k1, _st = pool.results([s], progs["c2"].nproc)
+    pool.set_rates(s, r2)
+    pool.run([s], 1800)
+    ps, ig, t, k, st = pool.results([s], progs["c2"].nproc)
+    rb = out[2].result
+    assert rb["kmc_step"] == k[0] == 3000 and rb["kmc_time"] == t[0]
+    np.testing.assert_array_equal(rb["procstat"], ps[0])
+    np.testing.assert_array_equal(rb["integ_rates"], ig[0])
+    assert out[1].result["kmc_step"] == k1[0] == 1200
+    assert abs(rb["interval_time"] - (t[0] - t1[0])) <= 1e-12 * t[0]
+    pool.close()
+
+
+def test_idle_session_moves_to_host_memory_under_pressure():
+    """An idle session is saved to host memory when a new request needs its room, and
+    its next request continues it bit for bit."""
+    reqs, progs = small_stream(n=40)
+    tmpl = next(r for r in reqs if r.model == "c3")
+    probe = serving.Server(arena_bytes=1 << 20, max_slots=4)
+    for k, p in progs.items():
+        probe.add_model(k, p)
+    need = probe.pool.slot_bytes(probe.models["c3"].model_id, (24, 24))
+    probe.close()
+    srv = serving.Server(arena_bytes=need + 4096, max_slots=8, quantum=400)
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    first = serving.Request(model="c3", size=(24, 24), rates=tmpl.rates, steps=800, seed=5, traj_id=1, rid=1,
+                            session="x")
+    other = serving.Request(model="c3", size=(24, 24), rates=tmpl.rates, steps=300, seed=6, traj_id=2, rid=2,
+                            arrival=0.0)
+    srv.serve([first])
+    srv.serve([other])  # needs the whole arena: the idle session goes to host memory
+    assert srv.sessions["x"].slot < 0 and srv.sessions["x"].image is not None and srv.evicted >= 1
+    again = serving.Request(model="c3", size=(24, 24), rates=None, steps=700, seed=5, traj_id=1, rid=3,
+                            session="x", keep=False)
+    out = {r.rid: r for r in srv.serve([again])}
+    srv.close()
+    pool = E.Pool(arena_bytes=need + 4096, max_slots=2)
+    mid = pool.add_model(progs["c3"])
+    s = pool.admit(mid, (24, 24), tmpl.rates, seed=5, rng=E.RNG_PHILOX, traj=1)
+    pool.run([s], 800)
+    pool.run([s], 700)
+    ps, ig, t, k, st = pool.results([s], progs["c3"].nproc)
+    pool.close()
+    rr = out[3].result
+    assert rr["kmc_step"] == k[0] == 1500 and rr["kmc_time"] == t[0]
+    np.testing.assert_array_equal(rr["procstat"], ps[0])
+    np.testing.assert_array_equal(rr["integ_rates"], ig[0])
