@@ -22,6 +22,14 @@ moved to host memory when admission needs room.  A request with ``keep=False`` e
 session.  Results report the request's own interval (TOFs from the procstat and
 integ_rates differences over its kmc_time) beside the trajectory's totals.
 
+Sampled results: a request with ``samples > 0`` also gets get_std_sampled_data's
+averages (kmos/run/__init__.py:865-966) over its steps, split into ``samples`` batches:
+the server ends a quantum at each batch boundary and takes the sample on the device
+(``kmc_pool_sample``: occupation weighted by kmc_time_step), so no lattice is copied
+back; the request's result carries ``sampled`` = TOFs from procstat and from
+integ_rates over the sampled time, the mean occupation, total and simulated time and
+steps.  A sampling request is not evicted while it runs.
+
 Scheduling policy: "fifo" admits in arrival order.  "srpt" (shortest remaining
 processing time) admits the waiting request with the fewest remaining steps first and,
 when the arena or the slot table is full, evicts the resident trajectory with the most
@@ -70,6 +78,8 @@ class Request:
     session: Optional[str] = None   # requests of one session continue one trajectory
     keep: bool = True               # with a session: keep its trajectory after this request
     start: Optional[tuple] = None   # (procstat, integ_rates, kmc_time) when the request began
+    samples: int = 0                # > 0: get_std_sampled_data averages over this many batches
+    to_sample: int = 0              # steps left to the next sample boundary
 
 
 @dataclass
@@ -139,6 +149,9 @@ class Server:
         if req.rates is not None and len(req.rates) != self.models[req.model].nproc:
             raise ValueError("request %d: %d rates for %d processes" % (req.rid, len(req.rates),
                                                                        self.models[req.model].nproc))
+        if req.samples > 0:
+            # samples batches of int(steps / samples) steps, as do_steps(sample_size / samples)
+            req.steps = req.samples * int(req.steps / req.samples)
         req.remaining = int(req.steps)
         if req.session is not None:
             sess = self.sessions.get(req.session)
@@ -162,10 +175,11 @@ class Server:
 
     # ------------------------------------------------------------------ scheduling
     def _need(self, req: Request) -> int:
+        extra = 4096 if req.samples > 0 else 0  # the on-device sampling record
         sess = self.sessions.get(req.session) if req.session is not None else None
         if sess is not None and sess.slot >= 0:
-            return 0  # continues a resident trajectory
-        return self.pool.slot_bytes(self.models[req.model].model_id, req.size)
+            return extra  # continues a resident trajectory
+        return self.pool.slot_bytes(self.models[req.model].model_id, req.size) + extra
 
     def _resident(self) -> int:
         """Slots in use: running requests and resident session trajectories waiting for
@@ -192,7 +206,7 @@ class Server:
         if self.policy != "srpt" or not self.waiting or not self.active:
             return 0
         n = 0
-        victims = sorted(self.active.values(), key=lambda r: -r.remaining)
+        victims = sorted((r for r in self.active.values() if r.samples == 0), key=lambda r: -r.remaining)
         free = self.pool.free_bytes()[0]
         head = self.waiting.peek()
         need = self._need(head)
@@ -268,6 +282,7 @@ class Server:
             budget -= need
             batch.append(req)
         self._snapshot(started)
+        self._begin_sampling([r for r in started if r.samples > 0])
         if not batch:
             return restored
         try:
@@ -295,7 +310,15 @@ class Server:
             r.slot, r.admitted = s, t
             r.start = None  # a fresh trajectory starts from zero counters
             self.active[s] = r
+        self._begin_sampling([r for r, s in zip(batch, slots) if s is not None and r.samples > 0])
         return restored + len([s for s in slots if s is not None])
+
+    def _begin_sampling(self, reqs: List[Request]) -> None:
+        if not reqs:
+            return
+        self.pool.sample_begin([r.slot for r in reqs])
+        for r in reqs:
+            r.to_sample = max(1, int(r.steps / r.samples))  # do_steps(sample_size / samples)
 
     def _snapshot(self, reqs: List[Request]) -> None:
         """Counters and clock of continued trajectories when their request begins."""
@@ -319,6 +342,22 @@ class Server:
             slots = [r.slot for r in rs]
             ps, ig, times, steps, status = self.pool.results(slots, entry.nproc)
             occ = self.pool.occupation_counts(slots, entry.nspecies * entry.spuck)
+            sampled = {}
+            smp = [r for r in rs if r.samples > 0]
+            if smp:
+                out = self.pool.sample_end([r.slot for r in smp])
+                for j, r in enumerate(smp):
+                    cells = float(np.prod(r.size))
+                    dt = out["times"][j, 0]
+                    with np.errstate(divide="ignore", invalid="ignore"):
+                        tof = entry.tof_matrix @ (out["dprocstat"][j, :entry.nproc] / dt / cells)
+                        tofi = entry.tof_matrix @ (out["dinteg"][j, :entry.nproc] / dt / cells)
+                    sampled[id(r)] = {
+                        "tof": dict(zip(entry.tof_names, tof)), "tof_integ": dict(zip(entry.tof_names, tofi)),
+                        "occupation": out["occ"][j, :entry.nspecies * entry.spuck].reshape(entry.nspecies,
+                                                                                          entry.spuck),
+                        "total_time": float(dt), "simulated_time": float(out["times"][j, 1]),
+                        "kmc_steps": int(out["steps"][j])}
             for i, r in enumerate(rs):
                 cells = int(np.prod(r.size))
                 if status[i] not in (0, 3):
@@ -333,6 +372,8 @@ class Server:
                     "tof_integ": dict(zip(entry.tof_names, entry.tof_matrix @ (ig[i] - ig0) / tt / cells)),
                     "coverage": occ[i].reshape(entry.nspecies, entry.spuck) / cells,
                 }
+                if id(r) in sampled:
+                    r.result["sampled"] = sampled[id(r)]
                 r.done = t
                 del self.active[r.slot]
                 self.finished.append(r)
@@ -356,21 +397,34 @@ class Server:
         if not self.active:
             return
         slots = list(self.active)
-        steps = [min(self.active[s].remaining, self.quantum) for s in slots]
+        steps = []
+        for s in slots:
+            r = self.active[s]
+            n = min(r.remaining, self.quantum)
+            if r.samples > 0:
+                n = min(n, r.to_sample)  # end the quantum at the next sample boundary
+            steps.append(n)
         before = self.pool.results(slots, 1)[3]
         self.pool.run(slots, steps, sync=True)
         self.quanta += 1
         _ps, _ig, _t, after, statuses = self.pool.results(slots, 1)
-        done = []
+        done, sample_now = [], []
         for s, n, k0, k1, st in zip(slots, steps, before, after, statuses):
             r = self.active[s]
             self.kmc_steps += int(k1 - k0)
             r.remaining -= n
+            if r.samples > 0:
+                r.to_sample -= n
+                if r.to_sample <= 0:
+                    sample_now.append(s)
+                    r.to_sample = max(1, int(r.steps / r.samples))
             # a trajectory that found no process (absorbing state) ends early, as the
             # reference stops there
             if r.remaining <= 0 or st != 0:
                 r.remaining = 0
                 done.append(r)
+        if sample_now:
+            self.pool.sample(sample_now)
         self._retire(done)
 
     def serve(self, arrivals: Sequence[Request], until_empty: bool = True, deadline: float = float("inf")):

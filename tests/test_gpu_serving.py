@@ -173,3 +173,30 @@ def test_idle_session_moves_to_host_memory_under_pressure():
     assert rr["kmc_step"] == k[0] == 1500 and rr["kmc_time"] == t[0]
     np.testing.assert_array_equal(rr["procstat"], ps[0])
     np.testing.assert_array_equal(rr["integ_rates"], ig[0])
+
+
+def test_sampled_request_matches_pool_sampling():
+    """A request with samples > 0 returns get_std_sampled_data's averages, taken on the
+    device at the batch boundaries; they equal kmc_pool_sample_run on the same
+    trajectory alone."""
+    reqs, progs = small_stream(n=40)
+    tmpl = next(r for r in reqs if r.model == "c2")
+    req = serving.Request(model="c2", size=(16, 16), rates=tmpl.rates, steps=2003, seed=4, traj_id=7, rid=1,
+                          samples=4)
+    other = serving.Request(model="c3", size=(12, 12), rates=next(r for r in reqs if r.model == "c3").rates,
+                            steps=900, seed=4, traj_id=8, rid=2)
+    srv = serving.Server(arena_bytes=64 << 20, max_slots=16, quantum=170)  # quanta cross the boundaries
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    out = {r.rid: r for r in srv.serve([req, other])}
+    srv.close()
+    got = out[1].result["sampled"]
+    assert out[1].result["kmc_step"] == 4 * 500
+    pool = E.Pool(arena_bytes=64 << 20, max_slots=2)
+    mid = pool.add_model(progs["c2"])
+    s = pool.admit(mid, (16, 16), tmpl.rates, seed=4, rng=E.RNG_PHILOX, traj=7)
+    want = pool.sample_run([s], 4, 500)
+    pool.close()
+    nocc = want["occ"].shape[1]
+    np.testing.assert_array_equal(got["occupation"].ravel(), want["occ"][0, :nocc])
+    assert got["total_time"] == want["times"][0, 0] and got["kmc_steps"] == want["steps"][0] == 2000
