@@ -18,6 +18,10 @@
  *
  * Model programs are int32 arrays produced by kmos_gb300.program.compile_model; their
  * layout is documented there and checked here (magic 0x4B4D4331, version 1).
+ *
+ * Threads: different handles and pools are independent; one handle or pool is driven
+ * by one host thread at a time (kmc_pool_cancel excepted, which any thread may call
+ * while a run is in flight).
  */
 #ifndef KMC_GB300_H
 #define KMC_GB300_H

@@ -1240,6 +1240,31 @@ int run_rounds(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, i
   return KMC_OK;
 }
 
+// Every slot of a run list admitted, and none listed twice (two warps would step one
+// trajectory at once).
+int check_run_list(kmc_pool *p, const int32_t *slots, int n) {
+  std::vector<char> seen(p->slots.size(), 0);
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+    if (seen[slots[i]]) return fail(KMC_ERR_ARG, "slot listed twice in one run");
+    seen[slots[i]] = 1;
+  }
+  return KMC_OK;
+}
+
+void clear_graphs(kmc_pool *p) {
+  if (p->graphs.empty()) return;
+  cudaStreamSynchronize(p->stream);  // no captured launch may still be running
+  for (auto &kv : p->graphs) {
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    cudaFree(kv.second.d_list);
+    cudaFree(kv.second.d_steps);
+  }
+  p->graphs.clear();
+}
+
 int read_slot(kmc_pool *p, int slot, SlotDev *out) {
   CK(cudaStreamSynchronize(p->stream));
   CK(cudaMemcpy(out, p->d_slots + slot, sizeof(SlotDev), cudaMemcpyDeviceToHost));
@@ -1387,6 +1412,7 @@ int kmc_pool_admit_many(kmc_pool *p, int32_t n, const int32_t *model_ids, const 
   for (int i = 0; i < n; i++) {
     const int mid = model_ids[i];
     if (mid < 0 || mid >= (int)p->models.size()) return fail(KMC_ERR_ARG, "bad model id");
+    if (rate_offsets[i] < 0) return fail(KMC_ERR_ARG, "negative rate offset");
     nrates = std::max(nrates, (size_t)rate_offsets[i] + p->models[mid].dev.P);
   }
   int rc = KMC_OK;
@@ -1473,15 +1499,14 @@ int kmc_pool_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int32_
   if (!p || n < 0 || (n && (!slots || !steps))) return fail(KMC_ERR_ARG, "bad arguments");
   if (n == 0) return KMC_OK;
   if (n > (int)p->slots.size()) return fail(KMC_ERR_ARG, "too many slots");
-  for (int i = 0; i < n; i++) {
-    int rc = check_slot(p, slots[i]);
-    if (rc) return rc;
+  int rc = check_run_list(p, slots, n);
+  if (rc) return rc;
+  for (int i = 0; i < n; i++)
     if (steps[i] < 0) return fail(KMC_ERR_ARG, "negative step count");
-  }
   CK(cudaSetDevice(p->device));
   *p->h_cancel = 0;
   CK(cudaEventRecord(p->ev0, p->stream));
-  int rc = launch_run(p, slots, steps, n, p->d_list, p->d_steps, nullptr);
+  rc = launch_run(p, slots, steps, n, p->d_list, p->d_steps, nullptr);
   CK(cudaEventRecord(p->ev1, p->stream));
   p->timed = true;
   return rc;
@@ -1489,13 +1514,17 @@ int kmc_pool_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int32_
 
 int kmc_pool_run_graph(kmc_pool *p, const int32_t *slots, int64_t steps, int32_t n) {
   if (!p || n < 1 || !slots || steps < 0) return fail(KMC_ERR_ARG, "bad arguments");
-  for (int i = 0; i < n; i++) {
-    int rc = check_slot(p, slots[i]);
-    if (rc) return rc;
-  }
+  if (n > (int)p->slots.size()) return fail(KMC_ERR_ARG, "too many slots");
+  int rc0 = check_run_list(p, slots, n);
+  if (rc0) return rc0;
   CK(cudaSetDevice(p->device));
   GraphKey key{steps, std::vector<int32_t>(slots, slots + n)};
   auto it = p->graphs.find(key);
+  if (it == p->graphs.end() && p->graphs.size() >= 64) {
+    // bounded cache: drop every captured graph when a 65th run list arrives
+    CK(cudaStreamSynchronize(p->stream));
+    clear_graphs(p);
+  }
   if (it == p->graphs.end()) {
     GraphEntry e;
     CK(cudaMalloc(&e.d_list, sizeof(int32_t) * n));
@@ -1586,26 +1615,14 @@ int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per
   if (!p || warps_per_block < 0 || warps_per_block > 16 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
   p->warps_per_block = warps_per_block;
   p->blocks_per_sm = blocks_per_sm;
-  for (auto &kv : p->graphs) {
-    cudaGraphExecDestroy(kv.second.exec);
-    cudaGraphDestroy(kv.second.graph);
-    cudaFree(kv.second.d_list);
-    cudaFree(kv.second.d_steps);
-  }
-  p->graphs.clear();
+  clear_graphs(p);
   return KMC_OK;
 }
 
 int kmc_pool_set_fast_path(kmc_pool *p, int32_t enable) {
   if (!p) return fail(KMC_ERR_ARG, "bad pool");
   p->fast_path = enable ? 1 : 0;
-  for (auto &kv : p->graphs) {
-    cudaGraphExecDestroy(kv.second.exec);
-    cudaGraphDestroy(kv.second.graph);
-    cudaFree(kv.second.d_list);
-    cudaFree(kv.second.d_steps);
-  }
-  p->graphs.clear();
+  clear_graphs(p);
   return KMC_OK;
 }
 
@@ -1687,18 +1704,17 @@ int kmc_pool_occupation_counts(kmc_pool *p, const int32_t *slots, int32_t n, int
     int rc = check_slot(p, slots[i]);
     if (rc) return rc;
   }
-  int32_t *d_list = nullptr;
-  unsigned long long *d_out = nullptr;
-  CK(cudaMallocAsync(&d_list, sizeof(int32_t) * n, p->stream));
-  CK(cudaMallocAsync(&d_out, sizeof(unsigned long long) * (size_t)n * stride, p->stream));
+  AsyncScratch s_list(p->stream), s_out(p->stream);
+  CK(s_list.alloc(sizeof(int32_t) * n));
+  CK(s_out.alloc(sizeof(unsigned long long) * (size_t)n * stride));
+  int32_t *d_list = s_list.as<int32_t>();
+  unsigned long long *d_out = s_out.as<unsigned long long>();
   CK(cudaMemsetAsync(d_out, 0, sizeof(unsigned long long) * (size_t)n * stride, p->stream));
   CK(cudaMemcpyAsync(d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
   kmc_occupation_kernel<<<n, 256, 0, p->stream>>>(p->d_slots, p->d_models, d_list, n, stride, d_out);
   CK(cudaGetLastError());
   p->launches++;
   CK(cudaMemcpyAsync(out, d_out, sizeof(unsigned long long) * (size_t)n * stride, cudaMemcpyDeviceToHost, p->stream));
-  CK(cudaFreeAsync(d_list, p->stream));
-  CK(cudaFreeAsync(d_out, p->stream));
   CK(cudaStreamSynchronize(p->stream));
   return KMC_OK;
 }

@@ -68,6 +68,21 @@ struct Layout {
   size_t lat, as1, as2, rates, integ, accum, nsites, procstat, total;
 };
 
+// Stream-ordered device scratch, freed on its stream when it goes out of scope (on
+// error returns too).
+struct AsyncScratch {
+  void *ptr = nullptr;
+  cudaStream_t stream;
+  explicit AsyncScratch(cudaStream_t s) : stream(s) {}
+  AsyncScratch(const AsyncScratch &) = delete;
+  AsyncScratch &operator=(const AsyncScratch &) = delete;
+  cudaError_t alloc(size_t bytes) { return cudaMallocAsync(&ptr, bytes, stream); }
+  template <class T> T *as() const { return static_cast<T *>(ptr); }
+  ~AsyncScratch() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+  }
+};
+
 inline Layout slot_layout(int P, int V) {
   Layout L;
   size_t o = 0;

@@ -311,17 +311,16 @@ int fetch_state(kmc_pool *p, int slot, HostState &st) {
   h.nentries = off[P];
   st.entries.resize(off[P]);
   if (off[P] > 0) {
-    int64_t *d_off = nullptr;
-    int32_t *d_ent = nullptr;
-    CK(cudaMallocAsync(&d_off, sizeof(int64_t) * (P + 1), p->stream));
-    CK(cudaMallocAsync(&d_ent, sizeof(int32_t) * off[P], p->stream));
+    AsyncScratch s_off(p->stream), s_ent(p->stream);
+    CK(s_off.alloc(sizeof(int64_t) * (P + 1)));
+    CK(s_ent.alloc(sizeof(int32_t) * off[P]));
+    int64_t *d_off = s_off.as<int64_t>();
+    int32_t *d_ent = s_ent.as<int32_t>();
     CK(cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, p->stream));
     kmc_pack_tables_kernel<<<P, 256, 0, p->stream>>>(d.as1, V + 1, d_off, P, d_ent);
     CK(cudaGetLastError());
     p->launches++;
     CK(cudaMemcpyAsync(st.entries.data(), d_ent, sizeof(int32_t) * off[P], cudaMemcpyDeviceToHost, p->stream));
-    CK(cudaFreeAsync(d_off, p->stream));
-    CK(cudaFreeAsync(d_ent, p->stream));
     CK(cudaStreamSynchronize(p->stream));
   }
   h.bytes = image_layout(P, V, h.nentries).total;
@@ -348,18 +347,17 @@ int store_state(kmc_pool *p, int slot, const HostState &st) {
   CK(cudaMemcpyAsync(d.lat, st.lat.data(), V, cudaMemcpyHostToDevice, p->stream));
   std::vector<int64_t> off(P + 1, 0);
   for (int i = 0; i < P; i++) off[i + 1] = off[i] + st.nsites[i];
-  int64_t *d_off = nullptr;
-  int32_t *d_ent = nullptr;
+  AsyncScratch s_off(p->stream), s_ent(p->stream);
   if (off[P] > 0) {
-    CK(cudaMallocAsync(&d_off, sizeof(int64_t) * (P + 1), p->stream));
-    CK(cudaMallocAsync(&d_ent, sizeof(int32_t) * off[P], p->stream));
+    CK(s_off.alloc(sizeof(int64_t) * (P + 1)));
+    CK(s_ent.alloc(sizeof(int32_t) * off[P]));
+    int64_t *d_off = s_off.as<int64_t>();
+    int32_t *d_ent = s_ent.as<int32_t>();
     CK(cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, p->stream));
     CK(cudaMemcpyAsync(d_ent, st.entries.data(), sizeof(int32_t) * off[P], cudaMemcpyHostToDevice, p->stream));
     kmc_unpack_tables_kernel<<<P, 256, 0, p->stream>>>(d.as1, d.as2, V + 1, d_off, P, d_ent);
     CK(cudaGetLastError());
     p->launches++;
-    CK(cudaFreeAsync(d_off, p->stream));
-    CK(cudaFreeAsync(d_ent, p->stream));
   }
   d.layer = h.layer; d.status = h.status; d.rng_kind = h.rng_kind; d.accum_from = h.accum_from;
   d.seed = h.seed; d.traj = h.traj;
@@ -877,17 +875,16 @@ static int sample_launch(kmc_pool *p, const int32_t *slots, int32_t n, int mode,
     if (!sh.samp_bytes) return fail(KMC_ERR_ARG, "slot is not sampling (kmc_pool_sample_begin first)");
     recs[i] = reinterpret_cast<double *>(p->arena + sh.samp_off);
   }
-  int32_t *d_list = nullptr;
-  double **d_recs = nullptr;
-  CK(cudaMallocAsync(&d_list, sizeof(int32_t) * n, p->stream));
-  CK(cudaMallocAsync(&d_recs, sizeof(double *) * n, p->stream));
+  AsyncScratch s_list(p->stream), s_recs(p->stream);
+  CK(s_list.alloc(sizeof(int32_t) * n));
+  CK(s_recs.alloc(sizeof(double *) * n));
+  int32_t *d_list = s_list.as<int32_t>();
+  double **d_recs = s_recs.as<double *>();
   CK(cudaMemcpyAsync(d_list, slots, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
   CK(cudaMemcpyAsync(d_recs, recs.data(), sizeof(double *) * n, cudaMemcpyHostToDevice, p->stream));
   kmc_sample_kernel<<<n, 256, 0, p->stream>>>(p->d_slots, p->d_models, d_list, d_recs, n, mode, out);
   CK(cudaGetLastError());
   p->launches++;
-  CK(cudaFreeAsync(d_list, p->stream));
-  CK(cudaFreeAsync(d_recs, p->stream));
   return KMC_OK;
 }
 
@@ -945,8 +942,9 @@ static int sample_finish(kmc_pool *p, const int32_t *slots, int32_t n, int32_t o
                          int64_t *steps, int32_t *status) {
   const size_t nocc = (size_t)n * occ_stride, nps = (size_t)n * proc_stride;
   const size_t bytes = nocc * 8 + nps * 16 + (size_t)n * (16 + 8 + 4);
-  char *d = nullptr;
-  CK(cudaMallocAsync(&d, bytes, p->stream));
+  AsyncScratch s_out(p->stream);
+  CK(s_out.alloc(bytes));
+  char *d = s_out.as<char>();
   SampleOut out;
   out.occ_stride = occ_stride;
   out.proc_stride = proc_stride;
@@ -957,10 +955,9 @@ static int sample_finish(kmc_pool *p, const int32_t *slots, int32_t n, int32_t o
   out.steps = reinterpret_cast<int64_t *>(d + nocc * 8 + nps * 16 + (size_t)n * 16);
   out.status = reinterpret_cast<int32_t *>(d + nocc * 8 + nps * 16 + (size_t)n * 24);
   int rc = sample_launch(p, slots, n, SAMPLE_END, out);
-  if (rc) { cudaFreeAsync(d, p->stream); return rc; }
+  if (rc) return rc;
   std::vector<char> h(bytes);
   CK(cudaMemcpyAsync(h.data(), d, bytes, cudaMemcpyDeviceToHost, p->stream));
-  CK(cudaFreeAsync(d, p->stream));
   CK(cudaStreamSynchronize(p->stream));
   if (occ_mean) memcpy(occ_mean, h.data(), nocc * 8);
   if (procstat_delta) memcpy(procstat_delta, h.data() + nocc * 8, nps * 8);

@@ -202,3 +202,33 @@ def test_serial_and_fast_paths_agree(config):
         np.testing.assert_array_equal(ta[1], tb[1])
         np.testing.assert_array_equal(pa, pb)
         assert ca == cb
+
+
+def test_run_list_checks():
+    """A slot listed twice in one run, and negative rate offsets, are refused before any
+    launch."""
+    prog = PG.compile_model(fixture_model("ZGB_model"), "local_smart")
+    pool = E.Pool(arena_bytes=32 << 20, max_slots=4)
+    mid = pool.add_model(prog)
+    s = pool.admit(mid, (8, 8), [1.0] * prog.nproc, seed=1)
+    with pytest.raises(E.KMCError) as e:
+        pool.run([s, s], 10)
+    assert e.value.code == 1
+    with pytest.raises(E.KMCError) as e:
+        pool.run_graph([s, s], 10)
+    assert e.value.code == 1
+    import ctypes
+    L = E.load()
+    mids = np.array([mid], np.int32)
+    dims = np.array([8, 8, 1], np.int32)
+    seeds = np.array([1], np.int32)
+    rates = np.ones(prog.nproc)
+    offs = np.array([-1], np.int32)
+    out = np.zeros(1, np.int32)
+    P32, PD = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
+    rc = L.kmc_pool_admit_many(pool.h, 1, mids.ctypes.data_as(P32), dims.ctypes.data_as(P32), 0,
+                               seeds.ctypes.data_as(P32), E.RNG_PHILOX, None, rates.ctypes.data_as(PD),
+                               offs.ctypes.data_as(P32), out.ctypes.data_as(P32))
+    assert rc == 1
+    pool.run([s], 10)  # the pool still works
+    pool.close()
