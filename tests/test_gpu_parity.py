@@ -232,3 +232,27 @@ def test_run_list_checks():
     assert rc == 1
     pool.run([s], 10)  # the pool still works
     pool.close()
+
+
+def test_cancel_stops_a_running_batch():
+    """kmc_pool_cancel from the host ends a long persistent launch within a second (the
+    kernel polls the host-mapped flag every 1024 steps): the trajectories it was running
+    end with the cancelled status, and the pool keeps working for new trajectories."""
+    import time
+    wl = configs.build(2, n=64, steps=0)
+    pool = E.Pool(arena_bytes=256 << 20, max_slots=128)
+    mid = pool.add_model(wl.program)
+    slots = pool.admit_many([mid] * wl.n, wl.sizes, wl.rates, seeds=wl.seeds, rng=E.RNG_PHILOX, trajs=wl.trajs)
+    pool.run(slots, 10_000_000, sync=False)  # about a minute if nothing stops it
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    pool.cancel()
+    pool.sync()
+    assert time.perf_counter() - t0 < 2.0
+    _ps, _ig, _t, steps, status = pool.results(slots, 1)
+    assert (steps < 10_000_000).all()
+    assert set(status.tolist()) <= {3, 8} and (status == 8).any()
+    fresh = pool.admit(mid, (16, 16), wl.rates[0], seed=1)
+    pool.run([fresh], 2000)
+    assert pool.status(fresh) == 0 and pool.clock(fresh)[1] == 2000
+    pool.close()
