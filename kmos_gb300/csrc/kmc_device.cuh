@@ -29,6 +29,7 @@ struct ModelDev {
   int32_t len, backend, P, nspecies, null_species, spuck, ngroups;
   int32_t off_proc, off_touch, off_groups, off_site_layer, off_site_default, max_k;
   int32_t off_hot, hot_len, hot_grp, hot_tab, reach_x, reach_y, reach_z;
+  int32_t max_nedit;  // most edits of any fast stream (selects the 3- or 4-round kernel)
 };
 
 struct __align__(16) SlotDev {
@@ -358,22 +359,24 @@ __device__ inline void run_stream(View &v, int pos, int bx, int by, int bz) {
 namespace kmc {
 
 constexpr int FAST_SLOTS = 128;
-constexpr int FAST_EDITS = 96;
+constexpr int FAST_EDITS = 128;  // largest fast stream: 4 rounds of 32 edits
 constexpr int LOG_MAX = 16;   // lane-private write log entries (a multiple of 4)
 constexpr int TAIL_MAX = 6;   // prefetched list-tail entries per process
 constexpr int TAIL_PROCS = 64; // processes 0..63 get prefetched tails
-constexpr int FAST_ROUNDS = FAST_EDITS / 32;
 constexpr int FAST_MAXV = (1 << 23) - 1;
 
 enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
 
+// R rounds of 32 edits: the step kernel comes in R = 3 (streams of up to 96 edits, the
+// common case) and R = 4 (up to 128, large lateral-interaction groups).
+template <int R>
 struct FastSmem {
   int32_t latv[FAST_SLOTS];
   int32_t latsite[FAST_SLOTS];
-  int8_t ekind[FAST_EDITS];    // E_GDEL / E_DEL / E_ADD
-  int16_t ep[FAST_EDITS];      // process, 0-based
-  int32_t esite[FAST_EDITS];   // target site
-  int32_t em[FAST_EDITS];      // prefetched avail_sites(p, site, 2) of del edits
+  int8_t ekind[32 * R];    // E_GDEL / E_DEL / E_ADD
+  int16_t ep[32 * R];      // process, 0-based
+  int32_t esite[32 * R];   // target site
+  int32_t em[32 * R];      // prefetched avail_sites(p, site, 2) of del edits
   int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS
   uint4 lkey4[LOG_MAX / 4][32];  // lane-private write logs, four keys per 16 bytes (lane-minor)
   int32_t lval[LOG_MAX][32];

@@ -69,17 +69,17 @@ using namespace kmc_host;
 #endif
 constexpr int KMC_NPHASE = 16;
 
-template <int NP>
+template <int NP, int R>
 struct WarpSmem {
   double rates[NP * 32];
   double accum[NP * 32];
   double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
   int32_t ns[NP * 32];
-  uint32_t pmask[NP * 32][FAST_ROUNDS];  // edits of each process this step, one bit per edit
+  uint32_t pmask[NP * 32][R];  // edits of each process this step, one bit per edit
   int32_t ndel[NP * 32];                 // del edits of each process so far this step (0 between steps)
   long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
   long long tprev;
-  FastSmem f;
+  FastSmem<R> f;
 };
 
 // Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
@@ -87,17 +87,17 @@ struct WarpSmem {
 // warp-parallel while the edits were evaluated: em[k] = avail_sites(p, site_k, 2) for
 // every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
 // j < min(nd, TAIL_MAX), nd = its del edits.
-template <int NP>
-__device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_ROUNDS], int32_t *ndel,
+template <int NP, int R>
+__device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R], int32_t *ndel,
                               const View &v, int p, int rounds) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
   const int n0 = ns[p];
   const int lane = threadIdx.x & 31;
-  uint32_t bits[FAST_ROUNDS];
+  uint32_t bits[R];
 #pragma unroll
-  for (int r = 0; r < FAST_ROUNDS; r++) {
+  for (int r = 0; r < R; r++) {
     bits[r] = r < rounds ? pmask[p][r] : 0u;
     pmask[p][r] = 0u;
   }
@@ -136,7 +136,7 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
   };
   int n = n0;
 #pragma unroll
-  for (int r = 0; r < FAST_ROUNDS; r++) {
+  for (int r = 0; r < R; r++) {
     uint32_t b = bits[r];
     while (b) {
       const int k = 32 * r + __ffs(b) - 1;
@@ -178,10 +178,10 @@ __device__ int replay_process(FastSmem &f, int32_t *ns, uint32_t (*pmask)[FAST_R
 
 // One kMC step's run_proc_nr through the gather / evaluate / replay path.  All lanes
 // call it and get the status.
-template <int NP>
-__device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
+template <int NP, int R>
+__device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
                          int lane) {
-  FastSmem &f = sm.f;
+  FastSmem<R> &f = sm.f;
   const int nlat = fs[0], nchk = fs[1], nwr = fs[2], nedit = fs[3];
   const int32_t *coords = fs + 4;
   const int32_t *chk = coords + nlat;
@@ -215,10 +215,10 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   //    del edit's avail_sites(p, site, 2), and the list entry avail_sites(p, n0 - j, 1)
   //    its swap-remove can move, j = its rank among the process's dels this step.
   int ne = 0;
-  int32_t emv[FAST_ROUNDS], tv[FAST_ROUNDS];
-  int empos[FAST_ROUNDS], tslot[FAST_ROUNDS];
+  int32_t emv[R], tv[R];
+  int empos[R], tslot[R];
 #pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
+  for (int rr = 0; rr < R; rr++) {
     emv[rr] = 0;
     empos[rr] = -1;
     tv[rr] = 0;
@@ -296,7 +296,7 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   KMC_PHASE(sm, 5);
   // the loads issued during evaluation land now
 #pragma unroll
-  for (int rr = 0; rr < FAST_ROUNDS; rr++) {
+  for (int rr = 0; rr < R; rr++) {
     if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
     if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
   }
@@ -307,9 +307,9 @@ __device__ int fast_step(WarpSmem<NP> &sm, const Hot &H, View &v, const int32_t 
   for (int j = lane; j < v.P; j += 32) {
     uint32_t any = 0;
 #pragma unroll
-    for (int r = 0; r < FAST_ROUNDS; r++) any |= r < rounds ? sm.pmask[j][r] : 0u;
+    for (int r = 0; r < R; r++) any |= r < rounds ? sm.pmask[j][r] : 0u;
     if (any) {
-      const int e = replay_process<NP>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds);
+      const int e = replay_process<NP, R>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds);
       if (e) err = e;
     }
   }
@@ -339,7 +339,7 @@ struct RunArgs {
   unsigned long long *phase;      // KMC_NPHASE cycle sums (KMC_PHASE_TIMING builds)
 };
 
-template <int NP>
+template <int NP, int R>
 __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -356,8 +356,8 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
   H.tab = M.hot_tab;
   H.nspecies = M.nspecies;
   const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
-  WarpSmem<NP> &sm = reinterpret_cast<WarpSmem<NP> *>(smem_raw + hot_bytes)[wib];
-  for (int i = lane; i < NP * 32 * FAST_ROUNDS; i += 32) (&sm.pmask[0][0])[i] = 0u;
+  WarpSmem<NP, R> &sm = reinterpret_cast<WarpSmem<NP, R> *>(smem_raw + hot_bytes)[wib];
+  for (int i = lane; i < NP * 32 * R; i += 32) (&sm.pmask[0][0])[i] = 0u;
   for (int i = lane; i < NP * 32; i += 32) sm.ndel[i] = 0;
   for (int i = lane; i < KMC_NPHASE; i += 32) sm.ph[i] = 0;
   __syncthreads();
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
       }
       KMC_PHASE(sm, 3);
       if (fs_off) {
-        err = fast_step<NP>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
+        err = fast_step<NP, R>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
       } else {
         if (lane == 0) {
           v.minp = P;
@@ -958,6 +958,7 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
     if (!species_ok(prog[m->off_site_default + n])) return fail(KMC_ERR_PROGRAM, "bad default species");
   // hot section: fast streams with slot references below nlat, known edit kinds,
   // in-range processes / groups / species, edit offsets inside the stream
+  m->max_nedit = 0;
   m->off_hot = prog[21];
   m->hot_len = prog[20];
   m->hot_grp = prog[17];
@@ -996,6 +997,7 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
       if (nlat < 0 || nlat > FAST_SLOTS || nchk < 0 || nchk > nlat || nwr < 0 || nwr > nlat || nedit < 0 ||
           nedit > FAST_EDITS)
         return fail(KMC_ERR_PROGRAM, "fast stream exceeds the on-chip limits");
+      m->max_nedit = std::max(m->max_nedit, nedit);
       const int head = 4 + nlat + 2 * nchk + 2 * nwr + nedit;
       if (off + head > hl) return fail(KMC_ERR_PROGRAM, "fast stream overruns program");
       for (int c = 0; c < nlat; c++) if (!coord_ok(hot[off + 4 + c])) return fail(KMC_ERR_PROGRAM, "bad fast slot");
@@ -1063,31 +1065,32 @@ constexpr int STAGE_MAX_WORDS = 16384;  // hot sections up to 64 KB go to shared
 
 // One launch of the run kernel: every listed slot runs `model`.
 struct LaunchPlan {
-  int model, first, count, blocks, threads, np;
+  int model, first, count, blocks, threads, np, rounds;
   size_t smem;
   RunArgs a;
 };
 
-template <int NP>
+template <int NP, int R>
 int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   L.np = NP;
+  L.rounds = R;
   // The attribute is a per-function cap shared by every plan (and pool) on the device:
   // raise it to the device's limit once rather than to this plan's size, which would
   // lower it under a plan made before this one.
   cudaFuncAttributes fa;
-  CK(cudaFuncGetAttributes(&fa, kmc_run_kernel<NP>));
+  CK(cudaFuncGetAttributes(&fa, kmc_run_kernel<NP, R>));
   int optin = 0;
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
   const int cap = optin - (int)fa.sharedSizeBytes;
   if (fa.maxDynamicSharedSizeBytes < cap)
-    CK(cudaFuncSetAttribute(kmc_run_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    CK(cudaFuncSetAttribute(kmc_run_kernel<NP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
   if (p->warps_per_block > 0) {
     const int wpb = p->warps_per_block;
     L.threads = 32 * wpb;
-    L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
+    L.smem = hot_bytes + sizeof(WarpSmem<NP, R>) * wpb;
     if ((int64_t)L.smem > cap) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
     int bps = p->blocks_per_sm;
-    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP>, L.threads, L.smem));
+    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP, R>, L.threads, L.smem));
     if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
     L.blocks = std::max(1, std::min((L.count + wpb - 1) / wpb, p->num_sms * bps));
     return KMC_OK;
@@ -1097,14 +1100,14 @@ int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   // split evenly over the SMs
   const int regs = std::max(1, fa.numRegs);
   int maxw = std::min(16, 65536 / (regs * 32));
-  maxw = std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / (int64_t)sizeof(WarpSmem<NP>));
+  maxw = std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / (int64_t)sizeof(WarpSmem<NP, R>));
   if (maxw < 1) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
   const int blocks = std::max(1, std::min(p->num_sms, L.count));
   const int rounds = (L.count + blocks * maxw - 1) / (blocks * maxw);
   const int warps = (L.count + rounds - 1) / rounds;
   const int wpb = std::min(maxw, (warps + blocks - 1) / blocks);
   L.threads = 32 * wpb;
-  L.smem = hot_bytes + sizeof(WarpSmem<NP>) * wpb;
+  L.smem = hot_bytes + sizeof(WarpSmem<NP, R>) * wpb;
   L.blocks = blocks;
   return KMC_OK;
 }
@@ -1149,11 +1152,15 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
     a.stage_words = (md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
     a.phase = p->d_phase;
     const size_t hot_bytes = ((size_t)a.stage_words * 4 + 15) / 16 * 16;
+    // fast streams of more than 96 edits run in the 4-round kernel (built for up to 64
+    // processes); a larger model with such streams takes the serial interpreter
+    const bool big = md.max_nedit > 96;
+    if (big && md.P > 64) a.fast = 0;
     int rc;
-    if (md.P <= 32) rc = plan_kernel<1>(p, L, hot_bytes);
-    else if (md.P <= 64) rc = plan_kernel<2>(p, L, hot_bytes);
-    else if (md.P <= 128) rc = plan_kernel<4>(p, L, hot_bytes);
-    else rc = plan_kernel<8>(p, L, hot_bytes);
+    if (md.P <= 32) rc = big ? plan_kernel<1, 4>(p, L, hot_bytes) : plan_kernel<1, 3>(p, L, hot_bytes);
+    else if (md.P <= 64) rc = big ? plan_kernel<2, 4>(p, L, hot_bytes) : plan_kernel<2, 3>(p, L, hot_bytes);
+    else if (md.P <= 128) rc = plan_kernel<4, 3>(p, L, hot_bytes);
+    else rc = plan_kernel<8, 3>(p, L, hot_bytes);
     if (rc) return rc;
     plans.push_back(L);
     i = j;
@@ -1192,11 +1199,13 @@ int issue_run(kmc_pool *p, std::vector<LaunchPlan> &plans, const int32_t *d_list
       st = p->aux[i];
       CK(cudaStreamWaitEvent(st, p->fork_ev, 0));
     }
-    switch (L.np) {
-      case 1: kmc_run_kernel<1><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 2: kmc_run_kernel<2><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 4: kmc_run_kernel<4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      default: kmc_run_kernel<8><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+    switch (L.np * 10 + L.rounds) {
+      case 13: kmc_run_kernel<1, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 14: kmc_run_kernel<1, 4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 23: kmc_run_kernel<2, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 24: kmc_run_kernel<2, 4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      case 43: kmc_run_kernel<4, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
+      default: kmc_run_kernel<8, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
     }
     CK(cudaGetLastError());
     p->launches++;

@@ -115,7 +115,7 @@ OP_STRIP = 6
 
 HEADER_WORDS = 24
 FAST_MAX_SLOTS = 128
-FAST_MAX_EDITS = 96
+FAST_MAX_EDITS = 128
 NLI_TABLE_MAX = 4096
 
 

@@ -20,7 +20,9 @@ CASES = [("AB_model", "local_smart", (20, 20)), ("ZGB_model", "local_smart", (16
          ("pairwise_interaction", "local_smart", (8, 8)), ("default_xml", "local_smart", (10, 10)),
          ("pdopd_xml", "local_smart", (8, 8)), ("pdopd_xml", "lat_int", (8, 8)),
          # lattices narrower than 2*reach+1: every step takes the serial interpreter
-         ("pairwise_interaction", "lat_int", (5, 5)), ("ZGB_model", "local_smart", (3, 3))]
+         ("pairwise_interaction", "lat_int", (5, 5)), ("ZGB_model", "local_smart", (3, 3)),
+         # streams of more than 96 edits: the 4-round fast path
+         ("CO_oxidation_Ruo2", "lat_int", (14, 14)), ("default_xml", "lat_int", (14, 14))]
 
 
 def random_rates(P, seed):
