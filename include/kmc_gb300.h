@@ -210,6 +210,10 @@ KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t
 /* 1 (default): steps whose process has a fast stream run through the gather /
  * replay / scatter path; 0: every step runs the serial interpreter (same results). */
 KMC_API int kmc_pool_set_fast_path(kmc_pool *pool, int32_t enable);
+/* Table placement: 1 (default) copies each model's hot section (fast streams, group
+ * records, nli tables; up to 64 KB) into every block's shared memory, 0 reads it from
+ * global memory through L1 (more shared memory left for warps). */
+KMC_API int kmc_pool_set_table_placement(kmc_pool *pool, int32_t shared);
 /* Device time (ms, CUDA events on the pool stream) of the last kmc_pool_run launch. */
 KMC_API int kmc_pool_last_kernel_ms(kmc_pool *pool, float *ms);
 /* CUDA events on the pool stream around a region of work: start, then stop waits for

@@ -1149,7 +1149,7 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
     a.cancel = p->d_cancel;
     a.fast = p->fast_path;
     a.model = model;
-    a.stage_words = (md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
+    a.stage_words = (p->stage_hot && md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
     a.phase = p->d_phase;
     const size_t hot_bytes = ((size_t)a.stage_words * 4 + 15) / 16 * 16;
     // fast streams of more than 96 edits run in the 4-round kernel (built for up to 64
@@ -1624,6 +1624,13 @@ int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per
   if (!p || warps_per_block < 0 || warps_per_block > 16 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
   p->warps_per_block = warps_per_block;
   p->blocks_per_sm = blocks_per_sm;
+  clear_graphs(p);
+  return KMC_OK;
+}
+
+int kmc_pool_set_table_placement(kmc_pool *p, int32_t shared) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  p->stage_hot = shared ? 1 : 0;
   clear_graphs(p);
   return KMC_OK;
 }

@@ -130,6 +130,7 @@ struct kmc_pool {
   int64_t launches = 0;
   int warps_per_block = 4;
   int fast_path = 1;
+  int stage_hot = 1;  // 1: a model's hot section goes to shared memory when it fits
   int blocks_per_sm = 0;  // 0 = occupancy maximum
   std::unordered_map<kmc_host::GraphKey, kmc_host::GraphEntry, kmc_host::GraphKeyHash> graphs;
   std::mutex mu;

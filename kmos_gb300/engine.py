@@ -89,6 +89,7 @@ SIGNATURES = {
     "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
     "kmc_pool_set_fast_path": (_i32, [_vp, _i32]),
+    "kmc_pool_set_table_placement": (_i32, [_vp, _i32]),
     "kmc_pool_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_pool_timer_start": (_i32, [_vp]),
     "kmc_pool_timer_stop": (_i32, [_vp, _P(ctypes.c_float)]),
@@ -436,6 +437,11 @@ class Pool:
 
     def set_fast_path(self, enable: bool):
         _check(load().kmc_pool_set_fast_path(self.h, 1 if enable else 0))
+
+    def set_table_placement(self, shared: bool):
+        """Hot section (fast streams, nli tables) in shared memory (True) or read from
+        global memory (False)."""
+        _check(load().kmc_pool_set_table_placement(self.h, 1 if shared else 0))
 
     def last_kernel_ms(self) -> float:
         ms = ctypes.c_float()
