@@ -466,6 +466,31 @@ oracle_t *oracle_create(const int32_t *prog, int prog_len, int X, int Y, int Z, 
     return o;
 }
 
+/* The tables of a given lattice from scratch: every table emptied, then the touch-up of
+ * every site (of every site type; lat_int: of every cell) as initialize_state runs them
+ * (proclist_generic_subroutines.mpy:236-304).  A touch-up lists exactly the processes
+ * whose conditions hold at its site, so the entries are the processes the lattice enables
+ * -- in touch-up order, which need not be the order an incremental run reaches.  Used by
+ * the tests as a size-independent invariant of long runs. */
+int oracle_rebuild_tables(oracle_t *o, const int32_t *lattice)
+{
+    for (int i = 0; i < o->V; i++) o->lattice[i] = lattice[i];
+    memset(o->avail_sites, 0, sizeof(int32_t) * (size_t)o->P * o->V * 2);
+    memset(o->nr_of_sites, 0, sizeof(int32_t) * o->P);
+    o->err = 0;
+    for (int k = 0; k < o->Z; k++)
+        for (int j = 0; j < o->Y; j++)
+            for (int i = 0; i < o->X; i++) {
+                if (o->backend == 1) {
+                    run_stream(o, o->prog[o->off_touch], i, j, k);
+                } else {
+                    for (int nr = 1; nr <= o->spuck; nr++) run_stream(o, o->prog[o->off_touch + nr - 1], i, j, k);
+                }
+                if (o->err) return o->err;
+            }
+    return o->err;
+}
+
 void oracle_set_rate_const(oracle_t *o, int proc, double rate) { o->rates[proc - 1] = rate; }
 void oracle_update_accum_rate(oracle_t *o) { update_accum_rate(o); }
 void oracle_update_integ_rate(oracle_t *o) { update_integ_rate(o); }

@@ -74,6 +74,7 @@ def lib():
         L.oracle_get_occupation.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dbl)]
         L.oracle_philox.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
         L.oracle_draws.argtypes = [vp, i64, ctypes.POINTER(dbl)]
+        L.oracle_rebuild_tables.argtypes = [vp, P32]
         _lib = L
     return _lib
 
@@ -197,6 +198,13 @@ class Oracle:
                             ig.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         return dict(lattice=lat, as1=as1.reshape(P, V + 1), as2=as2.reshape(P, V + 1), nsites=ns,
                     procstat=ps, integ=ig)
+
+    def rebuild_tables(self, lattice):
+        """Sets the lattice and derives every table from it by touch-ups
+        (oracle_rebuild_tables); returns export()."""
+        lat = np.ascontiguousarray(lattice, dtype=np.int32)
+        self._check(lib().oracle_rebuild_tables(self.h, _p32(lat)))
+        return self.export()
 
     def occupation(self, nspecies_out=None):
         ns = self.nspecies if nspecies_out is None else nspecies_out
