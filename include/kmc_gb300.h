@@ -64,6 +64,12 @@ typedef struct kmc_pool kmc_pool;
 KMC_API const char *kmc_last_error(void);
 /* Library version string. */
 KMC_API const char *kmc_version(void);
+/* Checks a model program (kmos_gb300.program.compile_model's words) the way
+ * kmc_create and kmc_pool_add_model do before anything reaches the device: header,
+ * op streams, fast streams (slot references, table indices inside their tables,
+ * 16-byte placement), group records and nli tables.  KMC_OK or KMC_ERR_PROGRAM with
+ * kmc_last_error() naming the fault.  Needs no GPU. */
+KMC_API int kmc_check_program(const int32_t *program, int32_t program_len);
 
 /* ------------------------------------------------------------------------------
  * One trajectory (plain drop-in)

@@ -367,6 +367,12 @@ constexpr int FAST_MAXV = (1 << 23) - 1;
 
 enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
 
+// Start of a fast stream's edit quads (stream-relative words): after the head, rounded
+// up to 16 bytes.
+__host__ __device__ inline int fast_rec_offset(int nlat, int nchk, int nwr) {
+  return (4 + nlat + 2 * nchk + 2 * nwr + 3) & ~3;
+}
+
 // R rounds of 32 edits: the step kernel comes in R = 3 (streams of up to 96 edits, the
 // common case) and R = 4 (up to 128, large lateral-interaction groups).
 template <int R>

@@ -163,10 +163,10 @@ __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R],
         else if (nlog == 0 || !logged(0, n, last))
           last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
         put(0, m, last);
-        put(0, n, 0);
+        a1[n] = 0;  // vacated top entry: read again only after an add (logged) refills it
         put(1, last, m);
       } else {
-        put(0, m, 0);
+        a1[m] = 0;  // the same, m being the top
       }
       put(1, site, 0);
       n -= 1;
@@ -182,11 +182,13 @@ template <int NP, int R>
 __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
                          int lane) {
   FastSmem<R> &f = sm.f;
-  const int nlat = fs[0], nchk = fs[1], nwr = fs[2], nedit = fs[3];
+  const int nlat = fs[0], nchk = fs[1], nwr = fs[2];
+  const int nedit = fs[3] & 0xFFFF, nq = (int)((uint32_t)fs[3] >> 16);
   const int32_t *coords = fs + 4;
   const int32_t *chk = coords + nlat;
   const int32_t *wr = chk + 2 * nchk;
-  const int32_t *eoff = wr + 2 * nwr;
+  // edit k's quads, nedit quads apart: [h, target slot, x, 0], then packed references
+  const int4 *quad = reinterpret_cast<const int4 *>(fs + fast_rec_offset(nlat, nchk, nwr));
   const unsigned lt = (1u << lane) - 1u;
   // 1. gather every slot (all lattice loads in flight together); check the old species
   //    of first replaces
@@ -226,37 +228,40 @@ __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32
     if (32 * rr >= nedit) continue;
     const int k = 32 * rr + lane;
     bool on = false;
-    int kind = E_GDEL, p = 0, site = 0;
+    int kind = E_GDEL, p = 0, site = 0, tgt = 0;
     if (k < nedit) {
-      const int32_t *e = fs + eoff[k];
-      const uint32_t h = (uint32_t)e[0];
+      // all of the edit's quads in flight together; the table index is the base plus
+      // code(slot) * mul over every packed reference (unused ones are 0: slot 0 times 0)
+      const int4 q0 = quad[k];
+      int4 q1 = make_int4(0, 0, 0, 0), q2 = q1, q3 = q1;
+      if (nq >= 1) q1 = quad[nedit + k];
+      if (nq >= 2) q2 = quad[2 * nedit + k];
+      if (nq >= 3) q3 = quad[3 * nedit + k];
+      const uint32_t h = (uint32_t)q0.x;
       const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-      if (op >= 6) {  // nli through its table: index_base + sum(code(slot) * mul)
-        int idx = e[2];
-        if (cnt > 0 && cnt <= 8) {
-          // eight independent reads, clamped to the record, so they issue together
-          const int cm = cnt - 1;
-          int sl[8], mu[8];
-#pragma unroll
-          for (int c = 0; c < 8; c++) {
-            sl[c] = e[3 + min(c, cm)];
-            mu[c] = e[3 + cnt + min(c, cm)];
-          }
-#pragma unroll
-          for (int c = 0; c < 8; c++) idx += c < cnt ? species_code(f.latv[sl[c]], H.nspecies) * mu[c] : 0;
-        } else {
-          for (int c = 0; c < cnt; c++) idx += species_code(f.latv[e[3 + c]], H.nspecies) * e[3 + cnt + c];
-        }
+      tgt = q0.y;
+      if (op >= 6) {
+        const int ns = H.nspecies;
+        auto tref = [&](int32_t w) { return species_code(f.latv[w & 0xFF], ns) * (w >> 8); };
+        int idx = q0.z + ((tref(q1.x) + tref(q1.y)) + (tref(q1.z) + tref(q1.w)));
+        if (nq >= 2) idx += (tref(q2.x) + tref(q2.y)) + (tref(q2.z) + tref(q2.w));
+        if (nq >= 3) idx += (tref(q3.x) + tref(q3.y)) + (tref(q3.z) + tref(q3.w));
         p = H.h[idx];
         on = p != 0;
         kind = op == 6 ? E_DEL : E_ADD;
       } else if (op == 2) {
         on = true; p = arg;
       } else if (op == 3) {
-        on = true;
-        for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], f.latv), e[2 + cnt + c]);
+        if (cnt <= 1) {  // the condition is in the quad: [h, target, slot, mask]
+          on = cnt == 0 || in_mask(f.latv[q0.z], q0.w);
+        } else {
+          const int32_t *e = fs + q0.z;  // [h, target, ref * cnt, mask * cnt]
+          on = true;
+          for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], f.latv), e[2 + cnt + c]);
+        }
         p = arg; kind = E_ADD;
       } else {
+        const int32_t *e = fs + q0.z;  // [h, target, 0, record offset, ref * cnt]
         p = nli_refs(H, cnt, e[2], e[3], e + 4, f.latv);
         on = p != 0;
         kind = op == 4 ? E_DEL : E_ADD;
@@ -264,7 +269,7 @@ __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32
     }
     KMC_PHASE(sm, 12);
     if (on) {
-      site = f.latsite[fs[eoff[k] + 1]];
+      site = f.latsite[tgt];
       if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
     }
     KMC_PHASE(sm, 13);
@@ -989,46 +994,63 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
           if (hot[toff + i] < 0 || hot[toff + i] > m->P) return fail(KMC_ERR_PROGRAM, "bad nli table entry");
       }
     }
+    if (m->off_hot % 4) return fail(KMC_ERR_PROGRAM, "hot section not on 16 bytes");
     for (int i = 0; i < m->P; i++) {
       const int off = hot[i];
       if (off == 0) continue;
-      if (off < m->P + 1 || off + 4 > hl) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
-      const int nlat = hot[off], nchk = hot[off + 1], nwr = hot[off + 2], nedit = hot[off + 3];
+      if (off < m->P + 1 || off + 4 > hl || off % 4) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
+      const int nlat = hot[off], nchk = hot[off + 1], nwr = hot[off + 2];
+      const int nedit = hot[off + 3] & 0xFFFF, nq = (int)((uint32_t)hot[off + 3] >> 16);
       if (nlat < 0 || nlat > FAST_SLOTS || nchk < 0 || nchk > nlat || nwr < 0 || nwr > nlat || nedit < 0 ||
-          nedit > FAST_EDITS)
+          nedit > FAST_EDITS || nq > 3)
         return fail(KMC_ERR_PROGRAM, "fast stream exceeds the on-chip limits");
       m->max_nedit = std::max(m->max_nedit, nedit);
-      const int head = 4 + nlat + 2 * nchk + 2 * nwr + nedit;
+      const int rec = fast_rec_offset(nlat, nchk, nwr);
+      const int64_t head = (int64_t)rec + 4 * (1 + nq) * (int64_t)nedit;
       if (off + head > hl) return fail(KMC_ERR_PROGRAM, "fast stream overruns program");
       for (int c = 0; c < nlat; c++) if (!coord_ok(hot[off + 4 + c])) return fail(KMC_ERR_PROGRAM, "bad fast slot");
-      const int32_t *chk = hot + off + 4 + nlat, *wr = chk + 2 * nchk, *eo = wr + 2 * nwr;
+      const int32_t *chk = hot + off + 4 + nlat, *wr = chk + 2 * nchk;
       for (int c = 0; c < nchk; c++) if (chk[2 * c] < 0 || chk[2 * c] >= nlat) return fail(KMC_ERR_PROGRAM, "bad check");
       for (int c = 0; c < nwr; c++)
         if (wr[2 * c] < 0 || wr[2 * c] >= nlat || !species_ok(wr[2 * c + 1])) return fail(KMC_ERR_PROGRAM, "bad write");
       auto ref_ok = [&](int32_t r) { return r >= 0 ? r < nlat : species_ok(-r - 2); };
+      const int32_t *q = hot + off + rec;  // quad j of edit k at q + 4 * (j * nedit + k)
       for (int k = 0; k < nedit; k++) {
-        const int e = off + eo[k];
-        if (eo[k] < head || e + 2 > hl) return fail(KMC_ERR_PROGRAM, "bad edit offset");
-        const uint32_t h = (uint32_t)hot[e];
+        const int32_t *q0 = q + 4 * k;
+        const uint32_t h = (uint32_t)q0[0];
         const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-        if (hot[e + 1] < 0 || hot[e + 1] >= nlat) return fail(KMC_ERR_PROGRAM, "bad edit target");
+        if (q0[1] < 0 || q0[1] >= nlat) return fail(KMC_ERR_PROGRAM, "bad edit target");
         if (op == 6 || op == 7) {
-          // every index the table form can produce lies inside the group's table
-          if (arg >= m->ngroups || e + 3 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad nli table edit");
+          // every index the table form can produce lies inside the group's table: all
+          // 4 * nq packed references are summed, unused ones must be 0
+          if (arg >= m->ngroups || cnt > 4 * nq) return fail(KMC_ERR_PROGRAM, "bad nli table edit");
           const int toff = hot[m->hot_tab + arg];
           const int K = hot[hot[m->hot_grp + arg] + 1];
           int64_t size = 1;
-          for (int k = 0; k < K; k++) size *= (m->nspecies + 1);
-          int64_t lo = hot[e + 2], hi = hot[e + 2];
-          for (int c = 0; c < cnt; c++) {
-            if (hot[e + 3 + c] < 0 || hot[e + 3 + c] >= nlat || hot[e + 3 + cnt + c] < 0)
-              return fail(KMC_ERR_PROGRAM, "bad nli table edit");
-            hi += (int64_t)m->nspecies * hot[e + 3 + cnt + c];
+          for (int kk = 0; kk < K; kk++) size *= (m->nspecies + 1);
+          int64_t lo = q0[2], hi = q0[2];
+          for (int c = 0; c < 4 * nq; c++) {
+            const int32_t w = q[4 * ((1 + c / 4) * nedit + k) + c % 4];
+            if (c >= cnt ? w != 0 : (w < 0 || (w & 0xFF) >= nlat)) return fail(KMC_ERR_PROGRAM, "bad nli table edit");
+            hi += (int64_t)m->nspecies * (w >> 8);
           }
           if (toff <= 0 || lo < toff || hi >= toff + size) return fail(KMC_ERR_PROGRAM, "nli table edit outside its table");
-        } else if (op == 2) {
+          continue;
+        }
+        if (op == 2) {
           if (arg < 1 || arg > m->P) return fail(KMC_ERR_PROGRAM, "bad edit process");
-        } else if (op == 3) {
+          continue;
+        }
+        if (op == 3 && cnt <= 1) {  // inline condition
+          if (arg < 1 || arg > m->P || q0[2] < 0 || q0[2] >= nlat || (cnt == 0 && (q0[2] | q0[3])))
+            return fail(KMC_ERR_PROGRAM, "bad add edit");
+          continue;
+        }
+        // ops 3, 4, 5 keep their whole record in the stream's variable part
+        const int64_t e = (int64_t)off + q0[2];
+        if (q0[2] < head || e + 2 > hl || hot[e] != q0[0] || hot[e + 1] != q0[1])
+          return fail(KMC_ERR_PROGRAM, "bad edit offset");
+        if (op == 3) {
           if (arg < 1 || arg > m->P || e + 2 + 2 * cnt > hl) return fail(KMC_ERR_PROGRAM, "bad add edit");
           for (int c = 0; c < cnt; c++) if (!ref_ok(hot[e + 2 + c])) return fail(KMC_ERR_PROGRAM, "bad add ref");
         } else if (op == 4 || op == 5) {
@@ -1308,6 +1330,11 @@ extern "C" {
 
 const char *kmc_last_error(void) { return g_err.c_str(); }
 const char *kmc_version(void) { return "kmc_gb300 1.0 (sm_103a)"; }
+
+int kmc_check_program(const int32_t *program, int32_t program_len) {
+  ModelDev md{};
+  return validate_program(program, program_len, &md);
+}
 
 int kmc_pool_create(int32_t device, size_t arena_bytes, int32_t max_slots, kmc_pool **out) {
   if (!out || max_slots < 1) return fail(KMC_ERR_ARG, "bad arguments");

@@ -37,6 +37,7 @@ _p32, _p64, _pd, _pu32 = _P(_i32), _P(_i64), _P(_dbl), _P(_u32)
 SIGNATURES = {
     "kmc_last_error": (ctypes.c_char_p, []),
     "kmc_version": (ctypes.c_char_p, []),
+    "kmc_check_program": (_i32, [_p32, _i32]),
     "kmc_create": (_i32, [_p32, _i32, _p32, _i32, _i32, _i32, _u32, _P(_vp)]),
     "kmc_destroy": (_i32, [_vp]),
     "kmc_set_rate_const": (_i32, [_vp, _i32, _dbl]),
@@ -327,6 +328,13 @@ class Trajectory:
     def load_reload(self, path: str):
         """Second pass of base.reload_system into this trajectory."""
         _check(load().kmc_load_reload(self.h, os.fsencode(path)))
+
+
+def check_program(program) -> None:
+    """Raises KMCError (KMC_ERR_PROGRAM) unless the engine accepts the model program
+    (``kmc_check_program``; no GPU needed).  ``program``: a Program or its int32 words."""
+    words = np.ascontiguousarray(getattr(program, "words", program), dtype=np.int32)
+    _check(load().kmc_check_program(_ptr(words, _i32), len(words)))
 
 
 def reload_info(path: str):

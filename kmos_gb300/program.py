@@ -65,23 +65,30 @@ slot sees is known here: conditions on replaced slots are decided at compile tim
 add that can never fire is dropped), and every remaining read is of the value the slot
 had before the step.  All edits of a step can therefore be evaluated in parallel::
 
-    [nlat, nchk, nwr, nedit, coord * nlat, (slot, old_mask) * nchk,
-     (slot, species) * nwr, edit_offset * nedit, edits...]
-    edit  [kind | cnt << 8 | arg << 16, target slot, ref * cnt, (mask * cnt for adds)]
-          nli edits through a member scan: [h, target slot, 0, record offset, ref * cnt]
-          with the hot-relative offset of the group's member record;
-          nli edits through a table: [h, target slot, index base, slot * cnt, mul * cnt]:
-          the table entry is index_base + sum(code(slot_c) * mul_c), the constant
-          references and the table's own offset folded into index_base
-    kind  2 = guarded del (arg = proc), 3 = add (arg = proc, cnt conditions),
-          4 = nli del, 5 = nli add (member scan; arg = group, cnt = the group's K),
-          6 = nli del, 7 = nli add (table; arg = group, cnt = its non-constant refs)
+    [nlat, nchk, nwr, nedit | nq << 16, coord * nlat, (slot, old_mask) * nchk,
+     (slot, species) * nwr, 0 * (pad to 4 words), quad 0 * nedit, ..., quad nq * nedit,
+     variable parts...]
+    quad 0 of edit k  [kind | cnt << 8 | arg << 16, target slot, x, 0]
+    quad q >= 1       packed table references 4q-4 .. 4q-1 of edit k (slot | mul << 8)
+    kind  2 = guarded del (arg = proc; x = 0)
+          3 = add (arg = proc, cnt conditions): with at most one condition the quad
+              holds it, [h, target slot, slot, mask] ([h, target slot, 0, 0] for none);
+              else x = offset of its variable part [h, target slot, ref * cnt, mask * cnt]
+          4 = nli del, 5 = nli add through a member scan (arg = group, cnt = the group's
+              K; x = offset of [h, target slot, 0, record offset, ref * cnt], the record
+              offset hot-relative)
+          6 = nli del, 7 = nli add through a table (arg = group, cnt = its non-constant
+              references; x = index base): the table entry is x + sum(code(slot_c) *
+              mul_c) over the packed references, the constant references and the
+              table's own offset folded into x; unused references are 0 (slot 0 times 0)
     ref   >= 0: slot index (value before the step); < 0: constant species -ref-2
     Every edit's target coordinate is a slot, so its site is gathered with the others.
+    Edit k's quads lie nedit quads apart (lane k of a warp reads edit k: consecutive
+    16-byte loads), and the stream, its quads and the hot section start on 16 bytes.
 
 ``chk`` are the old-species checks of first replaces (later ones are checked here),
-``wr`` the final species of every replaced slot.  Edit offsets are relative to the
-stream start.  The hot section (header word 21) holds the fast-stream offset table,
+``wr`` the final species of every replaced slot.  Offsets of variable parts are
+relative to the stream start.  The hot section (header word 21) holds the fast-stream offset table,
 the streams, the group records and the nli tables with offsets relative to its own
 start, so a block can copy it to shared memory in one piece.  Header word 19 is the
 largest |offset| any fast stream reaches per axis: a lattice at least 2*reach+1 cells
@@ -598,17 +605,38 @@ class ProgramBuilder:
         for c in coords:
             reach = [max(reach[i], abs(c[i])) for i in range(3)]
         wr = sorted(static.items())
-        head = [len(coords), len(chk), len(wr), len(edits)] + [pack_coord(*c) for c in coords]
+        nedit = len(edits)
+        # quads of packed table references: enough for the widest table edit
+        nq = max([(e[0] >> 8 & 0xFF) for e in edits if (e[0] & 0xFF) >= 6] + [0])
+        nq = (nq + 3) // 4
+        if nq > 3:
+            return None
+        head = [len(coords), len(chk), len(wr), nedit | (nq << 16)] + [pack_coord(*c) for c in coords]
         for sl, mk in chk:
             head += [sl, mk]
         for sl, sp in wr:
             head += [sl, sp]
-        offs, body = [], []
-        base = len(head) + len(edits)
-        for e in edits:
-            offs.append(base + len(body))
-            body += e
-        return head + offs + body, reach
+        head += [0] * (-len(head) % 4)
+        quads = [[0] * (4 * nedit) for _ in range(1 + nq)]
+        body: List = []
+        body_at = len(head) + 4 * (1 + nq) * nedit
+        for k, e in enumerate(edits):
+            op, cnt = e[0] & 0xFF, e[0] >> 8 & 0xFF
+            if op >= 6:
+                x = e[2]
+                for c in range(cnt):
+                    quads[1 + c // 4][4 * k + c % 4] = e[3 + c] | (e[3 + cnt + c] << 8)
+            elif op == 2:
+                x = 0
+            elif op == 3 and (cnt == 0 or (cnt == 1 and e[2] >= 0)):
+                x, w = (e[2], e[3]) if cnt else (0, 0)  # the one condition, inline
+                quads[0][4 * k:4 * k + 4] = [e[0], e[1], x, w]
+                continue
+            else:
+                x = body_at + len(body)
+                body += e
+            quads[0][4 * k:4 * k + 4] = [e[0], e[1], x, 0]
+        return head + [w for q in quads for w in q] + body, reach
 
     def build(self) -> "Program":
         m = self.model
@@ -663,6 +691,7 @@ class ProgramBuilder:
                 w.emit(proc, *masks)
         # hot section: fast-stream offsets, fast streams, group records, nli tables;
         # offsets inside it are relative to its start
+        w.emit(*([0] * (-len(w.words) % 4)))  # the hot section starts on 16 bytes
         off_hot = len(w.words)
         hot: List[int] = [0] * (P + 1)
         reach = [0, 0, 0]
@@ -674,6 +703,7 @@ class ProgramBuilder:
                 continue
             words, rch = fast
             reach = [max(a, b) for a, b in zip(reach, rch)]
+            hot.extend([0] * (-len(hot) % 4))  # streams start on 16 bytes
             hot[p] = len(hot)
             hot.extend(words)
         hot[P] = len(hot)

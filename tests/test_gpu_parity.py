@@ -87,6 +87,45 @@ def test_trace_matches_oracle(name, backend, size, rng):
         np.testing.assert_allclose(g.accum_rates(), o.accum_rates(), rtol=0, atol=0)
 
 
+@pytest.mark.parametrize("name,backend,size", [CASES[i] for i in (1, 3, 4, 5, 9)])
+def test_rates_over_thirty_decades(name, backend, size):
+    """Rate constants 10^U(-25, 6): many accum terms fall below half an ulp of the
+    running sum (their adds change nothing, in the reference's order as here);
+    accum_rates stay the oracle's bit for bit, and so do the steps."""
+    prog = PG.compile_model(fixture_model(name), backend)
+    rates = (10.0 ** np.random.default_rng(23).uniform(-25, 6, size=prog.nproc)).tolist()
+    with E.Trajectory(prog, size, seed=29, rng=E.RNG_PHILOX, traj=1) as g:
+        o = O.Oracle(prog, size, seed=29, rng=O.RNG_PHILOX, traj=1)
+        for x in (g, o):
+            x.set_rates(rates)
+            x.update_accum_rate()
+        for chunk in (1, 700, 3000):
+            np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+            np.testing.assert_array_equal(g.accum_rates(), o.accum_rates())
+        assert_same_state(g, o, prog.nproc, o.V)
+
+
+@pytest.mark.parametrize("T", [300.0, 600.0])
+def test_lateral_interaction_at_one_temperature(T):
+    """The config-3 model (CO, lat_int) at one temperature.  At 300 K the lattice fills
+    with CO (every lateral-interaction edit of a step fires, the desorption terms are
+    ~1e-16 per site); at 600 K it is sparse."""
+    wl = configs.build(3, n=2, steps=0, sides=[16, 32])
+    kT = configs.K_B_EV * T
+    rates = [1e3] + [1e13 * np.exp(-(1.3 + 0.1 * bin(m).count("1")) / kT) for m in range(16)]
+    rates = [float(r) for r in rates + [1e13 * np.exp(-0.6 / kT)] * 4]
+    for i in range(wl.n):
+        with E.Trajectory(wl.program, wl.sizes[i], seed=wl.seeds[i], rng=E.RNG_PHILOX, traj=wl.trajs[i]) as g:
+            o = O.Oracle(wl.program, wl.sizes[i], seed=wl.seeds[i], rng=O.RNG_PHILOX, traj=wl.trajs[i])
+            for x in (g, o):
+                x.set_rates(rates)
+                x.update_accum_rate()
+            for chunk in (2000, 6000):
+                np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+                np.testing.assert_array_equal(g.accum_rates(), o.accum_rates())
+            assert_same_state(g, o, wl.program.nproc, o.V)
+
+
 @pytest.mark.parametrize("config", [1, 2, 3, 4])
 def test_benchmark_configs_match_oracle(config):
     wl = configs.build(config, n=3, steps=5000, sides=[16, 32])
