@@ -22,3 +22,20 @@ def golden_dir():
 def fixture_model(name):
     from kmos_gb300 import model as M
     return M.load_json(os.path.join(GOLDEN, "models", name + ".json"))
+
+
+def trimer_model():
+    """A square-lattice model with three-site adsorption (A3 in x and in y), desorption
+    and a hop: its local_smart adds carry two conditions, and its lat_int groups have
+    three coordinates, edit forms the fixture models do not reach."""
+    from kmos_gb300 import configs
+    from kmos_gb300.model import Process
+    c = configs._c
+    procs = [Process("A_desorption", "1", [c("A", "a")], [c("empty", "a")])]
+    for i, d in enumerate([(1, 0, 0), (0, 1, 0)]):
+        d2 = (2 * d[0], 2 * d[1], 0)
+        procs.append(Process("A3_adsorption%d" % i, "1", [c("empty", "a"), c("empty", "a", d), c("empty", "a", d2)],
+                             [c("A", "a"), c("A", "a", d), c("A", "a", d2)]))
+    procs.append(Process("A_hop", "1", [c("A", "a"), c("empty", "a", (1, 0, 0))],
+                         [c("empty", "a"), c("A", "a", (1, 0, 0))]))
+    return configs._square_model("trimer", ["empty", "A"], procs)

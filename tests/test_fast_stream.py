@@ -14,7 +14,7 @@ and the engine's program check, on the CPU.
 import numpy as np
 import pytest
 
-from conftest import fixture_model
+from conftest import fixture_model, trimer_model
 from kmos_gb300 import configs, engine as E, program as PG
 
 MODELS = ["AB_model", "CO_oxidation_Ruo2", "ZGB_model", "default_xml", "pairwise_interaction", "pdopd_xml"]
@@ -69,7 +69,7 @@ def by_scan(off, q0, latv, hot):
 def compiled(name, backend, tables=True, monkeypatch=None):
     if not tables:
         monkeypatch.setattr(PG, "NLI_TABLE_MAX", 0)
-    prog = PG.compile_model(fixture_model(name), backend)
+    prog = PG.compile_model(trimer_model() if name == "trimer" else fixture_model(name), backend)
     if not tables:
         monkeypatch.undo()
     return prog
@@ -86,13 +86,19 @@ def test_programs_pass_the_engine_check(name, backend):
         assert off % 4 == 0
 
 
+@pytest.mark.parametrize("backend", ["local_smart", "lat_int"])
+def test_trimer_programs_pass_the_engine_check(backend, monkeypatch):
+    E.check_program(compiled("trimer", backend))
+    E.check_program(compiled("trimer", backend, tables=False, monkeypatch=monkeypatch))
+
+
 @pytest.mark.parametrize("config", [1, 2, 3, 4])
 def test_benchmark_programs_pass_the_engine_check(config):
     E.check_program(configs.build(config, n=1, steps=0).program)
 
 
 @pytest.mark.parametrize("name", ["CO_oxidation_Ruo2", "ZGB_model", "pairwise_interaction", "pdopd_xml",
-                                  "default_xml"])
+                                  "default_xml", "trimer"])
 def test_table_edits_equal_member_scans(name, monkeypatch):
     a = compiled(name, "lat_int")
     b = compiled(name, "lat_int", tables=False, monkeypatch=monkeypatch)

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, fixture_model
+from conftest import GOLDEN, fixture_model, trimer_model
 from kmos_gb300 import configs, engine as E, program as PG
 from oracle import oracle as O
 
@@ -103,6 +103,33 @@ def test_rates_over_thirty_decades(name, backend, size):
             np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
             np.testing.assert_array_equal(g.accum_rates(), o.accum_rates())
         assert_same_state(g, o, prog.nproc, o.V)
+
+
+@pytest.mark.parametrize("which,backend,tables", [("trimer", "local_smart", True), ("trimer", "lat_int", True),
+                                                  ("trimer", "lat_int", False),
+                                                  ("pairwise_interaction", "lat_int", False),
+                                                  ("CO_oxidation_Ruo2", "lat_int", False)])
+def test_wide_conditions_and_member_scans(which, backend, tables, monkeypatch):
+    """Edit forms of the fast step the fixture models alone do not reach: adds with two
+    conditions (three-site processes, local_smart) and nli edits through member scans
+    of the group record (models compiled without nli tables)."""
+    if not tables:
+        monkeypatch.setattr(PG, "NLI_TABLE_MAX", 0)
+    m = trimer_model() if which == "trimer" else fixture_model(which)
+    prog = PG.compile_model(m, backend)
+    monkeypatch.undo()
+    P = prog.nproc
+    size = (14, 14) if which != "CO_oxidation_Ruo2" else (12, 12)
+    for traj in range(2):
+        rates = (10.0 ** np.random.default_rng(40 + traj).uniform(-1, 2, size=P)).tolist()
+        with E.Trajectory(prog, size, seed=31, rng=E.RNG_PHILOX, traj=traj) as g:
+            o = O.Oracle(prog, size, seed=31, rng=O.RNG_PHILOX, traj=traj)
+            for x in (g, o):
+                x.set_rates(rates)
+                x.update_accum_rate()
+            for chunk in (1, 999, 4000):
+                np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+            assert_same_state(g, o, P, o.V)
 
 
 @pytest.mark.parametrize("T", [300.0, 600.0])
