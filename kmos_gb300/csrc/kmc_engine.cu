@@ -86,10 +86,12 @@ struct WarpSmem {
 // returns a status.  Clears pmask[p] and ndel[p].  The loads it needs were issued
 // warp-parallel while the edits were evaluated: em[k] = avail_sites(p, site_k, 2) for
 // every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
-// j < min(nd, TAIL_MAX), nd = its del edits.
+// j < min(nd, TAIL_MAX), nd = its del edits.  In a dels-first stream (every del before
+// every add, no (process, site) named by two dels or by two adds) only the moves of
+// the dels are read back, so the cleared position entries and the adds are not logged.
 template <int NP, int R>
 __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R], int32_t *ndel,
-                              const View &v, int p, int rounds) {
+                              const View &v, int p, int rounds, bool dels_first) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
@@ -145,6 +147,11 @@ __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R],
       if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
         if (n + 1 >= v.stride) return ST_TABLE;  // full list: tables out of step with the lattice
         n += 1;
+        if (dels_first) {  // no del of this process follows, so nothing reads these back
+          a1[n] = site;
+          a2[site] = n;
+          continue;
+        }
         put(0, n, site);
         put(1, site, n);
         continue;
@@ -168,7 +175,8 @@ __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R],
       } else {
         a1[m] = 0;  // the same, m being the top
       }
-      put(1, site, 0);
+      if (dels_first) a2[site] = 0;  // no later del of this process names this site
+      else put(1, site, 0);
       n -= 1;
     }
   }
@@ -183,7 +191,9 @@ __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32
                          int lane) {
   FastSmem<R> &f = sm.f;
   const int nlat = fs[0], nchk = fs[1], nwr = fs[2];
-  const int nedit = fs[3] & 0xFFFF, nq = (int)((uint32_t)fs[3] >> 16);
+  const uint32_t w3 = (uint32_t)fs[3];
+  const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF;
+  const bool dels_first = (w3 >> 20) & 1;
   const int32_t *coords = fs + 4;
   const int32_t *chk = coords + nlat;
   const int32_t *wr = chk + 2 * nchk;
@@ -314,7 +324,7 @@ __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32
 #pragma unroll
     for (int r = 0; r < R; r++) any |= r < rounds ? sm.pmask[j][r] : 0u;
     if (any) {
-      const int e = replay_process<NP, R>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds);
+      const int e = replay_process<NP, R>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds, dels_first);
       if (e) err = e;
     }
   }
@@ -1000,9 +1010,10 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
       if (off == 0) continue;
       if (off < m->P + 1 || off + 4 > hl || off % 4) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
       const int nlat = hot[off], nchk = hot[off + 1], nwr = hot[off + 2];
-      const int nedit = hot[off + 3] & 0xFFFF, nq = (int)((uint32_t)hot[off + 3] >> 16);
+      const uint32_t w3 = (uint32_t)hot[off + 3];
+      const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF, dels_first = (w3 >> 20) & 0xF;
       if (nlat < 0 || nlat > FAST_SLOTS || nchk < 0 || nchk > nlat || nwr < 0 || nwr > nlat || nedit < 0 ||
-          nedit > FAST_EDITS || nq > 3)
+          nedit > FAST_EDITS || nq > 3 || dels_first > 1 || (w3 >> 24))
         return fail(KMC_ERR_PROGRAM, "fast stream exceeds the on-chip limits");
       m->max_nedit = std::max(m->max_nedit, nedit);
       const int rec = fast_rec_offset(nlat, nchk, nwr);
@@ -1015,6 +1026,29 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
         if (wr[2 * c] < 0 || wr[2 * c] >= nlat || !species_ok(wr[2 * c + 1])) return fail(KMC_ERR_PROGRAM, "bad write");
       auto ref_ok = [&](int32_t r) { return r >= 0 ? r < nlat : species_ok(-r - 2); };
       const int32_t *q = hot + off + rec;  // quad j of edit k at q + 4 * (j * nedit + k)
+      if (dels_first) {
+        // the flag promises every del-kind edit before every add-kind edit, and adds that
+        // cannot name one (process, site) twice: distinct (proc or group, target) and
+        // not both the plain and the nli form
+        bool seen_add = false, plain[2] = {false, false}, nli[2] = {false, false};
+        for (int k = 0; k < nedit; k++) {
+          const int32_t *a = q + 4 * k;
+          const int op = a[0] & 0xFF;
+          const bool add = op == 3 || op == 5 || op == 7;
+          if (add) seen_add = true;
+          else if (seen_add) return fail(KMC_ERR_PROGRAM, "fast stream marked dels-first has a del after an add");
+          ((op == 2 || op == 3) ? plain : nli)[add] = true;
+          for (int k2 = 0; k2 < k; k2++) {
+            const int32_t *b = q + 4 * k2;
+            const int op2 = b[0] & 0xFF;
+            if ((op2 == 3 || op2 == 5 || op2 == 7) == add && ((uint32_t)b[0] >> 16) == ((uint32_t)a[0] >> 16) &&
+                b[1] == a[1])
+              return fail(KMC_ERR_PROGRAM, "fast stream marked dels-first names one target twice");
+          }
+        }
+        if ((plain[0] && nli[0]) || (plain[1] && nli[1]))
+          return fail(KMC_ERR_PROGRAM, "fast stream marked dels-first mixes edit forms");
+      }
       for (int k = 0; k < nedit; k++) {
         const int32_t *q0 = q + 4 * k;
         const uint32_t h = (uint32_t)q0[0];

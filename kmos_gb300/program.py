@@ -65,7 +65,7 @@ slot sees is known here: conditions on replaced slots are decided at compile tim
 add that can never fire is dropped), and every remaining read is of the value the slot
 had before the step.  All edits of a step can therefore be evaluated in parallel::
 
-    [nlat, nchk, nwr, nedit | nq << 16, coord * nlat, (slot, old_mask) * nchk,
+    [nlat, nchk, nwr, nedit | nq << 16 | dels_first << 20, coord * nlat, (slot, old_mask) * nchk,
      (slot, species) * nwr, 0 * (pad to 4 words), quad 0 * nedit, ..., quad nq * nedit,
      variable parts...]
     quad 0 of edit k  [kind | cnt << 8 | arg << 16, target slot, x, 0]
@@ -85,6 +85,11 @@ had before the step.  All edits of a step can therefore be evaluated in parallel
     Every edit's target coordinate is a slot, so its site is gathered with the others.
     Edit k's quads lie nedit quads apart (lane k of a warp reads edit k: consecutive
     16-byte loads), and the stream, its quads and the hot section start on 16 bytes.
+    dels_first = 1: every del-kind edit (2, 4, 6) comes before every add-kind edit (3, 5,
+    7), and no two adds, nor two dels, can name the same (process, site) (distinct
+    (proc, target) for kinds 2 and 3, distinct (group, target) for kinds 4-7, not both
+    forms among the adds or among the dels): true of every lat_int stream.  The engine's
+    replay then reads back only what the dels move, and logs nothing else.
 
 ``chk`` are the old-species checks of first replaces (later ones are checked here),
 ``wr`` the final species of every replaced slot.  Offsets of variable parts are
@@ -611,7 +616,20 @@ class ProgramBuilder:
         nq = (nq + 3) // 4
         if nq > 3:
             return None
-        head = [len(coords), len(chk), len(wr), nedit | (nq << 16)] + [pack_coord(*c) for c in coords]
+        # every del-kind edit before every add-kind edit (lat_int streams: the del list,
+        # the writes, the add list): the engine then appends the adds after the dels
+        kinds = [e[0] & 0xFF for e in edits]
+        dels = [i for i, op in enumerate(kinds) if op in (2, 4, 6)]
+        adds = [i for i, op in enumerate(kinds) if op in (3, 5, 7)]
+        # and no two adds, nor two dels, can name one (process, site): the appends then
+        # commute, and no del reads the position entry another del cleared
+        add_keys = [(kinds[i] == 3, edits[i][0] >> 16, edits[i][1]) for i in adds]
+        del_keys = [(kinds[i] == 2, edits[i][0] >> 16, edits[i][1]) for i in dels]
+        distinct = (len(set(add_keys)) == len(add_keys) and len({k[0] for k in add_keys}) <= 1 and
+                    len(set(del_keys)) == len(del_keys) and len({k[0] for k in del_keys}) <= 1)
+        dels_first = int(distinct and (not dels or not adds or max(dels) < min(adds)))
+        head = [len(coords), len(chk), len(wr), nedit | (nq << 16) | (dels_first << 20)]
+        head += [pack_coord(*c) for c in coords]
         for sl, mk in chk:
             head += [sl, mk]
         for sl, sp in wr:

@@ -31,7 +31,7 @@ def streams(words):
         if off == 0:
             continue
         nlat, nchk, nwr, x = hot[off:off + 4]
-        nedit, nq = x & 0xFFFF, x >> 16
+        nedit, nq = x & 0xFFFF, (x >> 16) & 0xF
         rec = off + ((4 + nlat + 2 * nchk + 2 * nwr + 3) & ~3)
         edits = []
         for k in range(nedit):
@@ -190,3 +190,35 @@ def test_inline_add_conditions():
             with pytest.raises(E.KMCError):
                 E.check_program(w)
     assert found > 0
+
+
+def test_dels_first_streams():
+    """Streams whose del-kind edits all precede their add-kind edits, with no two adds
+    and no two dels naming one (process, site), carry the dels-first flag (every lat_int stream does; the
+    engine appends their adds in parallel after the dels); setting it on any other
+    stream is refused."""
+    for name in ("ZGB_model", "CO_oxidation_Ruo2", "pairwise_interaction"):
+        lat = PG.compile_model(fixture_model(name), "lat_int")
+        w = [int(x) for x in lat.words]
+        hot = w[w[21]:w[21] + w[20]]
+        assert all((hot[hot[p] + 3] >> 20) & 1 for p in range(w[3]) if hot[p])
+    prog = PG.compile_model(fixture_model("ZGB_model"), "local_smart")
+    w0 = np.array(prog.words, dtype=np.int32)
+    off_hot = int(w0[21])
+    refused = 0
+    for p, off, nlat, edits, hot in streams(w0):
+        flag = (hot[off + 3] >> 20) & 1
+        kinds = [q0[0] & 0xFF for q0, _ in edits]
+        dels = [i for i, k in enumerate(kinds) if k in (2, 4, 6)]
+        adds = [i for i, k in enumerate(kinds) if k in (3, 5, 7)]
+        keys = [(edits[i][0][0] >> 16, edits[i][0][1]) for i in adds]
+        dkeys = [(edits[i][0][0] >> 16, edits[i][0][1]) for i in dels]
+        ordered = not dels or not adds or max(dels) < min(adds)
+        assert flag == int(ordered and len(set(keys)) == len(keys) and len(set(dkeys)) == len(dkeys))
+        if not flag:
+            w = w0.copy()
+            w[off_hot + off + 3] |= 1 << 20
+            with pytest.raises(E.KMCError):
+                E.check_program(w)
+            refused += 1
+    assert refused > 0
