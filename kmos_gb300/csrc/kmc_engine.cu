@@ -926,7 +926,16 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
   if (m->spuck < 1 || m->spuck > 32) return fail(KMC_ERR_PROGRAM, "sites per unit cell must be in 1..32");
   if (m->nspecies < 1 || m->nspecies > 30) return fail(KMC_ERR_PROGRAM, "species count must be in 1..30");
   if (m->backend != 0 && m->backend != 1) return fail(KMC_ERR_PROGRAM, "unknown backend");
+  if (m->ngroups < 0 || m->ngroups > len) return fail(KMC_ERR_PROGRAM, "bad group count");
   const int nt = m->backend == 1 ? 1 : m->spuck;
+  // [start, start + count) inside [0, limit), in 64-bit so that no offset can wrap
+  auto span_ok = [](int64_t start, int64_t count, int64_t limit) {
+    return start >= 0 && count >= 0 && start + count <= limit;
+  };
+  if (!span_ok(m->off_proc, m->P + 1, len) || !span_ok(m->off_touch, nt + 1, len) ||
+      !span_ok(m->off_groups, m->ngroups, len) || !span_ok(m->off_site_layer, m->spuck, len) ||
+      !span_ok(m->off_site_default, m->spuck, len))
+    return fail(KMC_ERR_PROGRAM, "program section outside the program");
   for (int i = 0; i <= m->P; i++)
     if (prog[m->off_proc + i] <= 0 || prog[m->off_proc + i] > len) return fail(KMC_ERR_PROGRAM, "bad op offset");
   for (int i = 0; i <= nt; i++)
@@ -979,18 +988,19 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
   m->hot_grp = prog[17];
   m->hot_tab = prog[18];
   m->reach_x = prog[19] & 0xFF; m->reach_y = (prog[19] >> 8) & 0xFF; m->reach_z = (prog[19] >> 16) & 0xFF;
-  if (m->off_hot <= 0 || m->hot_len <= m->P || m->off_hot + m->hot_len > len) {
+  if (m->off_hot <= 0 || m->hot_len <= m->P || !span_ok(m->off_hot, m->hot_len, len)) {
     m->off_hot = 0;
   } else {
     const int32_t *hot = prog + m->off_hot;
     const int hl = m->hot_len, G = std::max(m->ngroups, 1);
-    if (m->hot_grp < m->P + 1 || m->hot_grp + G > hl || m->hot_tab < m->P + 1 || m->hot_tab + G > hl)
+    if (m->hot_grp < m->P + 1 || !span_ok(m->hot_grp, G, hl) || m->hot_tab < m->P + 1 || !span_ok(m->hot_tab, G, hl))
       return fail(KMC_ERR_PROGRAM, "bad hot-section tables");
     for (int g = 0; g < m->ngroups; g++) {
       const int off = hot[m->hot_grp + g];
-      if (off <= 0 || off + 2 > hl) return fail(KMC_ERR_PROGRAM, "bad hot group record");
+      if (off <= 0 || !span_ok(off, 2, hl)) return fail(KMC_ERR_PROGRAM, "bad hot group record");
       const int M = hot[off], K = hot[off + 1];
-      if (K > KMC_MAXK || K < 0 || M < 0 || off + 2 + K + M * (1 + K) > hl) return fail(KMC_ERR_PROGRAM, "bad hot group record");
+      if (K > KMC_MAXK || K < 0 || M < 0 || !span_ok(off, 2 + K + (int64_t)M * (1 + K), hl))
+        return fail(KMC_ERR_PROGRAM, "bad hot group record");
       for (int mm = 0; mm < M; mm++) {
         const int pid = hot[off + 2 + K + mm * (1 + K)];
         if (pid < 1 || pid > m->P) return fail(KMC_ERR_PROGRAM, "bad group member");
@@ -999,7 +1009,7 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
       if (toff) {
         int64_t size = 1;
         for (int k = 0; k < K; k++) size *= (m->nspecies + 1);
-        if (toff < 0 || toff + size > hl) return fail(KMC_ERR_PROGRAM, "nli table overruns program");
+        if (!span_ok(toff, size, hl)) return fail(KMC_ERR_PROGRAM, "nli table overruns program");
         for (int64_t i = 0; i < size; i++)
           if (hot[toff + i] < 0 || hot[toff + i] > m->P) return fail(KMC_ERR_PROGRAM, "bad nli table entry");
       }
@@ -1008,7 +1018,7 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
     for (int i = 0; i < m->P; i++) {
       const int off = hot[i];
       if (off == 0) continue;
-      if (off < m->P + 1 || off + 4 > hl || off % 4) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
+      if (off < m->P + 1 || !span_ok(off, 4, hl) || off % 4) return fail(KMC_ERR_PROGRAM, "bad fast stream offset");
       const int nlat = hot[off], nchk = hot[off + 1], nwr = hot[off + 2];
       const uint32_t w3 = (uint32_t)hot[off + 3];
       const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF, dels_first = (w3 >> 20) & 0xF;
@@ -1101,10 +1111,11 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
   m->max_k = 0;
   for (int g = 0; g < m->ngroups; g++) {
     const int off = prog[m->off_groups + g];
-    if (off <= 0 || off + 2 > len) return fail(KMC_ERR_PROGRAM, "bad group offset");
+    if (off <= 0 || !span_ok(off, 2, len)) return fail(KMC_ERR_PROGRAM, "bad group offset");
     const int M = prog[off], K = prog[off + 1];
     if (K > KMC_MAXK) return fail(KMC_ERR_PROGRAM, "lateral-interaction group tests more than 16 sites");
-    if (off + 2 + K + M * (1 + K) > len) return fail(KMC_ERR_PROGRAM, "group record overruns program");
+    if (K < 0 || M < 0 || !span_ok(off, 2 + K + (int64_t)M * (1 + K), len))
+      return fail(KMC_ERR_PROGRAM, "group record overruns program");
     for (int k = 0; k < K; k++)
       if (!coord_ok(prog[off + 2 + k])) return fail(KMC_ERR_PROGRAM, "bad group coordinate");
     for (int mm = 0; mm < M; mm++) {
