@@ -345,14 +345,15 @@ __device__ inline void run_stream(View &v, int pos, int bx, int by, int bz) {
 // coordinate it reads or writes as a slot; every condition reads a slot's value from
 // before the step or a constant, so the edits of one step are evaluated in parallel:
 //   1. lanes load every slot's species and check the old species of the replaces;
-//   2. lanes evaluate the edits (guarded dels, adds, nli dels / adds), and a ballot
-//      compacts the ones that happen into a list in program order;
+//   2. lanes evaluate the edits (guarded dels, adds, nli dels / adds; one edit per lane,
+//      its record read as 16-byte quads), issue the loads the dels will need
+//      (avail_sites(p, site, 2) and the top entries of avail_sites(p, :, 1)), and a
+//      ballot compacts the edits that happen into a list in program order;
 //   3. edits of different processes touch different rows of avail_sites, so each lane
 //      takes one process and replays that process's edits in program order with the
-//      reference's add_proc / del_proc arithmetic: it first issues all the loads its
-//      dels need (avail_sites(p, site, 2) and the top entries of avail_sites(p, :, 1)),
-//      then applies the edits, writing through to memory and remembering its writes
-//      in a small lane-private log so later reads of the same entries stay on chip;
+//      reference's add_proc / del_proc arithmetic, writing through to memory and
+//      remembering the writes later reads need in a small lane-private log (in a
+//      dels-first stream only the entries its dels move);
 //   4. lanes write the final species of the replaced slots.
 // The edits and their order within each process are those of the serial interpreter;
 // edits of different processes commute.

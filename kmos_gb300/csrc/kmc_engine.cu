@@ -981,7 +981,8 @@ int validate_program(const int32_t *prog, int32_t len, ModelDev *m) {
   for (int n = 0; n < m->spuck; n++)
     if (!species_ok(prog[m->off_site_default + n])) return fail(KMC_ERR_PROGRAM, "bad default species");
   // hot section: fast streams with slot references below nlat, known edit kinds,
-  // in-range processes / groups / species, edit offsets inside the stream
+  // in-range processes / groups / species, table indices inside their tables, record
+  // offsets inside the stream, 16-byte placement
   m->max_nedit = 0;
   m->off_hot = prog[21];
   m->hot_len = prog[20];
