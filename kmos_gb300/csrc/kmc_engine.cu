@@ -1169,6 +1169,14 @@ int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
   const int regs = std::max(1, fa.numRegs);
   int maxw = std::min(16, 65536 / (regs * 32));
   maxw = std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / (int64_t)sizeof(WarpSmem<NP, R>));
+  // the occupancy calculator has the last word (register allocation granularity)
+  while (maxw >= 1) {
+    int nb = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kmc_run_kernel<NP, R>, 32 * maxw,
+                                                     hot_bytes + sizeof(WarpSmem<NP, R>) * maxw));
+    if (nb >= 1) break;
+    maxw--;
+  }
   if (maxw < 1) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
   const int blocks = std::max(1, std::min(p->num_sms, L.count));
   const int rounds = (L.count + blocks * maxw - 1) / (blocks * maxw);
