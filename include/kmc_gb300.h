@@ -253,6 +253,12 @@ KMC_API int kmc_pool_save_state(kmc_pool *pool, int32_t slot, void *buf, size_t 
  * hash); the image is validated (sizes, species, every table index) before it reaches
  * the device.  The new slot id goes to *slot. */
 KMC_API int kmc_pool_restore_state(kmc_pool *pool, int32_t model_id, const void *buf, size_t bytes, int32_t *slot);
+/* Checks a state image against a model program without a device: the checks
+ * kmc_pool_restore_state / kmc_load_state make before anything reaches the GPU (magic,
+ * sizes, program hash, species, every avail_sites entry in 1..volume and listed once per
+ * process).  KMC_OK, KMC_ERR_PROGRAM (bad program), KMC_ERR_ARG or KMC_ERR_TABLE (bad
+ * image). */
+KMC_API int kmc_check_image(const int32_t *program, int32_t program_len, const void *buf, size_t bytes);
 /* The same on a handle; kmc_load_state needs an image of the handle's model and size. */
 KMC_API int kmc_save_state(kmc_handle *h, void *buf, size_t capacity, size_t *bytes);
 KMC_API int kmc_load_state(kmc_handle *h, const void *buf, size_t bytes);

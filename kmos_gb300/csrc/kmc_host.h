@@ -164,4 +164,6 @@ int read_slot(kmc_pool *p, int slot, SlotDev *out);
 int run_rounds(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, int rounds,
                const std::function<int(int)> &after);
 int check_slot(kmc_pool *p, int slot);
+// Checks a model program (header, op streams, fast streams, groups, tables) and fills m.
+int validate_program(const int32_t *prog, int32_t len, ModelDev *m);
 }  // namespace kmc_host

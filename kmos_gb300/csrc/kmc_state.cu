@@ -691,6 +691,18 @@ int kmc_pool_restore_state(kmc_pool *p, int32_t model_id, const void *buf, size_
   return KMC_OK;
 }
 
+int kmc_check_image(const int32_t *program, int32_t program_len, const void *buf, size_t bytes) {
+  ModelDev md{};
+  int rc = validate_program(program, program_len, &md);
+  if (rc) return rc;
+  HostState st;
+  rc = read_image(buf, bytes, st);
+  if (rc) return rc;
+  if (st.h.program_hash != program_hash(std::vector<int32_t>(program, program + program_len)))
+    return fail(KMC_ERR_ARG, "state image was saved from another model program");
+  return check_state(st, md);
+}
+
 int kmc_save_state(kmc_handle *h, void *buf, size_t capacity, size_t *bytes) {
   if (!h || !h->pool) return fail(KMC_ERR_ARG, "bad handle");
   return kmc_pool_save_state(h->pool, h->slot, buf, capacity, bytes);

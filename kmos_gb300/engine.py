@@ -38,6 +38,7 @@ SIGNATURES = {
     "kmc_last_error": (ctypes.c_char_p, []),
     "kmc_version": (ctypes.c_char_p, []),
     "kmc_check_program": (_i32, [_p32, _i32]),
+    "kmc_check_image": (_i32, [_p32, _i32, _vp, _sz]),
     "kmc_create": (_i32, [_p32, _i32, _p32, _i32, _i32, _i32, _u32, _P(_vp)]),
     "kmc_destroy": (_i32, [_vp]),
     "kmc_set_rate_const": (_i32, [_vp, _i32, _dbl]),
@@ -335,6 +336,14 @@ def check_program(program) -> None:
     (``kmc_check_program``; no GPU needed).  ``program``: a Program or its int32 words."""
     words = np.ascontiguousarray(getattr(program, "words", program), dtype=np.int32)
     _check(load().kmc_check_program(_ptr(words, _i32), len(words)))
+
+
+def check_image(program, image: bytes) -> None:
+    """Raises KMCError unless ``image`` (a state image, ``Pool.save_state``) would be
+    accepted for ``program`` (``kmc_check_image``; no GPU needed)."""
+    words = np.ascontiguousarray(getattr(program, "words", program), dtype=np.int32)
+    buf = ctypes.create_string_buffer(bytes(image), len(image))
+    _check(load().kmc_check_image(_ptr(words, _i32), len(words), ctypes.cast(buf, ctypes.c_void_p), len(image)))
 
 
 def reload_info(path: str):

@@ -226,3 +226,32 @@ def test_dropin_save_and_reload_system(tmp_path):
         lattice.deallocate_system()
     finally:
         os.chdir(cwd)
+
+
+@pytest.mark.parametrize("name,backend,size", [MODELS[0], MODELS[1]])
+def test_oracle_written_image_continues_like_the_oracle(name, backend, size):
+    """An image written from an oracle trajectory by a writer that shares no code with the
+    engine (oracle/image.py) restores into a pool and steps on exactly as the oracle
+    does."""
+    from oracle import image as IM
+    prog = PG.compile_model(fixture_model(name), backend)
+    o = O.Oracle(prog, size, seed=7, rng=O.RNG_PHILOX, traj=3)
+    o.set_rates(rates_for(prog.nproc, 8))
+    o.update_accum_rate()
+    o.do_kmc_steps(2000)
+    img = IM.write_image(prog, o, size, seed=7, traj=3)
+    pool = E.Pool(arena_bytes=1 << 27, max_slots=4)
+    mid = pool.add_model(prog)
+    s = pool.restore_state(mid, img)
+    pool.run([s], 3000)
+    o.do_kmc_steps(3000)
+    ex = o.export()
+    np.testing.assert_array_equal(pool.lattice(s), ex["lattice"])
+    as1, as2 = pool.tables(s)
+    np.testing.assert_array_equal(as1, ex["as1"])
+    np.testing.assert_array_equal(as2, ex["as2"])
+    ps, ig, t, k, st = pool.results([s], prog.nproc)
+    np.testing.assert_array_equal(ps[0][:prog.nproc], ex["procstat"])
+    assert k[0] == o.kmc_step and st[0] == 0
+    assert abs(t[0] - o.kmc_time) <= 1e-12 * abs(o.kmc_time)
+    pool.close()
