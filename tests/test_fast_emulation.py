@@ -6,8 +6,12 @@ both avail_sites columns and nr_of_sites exactly as the oracle's serial interpre
 of the op program (run_proc_nr, the reference's put/take and lat_int order) leaves them.
 
 Checked on many steps of oracle trajectories of every fixture model under both backends,
-the three-site model, and models compiled without nli tables (member scans).  The GPU
-parity tests check the kernel itself; this pins the stream encoding independently of it.
+the three-site model, and models compiled without nli tables (member scans).  The edits
+are applied twice: directly, and the way the kernel's replay applies them (lane-private
+write log, values loaded before the replay, the entries it leaves out of the log), so
+that the argument that no read needs an unlogged entry is checked too.  The GPU parity
+tests check the kernel itself; this pins the stream encoding and the replay's reads
+independently of it.
 """
 import numpy as np
 import pytest
@@ -25,9 +29,10 @@ def in_mask(species, mask):
     return ((mask & 0xFFFFFFFF) >> (31 if species < 0 else species)) & 1
 
 
-def emulate(words, ex, proc, site, dims):
+def emulate(words, ex, proc, site, dims, replay=False):
     """The fast step of (proc, site) applied to copies of the exported state; None when
-    the process has no fast stream."""
+    the process has no fast stream.  replay: apply the edits the way the kernel's
+    replay does (write log, values loaded before the replay) instead of directly."""
     w = [int(x) for x in words]
     ns_species, spuck = w[4], w[6]
     hot = w[w[21]:w[21] + w[20]]
@@ -93,30 +98,102 @@ def emulate(words, ex, proc, site, dims):
                     p = mem[0]
             if p:
                 fired.append(("del" if op == 4 else "add", p, target))
-    for kind, p, s in fired:  # add_proc / del_proc (base.mpy:211-302), program order
-        q = p - 1
-        n = ns[q]
-        if kind == "add":
-            as1[q, n + 1] = s
-            as2[q, s] = n + 1
-            ns[q] = n + 1
-            continue
-        m = as2[q, s]
-        if m == 0:
-            assert kind == "gdel", "an nli del of an absent entry"
-            continue
-        last = as1[q, n]
-        if m < n:
-            as1[q, m] = last
-            as2[q, last] = m
-            as1[q, n] = 0
-        else:
-            as1[q, m] = 0
-        as2[q, s] = 0
-        ns[q] = n - 1
+    if replay:
+        replay_like_the_kernel(fired, as1, as2, ns, dels_first=bool((w3 >> 20) & 1))
+    else:
+        for kind, p, s in fired:  # add_proc / del_proc (base.mpy:211-302), program order
+            q = p - 1
+            n = ns[q]
+            if kind == "add":
+                as1[q, n + 1] = s
+                as2[q, s] = n + 1
+                ns[q] = n + 1
+                continue
+            m = as2[q, s]
+            if m == 0:
+                assert kind == "gdel", "an nli del of an absent entry"
+                continue
+            last = as1[q, n]
+            if m < n:
+                as1[q, m] = last
+                as2[q, last] = m
+                as1[q, n] = 0
+            else:
+                as1[q, m] = 0
+            as2[q, s] = 0
+            ns[q] = n - 1
     for j in range(nwr):
         lat[latsite[wr[2 * j]] - 1] = wr[2 * j + 1]
     return lat, as1, as2, ns
+
+
+LOG_MAX, TAIL_MAX, TAIL_PROCS = 16, 6, 64  # the kernel's (kmc_device.cuh)
+
+
+def replay_like_the_kernel(fired, as1, as2, ns, dels_first):
+    """The step kernel's replay (replay_process): each process on its own, reads of a
+    del's position and of the list top from the lane's write log (newest first), else
+    from the values loaded before the replay (the position of every del's site, the
+    top TAIL_MAX list entries), else from memory, which every write reaches; the
+    vacated top entries are never logged, and in a dels-first stream neither are the
+    cleared positions nor the adds.  A read that needed an entry left out of the log
+    would see a value from before the step, and the tables would come out wrong."""
+    pre1, pre2, n0s = as1.copy(), as2.copy(), ns.copy()
+    for p in sorted({p for _k, p, _s in fired}):
+        q = p - 1
+        edits = [(k, s) for k, pp, s in fired if pp == p]
+        ndel = sum(1 for k, _s in edits if k != "add")
+        n0 = n0s[q]
+        tail = {n0 - j: pre1[q, n0 - j] for j in range(min(ndel, TAIL_MAX)) if n0 - j >= 1} if q < TAIL_PROCS else {}
+        log, logok, n = [], True, n0
+
+        def put(table, index, val, logged=True):
+            nonlocal logok
+            (as2 if table else as1)[q, index] = val
+            if logged and logok:
+                if len(log) < LOG_MAX:
+                    log.append(((table, index), val))
+                else:
+                    logok = False
+
+        def lookup(table, index):
+            for key, val in reversed(log):
+                if key == (table, index):
+                    return val
+            return None
+
+        for kind, s in edits:
+            if kind == "add":
+                n += 1
+                put(0, n, s, not dels_first)
+                put(1, s, n, not dels_first)
+                continue
+            if not logok:
+                m = as2[q, s]
+            else:
+                m = lookup(1, s)
+                m = pre2[q, s] if m is None else m
+            if m == 0:
+                assert kind == "gdel", "an nli del of an absent entry"
+                continue
+            if m < n:
+                if not logok:
+                    last = as1[q, n]
+                else:
+                    last = lookup(0, n)
+                    if last is None and q < TAIL_PROCS and n0 - n < TAIL_MAX and n <= n0:
+                        assert n in tail, "the kernel would read a list entry it did not load"
+                        last = tail[n]
+                    elif last is None:
+                        last = as1[q, n]
+                put(0, m, last)
+                put(0, n, 0, False)
+                put(1, last, m)
+            else:
+                put(0, m, 0, False)
+            put(1, s, 0, not dels_first)
+            n -= 1
+        ns[q] = n
 
 
 CASES = [("AB_model", "local_smart", (20, 20), True), ("ZGB_model", "local_smart", (16, 12), True),
@@ -125,7 +202,11 @@ CASES = [("AB_model", "local_smart", (20, 20), True), ("ZGB_model", "local_smart
          ("pairwise_interaction", "local_smart", (8, 8), True), ("default_xml", "local_smart", (10, 10), True),
          ("pdopd_xml", "local_smart", (8, 8), True), ("pdopd_xml", "lat_int", (8, 8), True),
          ("trimer", "local_smart", (14, 14), True), ("trimer", "lat_int", (14, 14), True),
-         ("trimer", "lat_int", (14, 14), False), ("pairwise_interaction", "lat_int", (16, 16), False)]
+         ("trimer", "lat_int", (14, 14), False), ("pairwise_interaction", "lat_int", (16, 16), False),
+         # the smallest lattices the fast path takes: short lists, so a del often reads an
+         # entry an earlier del of the same step moved (the replay's write log is used)
+         ("ZGB_model", "lat_int", (5, 5), True), ("CO_oxidation_Ruo2", "lat_int", (5, 5), True),
+         ("ZGB_model", "local_smart", (5, 5), True), ("default_xml", "local_smart", (5, 5), True)]
 
 
 @pytest.mark.parametrize("name,backend,size,tables", CASES)
@@ -134,6 +215,8 @@ def test_fast_stream_equals_serial_interpretation(name, backend, size, tables, m
         monkeypatch.setattr(PG, "NLI_TABLE_MAX", 0)
     prog = PG.compile_model(trimer_model() if name == "trimer" else fixture_model(name), backend)
     monkeypatch.undo()
+    reach = int(prog.words[19])
+    assert size[0] > 2 * (reach & 0xFF) and size[1] > 2 * ((reach >> 8) & 0xFF)  # the fast path's lattices
     rates = (10.0 ** np.random.default_rng(3).uniform(-1, 2, size=prog.nproc)).tolist()
     o = O.Oracle(prog, size, seed=11, rng=O.RNG_PHILOX, traj=1)
     o.set_rates(rates)
@@ -144,14 +227,17 @@ def test_fast_stream_equals_serial_interpretation(name, backend, size, tables, m
         o.do_kmc_steps(150)
         for _ in range(8):
             proc, site = o.get_next_kmc_step()
-            got = emulate(prog.words, o.export(), proc, site, dims)
+            before = o.export()
+            got = emulate(prog.words, before, proc, site, dims)
+            got_replay = emulate(prog.words, before, proc, site, dims, replay=True)
             o.run_proc_nr(proc, site)
             if got is None:
                 continue
             ex = o.export()
-            np.testing.assert_array_equal(got[0], ex["lattice"])
-            np.testing.assert_array_equal(got[1], ex["as1"])
-            np.testing.assert_array_equal(got[2], ex["as2"])
-            np.testing.assert_array_equal(got[3], ex["nsites"])
+            for g in (got, got_replay):
+                np.testing.assert_array_equal(g[0], ex["lattice"])
+                np.testing.assert_array_equal(g[1], ex["as1"])
+                np.testing.assert_array_equal(g[2], ex["as2"])
+                np.testing.assert_array_equal(g[3], ex["nsites"])
             checked += 1
     assert checked > 40
