@@ -22,7 +22,11 @@ CASES = [("AB_model", "local_smart", (20, 20)), ("ZGB_model", "local_smart", (16
          # lattices narrower than 2*reach+1: every step takes the serial interpreter
          ("pairwise_interaction", "lat_int", (5, 5)), ("ZGB_model", "local_smart", (3, 3)),
          # streams of more than 96 edits: the 4-round fast path
-         ("CO_oxidation_Ruo2", "lat_int", (14, 14)), ("default_xml", "lat_int", (14, 14))]
+         ("CO_oxidation_Ruo2", "lat_int", (14, 14)), ("default_xml", "lat_int", (14, 14)),
+         # the smallest lattices the fast path takes: short lists, so dels often read what
+         # an earlier del of the same step moved (the replay's write log)
+         ("ZGB_model", "lat_int", (5, 5)), ("CO_oxidation_Ruo2", "lat_int", (5, 5)),
+         ("ZGB_model", "local_smart", (5, 5)), ("default_xml", "local_smart", (5, 5))]
 
 
 def random_rates(P, seed):
