@@ -39,3 +39,22 @@ def trimer_model():
     procs.append(Process("A_hop", "1", [c("A", "a"), c("empty", "a", (1, 0, 0))],
                          [c("empty", "a"), c("A", "a", (1, 0, 0))]))
     return configs._square_model("trimer", ["empty", "A"], procs)
+
+
+def many_species_model(nspecies=16):
+    """A square-lattice model with ``nspecies`` adsorbates, each with adsorption,
+    desorption and hops in four directions (6 * nspecies processes): 16 species give 96
+    processes (four per lane of the step kernel), 30 give 180 (eight per lane), and
+    processes past the 64th, whose list tops the kernel does not load ahead."""
+    from kmos_gb300 import configs
+    from kmos_gb300.model import Process
+    c = configs._c
+    names = ["A%02d" % i for i in range(nspecies)]
+    procs = []
+    for sp in names:
+        procs.append(Process(sp + "_adsorption", "1", [c("empty", "a")], [c(sp, "a")]))
+        procs.append(Process(sp + "_desorption", "1", [c(sp, "a")], [c("empty", "a")]))
+        for i, d in enumerate(configs.DIRS, start=1):
+            procs.append(Process("%s_hop%d" % (sp, i), "1", [c(sp, "a"), c("empty", "a", d)],
+                                 [c("empty", "a"), c(sp, "a", d)]))
+    return configs._square_model("many_species", ["empty"] + names, procs)

@@ -16,7 +16,7 @@ independently of it.
 import numpy as np
 import pytest
 
-from conftest import fixture_model, trimer_model
+from conftest import fixture_model, many_species_model, trimer_model
 from kmos_gb300 import program as PG
 from oracle import oracle as O
 
@@ -206,14 +206,18 @@ CASES = [("AB_model", "local_smart", (20, 20), True), ("ZGB_model", "local_smart
          # the smallest lattices the fast path takes: short lists, so a del often reads an
          # entry an earlier del of the same step moved (the replay's write log is used)
          ("ZGB_model", "lat_int", (5, 5), True), ("CO_oxidation_Ruo2", "lat_int", (5, 5), True),
-         ("ZGB_model", "local_smart", (5, 5), True), ("default_xml", "local_smart", (5, 5), True)]
+         ("ZGB_model", "local_smart", (5, 5), True), ("default_xml", "local_smart", (5, 5), True),
+         # 96 processes: fast streams of processes past the 64th, whose list tops the
+         # kernel does not load ahead
+         ("many_species", "local_smart", (8, 8), True)]
 
 
 @pytest.mark.parametrize("name,backend,size,tables", CASES)
 def test_fast_stream_equals_serial_interpretation(name, backend, size, tables, monkeypatch):
     if not tables:
         monkeypatch.setattr(PG, "NLI_TABLE_MAX", 0)
-    prog = PG.compile_model(trimer_model() if name == "trimer" else fixture_model(name), backend)
+    model = {"trimer": trimer_model, "many_species": many_species_model}.get(name, lambda: fixture_model(name))()
+    prog = PG.compile_model(model, backend)
     monkeypatch.undo()
     reach = int(prog.words[19])
     assert size[0] > 2 * (reach & 0xFF) and size[1] > 2 * ((reach >> 8) & 0xFF)  # the fast path's lattices

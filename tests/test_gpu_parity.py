@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, fixture_model, trimer_model
+from conftest import GOLDEN, fixture_model, many_species_model, trimer_model
 from kmos_gb300 import configs, engine as E, program as PG
 from oracle import oracle as O
 
@@ -134,6 +134,25 @@ def test_wide_conditions_and_member_scans(which, backend, tables, monkeypatch):
             for chunk in (1, 999, 4000):
                 np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
             assert_same_state(g, o, P, o.V)
+
+
+@pytest.mark.parametrize("nspecies,backend", [(16, "local_smart"), (16, "lat_int"), (29, "local_smart")])
+def test_large_process_counts(nspecies, backend):
+    """96 and 174 processes: the kernels with four and eight processes per lane, fast
+    streams of processes past the 64th (whose list tops are not loaded ahead: their
+    replay reads them from memory) and the serial interpreter for the streams over the
+    on-chip limits."""
+    prog = PG.compile_model(many_species_model(nspecies), backend)
+    rates = (10.0 ** np.random.default_rng(5).uniform(-1, 2, size=prog.nproc)).tolist()
+    with E.Trajectory(prog, (12, 12), seed=13, rng=E.RNG_PHILOX, traj=2) as g:
+        o = O.Oracle(prog, (12, 12), seed=13, rng=O.RNG_PHILOX, traj=2)
+        for x in (g, o):
+            x.set_rates(rates)
+            x.update_accum_rate()
+        for chunk in (1, 999, 3000):
+            np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+        assert_same_state(g, o, prog.nproc, o.V)
+        np.testing.assert_array_equal(g.accum_rates(), o.accum_rates())
 
 
 @pytest.mark.parametrize("T", [300.0, 600.0])
