@@ -58,3 +58,19 @@ def many_species_model(nspecies=16):
             procs.append(Process("%s_hop%d" % (sp, i), "1", [c(sp, "a"), c("empty", "a", d)],
                                  [c("empty", "a"), c(sp, "a", d)]))
     return configs._square_model("many_species", ["empty"] + names, procs)
+
+
+def rows_model(k=8):
+    """Adsorption, desorption, and desorption of a whole row of ``k`` adsorbates at once:
+    the row event clears k sites, so one process (the row process anchored at each of
+    the 2k-1 cells around them, and the single desorption at each of the k sites) gets
+    many dels in one step -- more than the kernel loads list tops for ahead and more
+    writes than its replay log holds."""
+    from kmos_gb300 import configs
+    from kmos_gb300.model import Process
+    c = configs._c
+    procs = [Process("A_adsorption", "1", [c("empty", "a")], [c("A", "a")]),
+             Process("A_desorption", "1", [c("A", "a")], [c("empty", "a")]),
+             Process("A_row_desorption", "1", [c("A", "a", (i, 0, 0)) for i in range(k)],
+                     [c("empty", "a", (i, 0, 0)) for i in range(k)])]
+    return configs._square_model("rows", ["empty", "A"], procs)

@@ -16,7 +16,7 @@ independently of it.
 import numpy as np
 import pytest
 
-from conftest import fixture_model, many_species_model, trimer_model
+from conftest import fixture_model, many_species_model, rows_model, trimer_model
 from kmos_gb300 import program as PG
 from oracle import oracle as O
 
@@ -209,19 +209,25 @@ CASES = [("AB_model", "local_smart", (20, 20), True), ("ZGB_model", "local_smart
          ("ZGB_model", "local_smart", (5, 5), True), ("default_xml", "local_smart", (5, 5), True),
          # 96 processes: fast streams of processes past the 64th, whose list tops the
          # kernel does not load ahead
-         ("many_species", "local_smart", (8, 8), True)]
+         ("many_species", "local_smart", (8, 8), True),
+         # row desorption: dozens of dels of one process in one step, more than the list
+         # tops loaded ahead and than the replay log holds
+         ("rows", "local_smart", (16, 6), True), ("rows", "lat_int", (32, 4), True)]
 
 
 @pytest.mark.parametrize("name,backend,size,tables", CASES)
 def test_fast_stream_equals_serial_interpretation(name, backend, size, tables, monkeypatch):
     if not tables:
         monkeypatch.setattr(PG, "NLI_TABLE_MAX", 0)
-    model = {"trimer": trimer_model, "many_species": many_species_model}.get(name, lambda: fixture_model(name))()
+    model = {"trimer": trimer_model, "many_species": many_species_model,
+             "rows": rows_model}.get(name, lambda: fixture_model(name))()
     prog = PG.compile_model(model, backend)
     monkeypatch.undo()
     reach = int(prog.words[19])
     assert size[0] > 2 * (reach & 0xFF) and size[1] > 2 * ((reach >> 8) & 0xFF)  # the fast path's lattices
     rates = (10.0 ** np.random.default_rng(3).uniform(-1, 2, size=prog.nproc)).tolist()
+    if name == "rows":
+        rates = [20.0, 1.0, 50.0]  # rows fill up and leave often
     o = O.Oracle(prog, size, seed=11, rng=O.RNG_PHILOX, traj=1)
     o.set_rates(rates)
     o.update_accum_rate()

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, fixture_model, many_species_model, trimer_model
+from conftest import GOLDEN, fixture_model, many_species_model, rows_model, trimer_model
 from kmos_gb300 import configs, engine as E, program as PG
 from oracle import oracle as O
 
@@ -153,6 +153,22 @@ def test_large_process_counts(nspecies, backend):
             np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
         assert_same_state(g, o, prog.nproc, o.V)
         np.testing.assert_array_equal(g.accum_rates(), o.accum_rates())
+
+
+@pytest.mark.parametrize("backend,size", [("local_smart", (16, 6)), ("lat_int", (32, 4))])
+def test_many_dels_of_one_process(backend, size):
+    """Row desorption clears eight sites at once: one process gets up to dozens of dels
+    in a step, past the list tops the kernel loads ahead (the replay reads the rest from
+    memory) and past its write log (once full, every read goes to memory)."""
+    prog = PG.compile_model(rows_model(8), backend)
+    with E.Trajectory(prog, size, seed=17, rng=E.RNG_PHILOX, traj=5) as g:
+        o = O.Oracle(prog, size, seed=17, rng=O.RNG_PHILOX, traj=5)
+        for x in (g, o):
+            x.set_rates([20.0, 1.0, 50.0])
+            x.update_accum_rate()
+        for chunk in (1, 999, 5000):
+            np.testing.assert_array_equal(g.trace(chunk), o.trace(chunk))
+            assert_same_state(g, o, prog.nproc, o.V)
 
 
 @pytest.mark.parametrize("T", [300.0, 600.0])
