@@ -311,6 +311,33 @@ def test_serial_and_fast_paths_agree(config):
         assert ca == cb
 
 
+@pytest.mark.parametrize("config", [2, 3, 4])
+def test_launch_shape_and_table_placement_do_not_change_results(config):
+    """Every launch shape the autotuner tries (one balanced block per SM, 2 or 8 warps per
+    block) and both placements of the model's hot section (shared or global memory) give
+    the same trajectories bit for bit; steps per launch too (one launch of 3000 steps
+    against three of 1000)."""
+    wl = configs.build(config, n=40, steps=0, sides=[16, 32])
+    out = []
+    for warps, shared, launches in ((0, True, 1), (2, True, 1), (8, False, 1), (0, False, 3), (8, True, 3)):
+        pool = E.Pool(arena_bytes=1 << 30, max_slots=64)
+        pool.set_launch(warps, 0)
+        pool.set_table_placement(shared)
+        mid = pool.add_model(wl.program)
+        slots = pool.admit_many([mid] * wl.n, wl.sizes, wl.rates, seeds=wl.seeds, rng=E.RNG_PHILOX, trajs=wl.trajs)
+        for _ in range(launches):
+            pool.run(slots, 3000 // launches)
+        out.append([(pool.tables(s), pool.procstat(s), pool.clock(s), pool.lattice(s)) for s in slots])
+        pool.close()
+    for other in out[1:]:
+        for (ta, pa, ca, la), (tb, pb, cb, lb) in zip(out[0], other):
+            np.testing.assert_array_equal(ta[0], tb[0])
+            np.testing.assert_array_equal(ta[1], tb[1])
+            np.testing.assert_array_equal(pa, pb)
+            np.testing.assert_array_equal(la, lb)
+            assert ca == cb
+
+
 def test_run_list_checks():
     """A slot listed twice in one run, and negative rate offsets, are refused before any
     launch."""
