@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: only tests/,
  * __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm may load it,
- * and only as the checker or as the timed CPU baseline.  The product (kmos_gb300/)
+ * and only as the oracle or as the timed CPU baseline.  The product (kmos_gb300/)
  * never links or calls it.
  *
  * What it restates (mhoffman/kmos, paths relative to the project root):

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (``kmc_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: tests/, ``__graft_entry__.smoke()`` and bench.py's CPU
-baseline use this module as the checker.  The product never imports it.
+baseline use this module as the oracle.  The product never imports it.
 """
 from __future__ import annotations
 

@@ -1,4 +1,4 @@
-"""kmos ``.reload`` files, restated for the checker.
+"""kmos ``.reload`` files, restated for the oracle.
 
 TEST INFRASTRUCTURE ONLY: tests/ use this module to check the engine's
 ``kmc_save_reload`` / ``kmc_load_reload`` against an independent writer and reader of

@@ -5,7 +5,7 @@ The reference's kmos.run module (kmos/run/__init__.py) is imported with a stand-
 ``kmc_model`` whose base / lattice / proclist getters read an oracle trajectory (the
 CPU restatement of the compiled step loop) and a stand-in ``kmc_settings``.  Then
 KMC_Model.get_std_sampled_data and KMC_Model.get_atoms run unmodified on that state.
-The committed JSON pins oracle/sampling.py (the checker of the engine's on-device
+The committed JSON pins oracle/sampling.py (the oracle for the engine's on-device
 sampling) to the reference's Python arithmetic.
 
 Run in a container that has mhoffman/kmos at KMOS_REFERENCE (default /root/reference):

@@ -1,6 +1,6 @@
 """On-device sampling (kmc_pool_sample_*, kmos_gb300.sampling.get_std_sampled_data)
 against get_std_sampled_data (kmos/run/__init__.py:865-966): the reference's own code's
-outputs on oracle trajectories (tests/golden/sampling.json) and the checker's
+outputs on oracle trajectories (tests/golden/sampling.json) and the oracle's
 restatement (oracle/sampling.py) on a batch of mixed trajectories.
 
 Tolerances: kMC step counts exact; times, TOFs and occupation means within 1e-12

@@ -4,7 +4,7 @@
   saved, released and restored into another slot continues bit for bit like one that
   never left the device; images are validated before they reach the device.
 * .reload files (base.save_system / reload_system, base.mpy:363-578): the engine's file
-  equals the checker's writer (oracle/reload.py) on the same state, line for line; a
+  equals the oracle's writer (oracle/reload.py) on the same state, line for line; a
   file with the engine's "#gb300" lines resumes the trajectory exactly; a file in the
   reference's bare layout loads its lattice, tables and counters.
 """
@@ -118,7 +118,7 @@ def _lines(path):
 
 
 @pytest.mark.parametrize("name,backend,size", MODELS)
-def test_reload_file_matches_checker(name, backend, size, tmp_path):
+def test_reload_file_matches_oracle_writer(name, backend, size, tmp_path):
     prog = PG.compile_model(fixture_model(name), backend)
     rates = rates_for(prog.nproc, 4)
     with E.Trajectory(prog, size, seed=13, rng=E.RNG_GFORTRAN) as g:

@@ -1,4 +1,4 @@
-"""The checker's .reload writer and reader (oracle/reload.py) on the CPU: Fortran edit
+"""The oracle's .reload writer and reader (oracle/reload.py) on the CPU: Fortran edit
 descriptors of base.mpy:528-575 on known values, and a write / read round trip of an
 oracle trajectory's state."""
 import numpy as np
