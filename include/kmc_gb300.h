@@ -107,6 +107,10 @@ KMC_API int kmc_run_proc_nr(kmc_handle *h, int32_t proc, int32_t site);
  * 2411-2443, 1766-1791); site is the 1-based site index of the site (local_smart) or
  * of any site of the cell (lat_int). */
 KMC_API int kmc_touchup(kmc_handle *h, int32_t site);
+/* The touch-ups of n sites, in list order, in one launch: what kmos.run's
+ * _adjust_database (kmos/run/__init__.py:1439-1457) does with one touchup call per site.
+ * Sites as for kmc_touchup; all are checked before any runs. */
+KMC_API int kmc_touchup_many(kmc_handle *h, const int32_t *sites, int32_t n);
 /* base.get_species(site) (base.mpy:1164-1184) */
 KMC_API int kmc_get_species(kmc_handle *h, int32_t site, int32_t *species);
 /* base.replace_species(site, old, new) (base.mpy:1187-1231) */

@@ -736,12 +736,14 @@ __global__ void __launch_bounds__(256) kmc_init_kernel(InitArgs a) {
 }
 
 // ----------------------------------------------------------------- command kernel
-enum Cmd { CMD_RUN_PROC = 1, CMD_TOUCHUP = 2, CMD_GET_NEXT = 3, CMD_ACCUM = 4, CMD_INTEG = 5, CMD_REPLACE = 6 };
+enum Cmd { CMD_RUN_PROC = 1, CMD_TOUCHUP = 2, CMD_GET_NEXT = 3, CMD_ACCUM = 4, CMD_INTEG = 5, CMD_REPLACE = 6,
+           CMD_TOUCHUP_LIST = 7 };
 
 struct CmdArgs {
   SlotDev *slots;
   const ModelDev *models;
   int32_t slot, cmd, a0, a1, a2;
+  const int32_t *list;  // sites of CMD_TOUCHUP_LIST (a0 of them)
   int32_t *out;  // [status, proc, site]
 };
 
@@ -781,6 +783,16 @@ __global__ void kmc_command_kernel(CmdArgs a) {
       int bx, by, bz, bn;
       v.g.coords(a.a0, bx, by, bz, bn);
       run_stream(v, M.prog[M.off_touch + (M.backend == 1 ? 0 : bn - 1)], bx, by, bz);
+      status = v.err;
+      S.accum_from = v.minp;
+      break;
+    }
+    case CMD_TOUCHUP_LIST: {  // the touch-ups of a0 sites, one after the other, in list order
+      for (int k = 0; k < a.a0 && v.err == ST_OK; k++) {
+        int bx, by, bz, bn;
+        v.g.coords(a.list[k], bx, by, bz, bn);
+        run_stream(v, M.prog[M.off_touch + (M.backend == 1 ? 0 : bn - 1)], bx, by, bz);
+      }
       status = v.err;
       S.accum_from = v.minp;
       break;
@@ -1361,10 +1373,11 @@ int check_slot(kmc_pool *p, int slot) {
   return KMC_OK;
 }
 
-int run_command(kmc_pool *p, int slot, int cmd, int a0, int a1, int a2, int32_t *proc, int32_t *site) {
+int run_command(kmc_pool *p, int slot, int cmd, int a0, int a1, int a2, int32_t *proc, int32_t *site,
+                const int32_t *d_list) {
   CmdArgs c;
   c.slots = p->d_slots; c.models = p->d_models; c.slot = slot; c.cmd = cmd;
-  c.a0 = a0; c.a1 = a1; c.a2 = a2; c.out = p->d_cmd_out;
+  c.a0 = a0; c.a1 = a1; c.a2 = a2; c.list = d_list; c.out = p->d_cmd_out;
   kmc_command_kernel<<<1, 32, 0, p->stream>>>(c);
   CK(cudaGetLastError());
   p->launches++;
@@ -1968,12 +1981,12 @@ int kmc_set_rate_const(kmc_handle *h, int32_t proc, double rate) {
 
 int kmc_update_accum_rate(kmc_handle *h) {
   HCHECK(h);
-  return run_command(h->pool, h->slot, CMD_ACCUM, 0, 0, 0, nullptr, nullptr);
+  return run_command(h->pool, h->slot, CMD_ACCUM, 0, 0, 0, nullptr, nullptr, nullptr);
 }
 
 int kmc_update_integ_rate(kmc_handle *h) {
   HCHECK(h);
-  return run_command(h->pool, h->slot, CMD_INTEG, 0, 0, 0, nullptr, nullptr);
+  return run_command(h->pool, h->slot, CMD_INTEG, 0, 0, 0, nullptr, nullptr, nullptr);
 }
 
 static int finish_run(kmc_handle *h) {
@@ -2026,25 +2039,38 @@ int kmc_trace_steps(kmc_handle *h, int64_t n, int32_t *out) {
 
 int kmc_get_next_step(kmc_handle *h, int32_t *proc, int32_t *site) {
   HCHECK(h);
-  return run_command(h->pool, h->slot, CMD_GET_NEXT, 0, 0, 0, proc, site);
+  return run_command(h->pool, h->slot, CMD_GET_NEXT, 0, 0, 0, proc, site, nullptr);
 }
 
 int kmc_run_proc_nr(kmc_handle *h, int32_t proc, int32_t site) {
   HCHECK(h);
   if (proc < 1 || proc > h->P || site < 1 || site > h->V) return fail(KMC_ERR_ARG, "proc or site out of range");
-  return run_command(h->pool, h->slot, CMD_RUN_PROC, proc, site, 0, nullptr, nullptr);
+  return run_command(h->pool, h->slot, CMD_RUN_PROC, proc, site, 0, nullptr, nullptr, nullptr);
 }
 
 int kmc_touchup(kmc_handle *h, int32_t site) {
   HCHECK(h);
   if (site < 1 || site > h->V) return fail(KMC_ERR_ARG, "site out of range");
-  return run_command(h->pool, h->slot, CMD_TOUCHUP, site, 0, 0, nullptr, nullptr);
+  return run_command(h->pool, h->slot, CMD_TOUCHUP, site, 0, 0, nullptr, nullptr, nullptr);
+}
+
+int kmc_touchup_many(kmc_handle *h, const int32_t *sites, int32_t n) {
+  HCHECK(h);
+  if (n < 0 || (n > 0 && !sites)) return fail(KMC_ERR_ARG, "bad arguments");
+  for (int k = 0; k < n; k++)
+    if (sites[k] < 1 || sites[k] > h->V) return fail(KMC_ERR_ARG, "site out of range");
+  if (n == 0) return KMC_OK;
+  kmc_pool *p = h->pool;
+  AsyncScratch list(p->stream);
+  CK(list.alloc(sizeof(int32_t) * n));
+  CK(cudaMemcpyAsync(list.as<int32_t>(), sites, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+  return run_command(p, h->slot, CMD_TOUCHUP_LIST, n, 0, 0, nullptr, nullptr, list.as<int32_t>());
 }
 
 int kmc_replace_species(kmc_handle *h, int32_t site, int32_t old_species, int32_t new_species) {
   HCHECK(h);
   if (site < 1 || site > h->V) return fail(KMC_ERR_ARG, "site out of range");
-  return run_command(h->pool, h->slot, CMD_REPLACE, site, old_species, new_species, nullptr, nullptr);
+  return run_command(h->pool, h->slot, CMD_REPLACE, site, old_species, new_species, nullptr, nullptr, nullptr);
 }
 
 int kmc_get_species(kmc_handle *h, int32_t site, int32_t *species) {

@@ -49,6 +49,7 @@ SIGNATURES = {
     "kmc_get_next_step": (_i32, [_vp, _p32, _p32]),
     "kmc_run_proc_nr": (_i32, [_vp, _i32, _i32]),
     "kmc_touchup": (_i32, [_vp, _i32]),
+    "kmc_touchup_many": (_i32, [_vp, _p32, _i32]),
     "kmc_get_species": (_i32, [_vp, _i32, _p32]),
     "kmc_replace_species": (_i32, [_vp, _i32, _i32, _i32]),
     "kmc_get_kmc_time": (_i32, [_vp, _pd]),
@@ -232,6 +233,11 @@ class Trajectory:
 
     def touchup(self, site: int):
         _check(load().kmc_touchup(self.h, int(site)))
+
+    def touchup_many(self, sites):
+        """Touch-ups of many sites in order, one launch (``kmc_touchup_many``)."""
+        sites = np.ascontiguousarray(sites, dtype=np.int32)
+        _check(load().kmc_touchup_many(self.h, _ptr(sites, _i32), len(sites)))
 
     def get_species(self, site: int) -> int:
         s = _i32()

@@ -42,11 +42,27 @@ class _State:
         self.system_size = np.zeros(3, dtype=np.int32)
         self.seed = 1
         self.system_name = "kmc_model"
+        self.pending: list = []  # touch-ups queued, run before the next call reaches the engine
 
     def t(self) -> E.Trajectory:
         if self.traj is None:
             raise E.KMCError(1, "system not allocated: call proclist.init first")
+        if self.pending:
+            sites, self.pending = self.pending, []
+            self.traj.touchup_many(sites)
         return self.traj
+
+    def touchup(self, site) -> None:
+        """touchup_<layer>_<site> / touchup_cell: queued, so that kmos.run's
+        _adjust_database (one call per site, kmos/run/__init__.py:1439-1457) becomes one
+        launch; the queue runs, in call order, before any other call reaches the engine
+        (a touch-up error surfaces there)."""
+        if self.traj is None:
+            raise E.KMCError(1, "system not allocated: call proclist.init first")
+        nr = self.lattice2nr(site)
+        if not 1 <= nr <= int(np.prod(self.system_size)) * self.model.spuck:
+            raise E.KMCError(1, "site out of range")
+        self.pending.append(nr)
 
     # lattice mapping (lattice.mpy:146-210)
     def lattice2nr(self, site) -> int:
@@ -148,6 +164,7 @@ def _lattice(S: _State) -> types.SimpleNamespace:
     ns.replace_species = lambda site, old, new: S.t().replace_species(S.lattice2nr(site), int(old), int(new))
 
     def deallocate_system():
+        S.pending = []
         if S.traj is not None:
             S.traj.close()
             S.traj = None
@@ -204,11 +221,10 @@ def _proclist(S: _State) -> types.SimpleNamespace:
 
     ns.get_occupation = get_occupation
     if S.backend == "lat_int":
-        ns.touchup_cell = lambda cell: S.t().touchup(S.lattice2nr([cell[0], cell[1], cell[2], 1]))
+        ns.touchup_cell = lambda cell: S.touchup([cell[0], cell[1], cell[2], 1])
     else:
         for (lname, sname), n in m.site_ids().items():
-            setattr(ns, ("touchup_%s_%s" % (lname, sname)).lower(),
-                    lambda site: S.t().touchup(S.lattice2nr(site)))
+            setattr(ns, ("touchup_%s_%s" % (lname, sname)).lower(), lambda site: S.touchup(site))
     return ns
 
 

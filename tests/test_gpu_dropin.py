@@ -68,3 +68,54 @@ def test_do_steps_and_tof_readout_match_the_oracle(name, backend):
     assert [lattice.calculate_lattice2nr(x) for x in sites] == [1, 7, 100]
     assert [lattice.get_species(x) for x in sites] == [o.get_species(s) for s in (1, 7, 100)]
     lattice.deallocate_system()
+
+
+@pytest.mark.parametrize("name,backend", [("ZGB_model", "local_smart"), ("ZGB_model", "lat_int"),
+                                          ("CO_oxidation_Ruo2", "local_smart")])
+def test_put_and_adjust_database(name, backend):
+    """kmos.run's put (lattice.replace_species, then _adjust_database: a touch-up of every
+    site -- every cell for lat_int -- in order, then update_accum_rate;
+    kmos/run/__init__.py:1243-1314, 1439-1457) through the drop-in module, whose queued
+    touch-ups run as one launch, against the oracle making the same calls one by one."""
+    m, base, lattice, proclist = reset(name, size=10, seed=4, backend=backend)
+    prog = PG.compile_model(m, backend)
+    P = prog.nproc
+    o = O.Oracle(prog, (10, 10), layer=lattice.default_layer, seed=4, rng=O.RNG_GFORTRAN)
+    o.set_rates([base.get_rate(p) for p in range(1, P + 1)])
+    o.update_accum_rate()
+    proclist.do_kmc_steps(400)
+    o.do_kmc_steps(400)
+    rng = np.random.default_rng(9)
+    X, Y, spuck = 10, 10, int(lattice.spuck)
+    nspecies = len(m.species)
+    for _ in range(12):  # put
+        x, y, n = int(rng.integers(0, X)), int(rng.integers(0, Y)), int(rng.integers(1, spuck + 1))
+        new = int(rng.integers(0, nspecies))
+        old = lattice.get_species([x, y, 0, n])
+        lattice.replace_species([x, y, 0, n], old, new)
+        o.replace_species(lattice.calculate_lattice2nr([x, y, 0, n]), old, new)
+    touch = sorted(a for a in dir(proclist) if a.startswith("touchup_"))
+    for x in range(X):  # _adjust_database
+        for y in range(Y):
+            if backend == "lat_int":
+                proclist.touchup_cell([x, y, 0, 0])
+                o.touchup(lattice.calculate_lattice2nr([x, y, 0, 1]))
+            else:
+                for n in range(spuck):
+                    getattr(proclist, touch[n])([x, y, 0, n + 1])
+                    o.touchup(lattice.calculate_lattice2nr([x, y, 0, n + 1]))
+    base.update_accum_rate()
+    o.update_accum_rate()
+    ex = o.export()
+    for p in range(1, P + 1):
+        n_p = base.get_nrofsites(p)
+        assert n_p == ex["nsites"][p - 1]
+        assert [base.get_avail_site(p, i, 1) for i in range(1, n_p + 1)] == list(ex["as1"][p - 1, 1:n_p + 1])
+        assert base.get_accum_rate(p) == o.accum_rates()[p - 1]
+    proclist.do_kmc_steps(3000)
+    o.do_kmc_steps(3000)
+    ex = o.export()
+    assert base.get_kmc_step() == o.kmc_step
+    assert [base.get_nrofsites(p) for p in range(1, P + 1)] == list(ex["nsites"])
+    assert [lattice.get_species(lattice.calculate_nr2lattice(s)) for s in range(1, o.V + 1)] == list(ex["lattice"])
+    lattice.deallocate_system()
