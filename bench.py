@@ -21,6 +21,12 @@ reference step loop (the reference's Fortran build needs a Fortran compiler that
 machine does not have) on all host cores, on a bounded sample of the same workload.
 Under torchrun each rank runs its own batch (trajectory ids offset by rank): weak
 scaling, no collective on the data path.
+
+After the timed region rank 0 adds the two other parts of the metric: ``plain_dropin``,
+the steps/s of one trajectory of the workload through the handle API (the plain
+one-trajectory drop-in the batched rate is compared with; ``--plain 0`` skips it), and
+``serving``, p50 / p99 request latency and served steps/s of a short run of the serving
+loop on the configuration-5 request stream (one GPU only; ``--serving 0`` skips it).
 """
 from __future__ import annotations
 
@@ -60,6 +66,10 @@ def parse():
     ap.add_argument("--autotune", type=int, default=1, help="pick the launch shape on scratch trajectories first")
     ap.add_argument("--cpu-steps", type=int, default=0,
                     help="kMC steps per trajectory of the CPU sample (default: a 10-30 s sample per config)")
+    ap.add_argument("--plain", type=int, default=1,
+                    help="also time the plain drop-in: one trajectory of the workload through the handle API")
+    ap.add_argument("--serving", type=int, default=1,
+                    help="also run a short serving sample (configuration 5 stream, 1 s of arrivals, steps x 0.05)")
     return ap.parse_args()
 
 
@@ -375,9 +385,51 @@ def run_ours(args, dist: Dist):
             "clocks": clk,
             "gpu_launches": launches,
         }
-        print(json.dumps(line))
     pool.close()
+    if line is not None and args.plain:
+        line["plain_dropin"] = plain_dropin(wl)
+    if line is not None and args.serving and dist.world == 1:
+        line["serving"] = serving_sample()
+    if line is not None:
+        print(json.dumps(line))
     dist.close()
+
+
+def plain_dropin(wl):
+    """The plain method: one trajectory of the workload (its first) stepped through the
+    handle API (kmc_create / kmc_do_steps, what the f2py module calls), after the timed
+    region."""
+    from kmos_gb300 import engine as E
+    steps = 20000
+    with E.Trajectory(wl.program, wl.sizes[0], seed=wl.seeds[0], rng=E.RNG_PHILOX, traj=wl.trajs[0]) as g:
+        g.set_rates(wl.rates[0])
+        g.update_accum_rate()
+        g.do_kmc_steps(2000)
+        t0 = time.perf_counter()
+        g.do_kmc_steps(steps)
+        dt = time.perf_counter() - t0
+    size = "x".join(str(v) for v in wl.sizes[0][:2])
+    return {"value": steps / dt, "unit": UNIT, "trajectory": "%s, lattice %s, trajectory 0" % (wl.name, size),
+            "steps": steps}
+
+
+def serving_sample():
+    """A short run of the serving loop on the configuration-5 request stream (1 s of
+    Poisson arrivals at 500/s, steps x 0.05), after the timed region: p50 / p99 request
+    latency and served steps/s.  profiles/serving_config5.md has the full-size runs."""
+    from kmos_gb300 import configs, serving
+    reqs, progs = configs.serving_requests(rate=500.0, duration=1.0, steps_scale=0.05)
+    srv = serving.Server(arena_bytes=16 << 30, max_slots=4096, quantum=20000, policy="fifo")
+    for k, p in progs.items():
+        srv.add_model(k, p)
+    t0 = time.perf_counter()
+    done = srv.serve(reqs)
+    wall = time.perf_counter() - t0
+    stats = serving.latency_stats(done)
+    out = {"requests": len(reqs), "rate_per_s": 500.0, "duration_s": 1.0, "steps_scale": 0.05,
+           "served_steps_per_s": srv.kmc_steps / wall, "wall_s": wall, **stats}
+    srv.close()
+    return out
 
 
 def main():
