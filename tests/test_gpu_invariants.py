@@ -5,13 +5,14 @@ has run, sampled trajectories of every lattice size must have
   * exactly the processes their lattice enables listed (the oracle derives those from
     the lattice alone, by touch-ups: oracle_rebuild_tables);
   * procstat summing to kmc_step and a positive, finite kmc_time.
-The oracle cannot replay millions of steps of thousands of trajectories; these checks
-need no replay."""
+The table checks are tests/table_invariants.py (tests/test_planted_mistakes.py shows
+them catching planted mistakes).  The oracle cannot replay millions of steps of
+thousands of trajectories; these checks need no replay."""
 import numpy as np
 import pytest
 
 from kmos_gb300 import configs, engine as E
-from oracle import oracle as O
+from table_invariants import table_violations
 
 pytestmark = pytest.mark.gpu
 
@@ -45,19 +46,7 @@ def test_full_size_batch_invariants(config, steps):
     picks += [1, wl.n // 2, wl.n - 1]
     for i in sorted(set(picks))[:8]:
         s = slots[i]
-        lat = pool.lattice(s)
         as1, as2 = pool.tables(s)
-        ns = pool.nr_of_sites(s)
-        for p in range(P):
-            n = int(ns[p])
-            listed = as1[p][1:n + 1]
-            assert (listed >= 1).all() and (as1[p][n + 1:] == 0).all()
-            assert (as2[p][listed] == np.arange(1, n + 1)).all()
-            assert int((as2[p][1:] != 0).sum()) == n
-        o = O.Oracle(wl.program, wl.sizes[i], seed=1)
-        rb = o.rebuild_tables(lat)
-        for p in range(P):
-            got = set(as1[p][1:int(ns[p]) + 1].tolist())
-            want = set(rb["as1"][p][1:int(rb["nsites"][p]) + 1].tolist())
-            assert got == want, (config, i, p)
+        bad = table_violations(wl.program, wl.sizes[i], pool.lattice(s), as1, as2, pool.nr_of_sites(s))
+        assert bad == [], (config, i, bad[:3])
     pool.close()
