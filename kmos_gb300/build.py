@@ -34,12 +34,14 @@ def needs_build() -> bool:
     return any(os.path.getmtime(d) > t for d in DEPS)
 
 
-def build(force: bool = False, verbose: bool = False, phase_timing: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, phase_timing: bool = False, debug: bool = False) -> str:
     """Builds the library (``phase_timing``: a separate libkmcgb300_timing.so with the
-    step kernel's per-phase cycle accounting compiled in).  Translation units compile in
-    parallel, then link into one shared object."""
-    lib = LIB.replace(".so", "_timing.so") if phase_timing else LIB
-    if not force and not phase_timing and not needs_build():
+    step kernel's per-phase cycle accounting compiled in; ``debug``: a separate
+    libkmcgb300_debug.so whose kernels check every table and lattice index they compute
+    from table contents, KMC_DEBUG).  Translation units compile in parallel, then link
+    into one shared object."""
+    lib = LIB.replace(".so", "_timing.so") if phase_timing else LIB.replace(".so", "_debug.so") if debug else LIB
+    if not force and not phase_timing and not debug and not needs_build():
         return LIB
     flags = [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
              "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include")]
@@ -47,6 +49,8 @@ def build(force: bool = False, verbose: bool = False, phase_timing: bool = False
         flags.insert(0, "-Xptxas=-v")
     if phase_timing:
         flags.insert(0, "-DKMC_PHASE_TIMING")
+    if debug:
+        flags.insert(0, "-DKMC_DEBUG")
     with tempfile.TemporaryDirectory(prefix="kmcgb300_") as tmpdir:
         objs, procs = [], []
         for src in SOURCES:

@@ -24,6 +24,16 @@ enum Status {
 
 enum Rng { RNG_GFORTRAN = 0, RNG_PHILOX = 1 };
 
+// Every table and lattice index a step computes from table contents is checked in builds
+// with KMC_DEBUG: out of range, the step stops with ST_TABLE instead of touching memory
+// outside its slot.  The device-side counterpart of the host's program and state checks
+// (which make these indices in range by construction); off in the product build.
+#ifdef KMC_DEBUG
+#define KMC_IN(x, lo, hi) ((x) >= (lo) && (x) <= (hi))
+#else
+#define KMC_IN(x, lo, hi) true
+#endif
+
 struct ModelDev {
   const int32_t *prog;
   int32_t len, backend, P, nspecies, null_species, spuck, ngroups;
@@ -221,6 +231,7 @@ __device__ inline void add_proc(View &v, int p, int site) {
   if (p == 0) return;
   int32_t *a1 = v.as1 + (size_t)(p - 1) * v.stride;
   int32_t *a2 = v.as2 + (size_t)(p - 1) * v.stride;
+  if (!KMC_IN(site, 1, v.stride - 1)) { v.err = ST_TABLE; return; }
   if (v.collect) { a2[site] = 1; return; }
   const int n = v.ns[p - 1] + 1;
   // a list can hold every site once; more entries mean the tables no longer match the
@@ -237,11 +248,14 @@ __device__ inline void del_proc(View &v, int p, int site) {
   if (p == 0) return;
   int32_t *a1 = v.as1 + (size_t)(p - 1) * v.stride;
   int32_t *a2 = v.as2 + (size_t)(p - 1) * v.stride;
+  if (!KMC_IN(site, 1, v.stride - 1)) { v.err = ST_TABLE; return; }
   const int m = a2[site];
   if (m == 0) { v.err = ST_TABLE; return; }
   const int n = v.ns[p - 1];
+  if (!KMC_IN(n, m, v.stride - 1)) { v.err = ST_TABLE; return; }
   if (m < n) {
     const int last = a1[n];
+    if (!KMC_IN(last, 1, v.stride - 1)) { v.err = ST_TABLE; return; }
     a1[m] = last;
     a1[n] = 0;
     a2[last] = m;

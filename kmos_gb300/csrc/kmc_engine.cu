@@ -96,6 +96,7 @@ __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R],
   int32_t *a1 = v.as1 + row;
   int32_t *a2 = v.as2 + row;
   const int n0 = ns[p];
+  if (!KMC_IN(n0, 0, v.stride - 1)) return ST_TABLE;
   const int lane = threadIdx.x & 31;
   uint32_t bits[R];
 #pragma unroll
@@ -164,11 +165,13 @@ __device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R],
         if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
         continue;                            // guarded del of an absent entry
       }
+      if (!KMC_IN(m, 1, n)) return ST_TABLE;
       if (m < n) {
         int last;
         if (!logok) last = a1[n];
         else if (nlog == 0 || !logged(0, n, last))
           last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
+        if (!KMC_IN(last, 1, v.stride - 1)) return ST_TABLE;
         put(0, m, last);
         a1[n] = 0;  // vacated top entry: read again only after an add (logged) refills it
         put(1, last, m);
@@ -203,16 +206,21 @@ __device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32
   // 1. gather every slot (all lattice loads in flight together); check the old species
   //    of first replaces
   int32_t lvv[FAST_SLOTS / 32];
+  bool off_lattice = false;  // (KMC_DEBUG builds)
 #pragma unroll
   for (int rr = 0; rr < FAST_SLOTS / 32; rr++) {
     const int i = lane + 32 * rr;
     lvv[rr] = 0;
     if (i < nlat) {
-      const int site = v.g.site_near(bx, by, bz, coords[i]);
+      int site = v.g.site_near(bx, by, bz, coords[i]);
+      if (!KMC_IN(site, 1, v.stride - 1)) { site = 1; off_lattice = true; }
       f.latsite[i] = site;
       lvv[rr] = v.lat[site - 1];
     }
   }
+#ifdef KMC_DEBUG
+  if (__any_sync(0xffffffffu, off_lattice)) return ST_TABLE;
+#endif
   KMC_PHASE(sm, 11);
 #pragma unroll
   for (int rr = 0; rr < FAST_SLOTS / 32; rr++)
@@ -533,6 +541,7 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
       const int qe = (int)(qb >> 52) - 1023;
       int idx = (int)((((unsigned long long)qb & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - qe));
       if (idx > n) idx = n;
+      if (!KMC_IN(n, 1, S.V)) { status = ST_TABLE; break; }
 
 #pragma unroll
       for (int j = 0; j < NP; j++)

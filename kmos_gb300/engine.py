@@ -126,10 +126,12 @@ def library_path() -> str:
 
 
 def load(build_if_missing: bool = True, path: Optional[str] = None):
-    """Loads the engine library (building it first if it is missing or stale).  ``path``
-    selects another build of the same C-ABI (the phase-timing build)."""
+    """Loads the engine library (building it first if it is missing or stale).  ``path``,
+    or else the environment variable KMC_GB300_LIB, selects another build of the same
+    C-ABI (the phase-timing or the KMC_DEBUG build)."""
     global _lib
     if _lib is None:
+        path = path or os.environ.get("KMC_GB300_LIB") or None
         if path is None and build_if_missing and _build.needs_build():
             _build.build()
         lib = path or _build.LIB
