@@ -76,3 +76,25 @@ def test_export_writes_an_importable_model_directory(tmp_path):
         sys.path.remove(str(out))
         for mod in ("kmc_settings", "kmc_model"):
             sys.modules.pop(mod, None)
+
+
+def test_every_attribute_kmos_run_reads():
+    """The base / lattice / proclist attributes kmos.run and the kmos CLI read
+    (tests/golden/kmc_model_attrs.json, collected from their source by
+    tests/golden/make_kmc_model_attrs.py) are all there, for single- and multi-lattice
+    models under both backends -- except names from docstring examples (lattice_bridge,
+    site, co), the touchup_ prefix of an eval, the otf backend's rate-matrix calls, and
+    the lat_int-only backend / touchup_cell under local_smart (as in the f2py module)."""
+    import json
+    from conftest import GOLDEN, fixture_model
+    want = json.load(open(os.path.join(GOLDEN, "kmc_model_attrs.json")))
+    examples = {"lattice_bridge", "site", "co", "touchup_"}
+    otf = {"recalculate_rates_matrix", "update_chempot", "update_user_parameter"}
+    for name in ("CO_oxidation_Ruo2", "pdopd_xml"):
+        for backend in ("local_smart", "lat_int"):
+            base, lattice, proclist = kmc_model.configure(fixture_model(name), backend)
+            objs = {"base": base, "lattice": lattice, "proclist": proclist}
+            for mod, obj in objs.items():
+                skip = examples | otf | ({"backend", "touchup_cell"} if backend == "local_smart" else set())
+                missing = [a for a in want[mod] if a not in skip and not hasattr(obj, a)]
+                assert not missing, (name, backend, mod, missing)
