@@ -53,6 +53,17 @@ class Condition:
     implicit: bool = False
 
 
+@dataclass(frozen=True)
+class Bystander:
+    """A site whose species changes an otf process's rate but not whether it can run
+    (kmos/types.py:2160-2200): each ``allowed_species`` found at ``coord`` counts one
+    towards ``nr_<species>_<flag>``."""
+
+    allowed_species: Tuple[str, ...]
+    coord: Coord
+    flag: str = ""
+
+
 @dataclass
 class Process:
     name: str
@@ -61,6 +72,8 @@ class Process:
     actions: List[Condition] = field(default_factory=list)
     enabled: bool = True
     tof_count: Optional[Dict[str, float]] = None
+    bystanders: List[Bystander] = field(default_factory=list)
+    otf_rate: Optional[str] = None   # otf backend: the rate at a site, from base_rate and bystanders
 
     def executing_coord(self) -> Coord:
         """kmos ``Process.executing_coord`` (kmos/types.py:2094-2097): the action
@@ -280,6 +293,14 @@ def load_ini(path_or_text: str) -> Model:
             for term in [t.strip() for t in get("conditions").split("+")]:
                 sp, co = term.split("@")
                 proc.conditions.append(Condition(sp.strip(), _ini_coord(co, first_layer)))
+            otf = get("otf_rate")
+            proc.otf_rate = None if otf is None or otf.strip() == "None" else otf
+            if get("bystanders"):
+                # allowed@coord|flag (kmos/types.py:855-890), allowed a Python list literal
+                for term in [t.strip() for t in get("bystanders").split("+")]:
+                    allowed, co = term.split("@")
+                    co, flag = co.split("|")
+                    proc.bystanders.append(Bystander(tuple(_literal(allowed)), _ini_coord(co, first_layer), flag.strip()))
             processes.append(proc)
         elif section == "SpeciesList":
             default_species = get("default_species", "")
@@ -366,8 +387,16 @@ def load_xml(path: str) -> Model:
                     rate_constant=p.attrib["rate_constant"],
                     enabled=enabled.strip() not in ("False", "0"),
                     tof_count=_parse_tof_count(p.attrib.get("tof_count")),
+                    otf_rate=p.attrib.get("otf_rate"),
                 )
                 for sub in p:
+                    if sub.tag == "bystander":
+                        proc.bystanders.append(Bystander(
+                            tuple(sub.attrib["allowed_species"].split()),
+                            Coord(sub.attrib["coord_name"], tuple(int(v) for v in sub.attrib["coord_offset"].split()),
+                                  sub.attrib["coord_layer"]),
+                            sub.attrib.get("flag", "")))
+                        continue
                     if sub.tag not in ("action", "condition"):
                         continue
                     coord = Coord(
@@ -427,6 +456,9 @@ def from_project(project) -> Model:
                      for a in p.action_list],
             enabled=bool(getattr(p, "enabled", True)),
             tof_count=_parse_tof_count(getattr(p, "tof_count", None)),
+            bystanders=[Bystander(tuple(b.allowed_species), coord(b.coord), b.flag or "")
+                        for b in getattr(p, "bystander_list", [])],
+            otf_rate=getattr(p, "otf_rate", None),
         ))
     meta = {}
     for k in ("author", "email", "model_name", "model_dimension", "debug"):
@@ -461,6 +493,17 @@ def to_dict(model: Model) -> dict:
             d["implicit"] = True
         return d
 
+    def proc(p: Process):
+        d = {"name": p.name, "rate_constant": p.rate_constant, "enabled": p.enabled,
+             "tof_count": p.tof_count, "conditions": [cd(c) for c in p.conditions],
+             "actions": [cd(a) for a in p.actions]}
+        if p.bystanders:
+            d["bystanders"] = [{"allowed_species": list(b.allowed_species), "flag": b.flag,
+                                "coord": [b.coord.name, list(b.coord.offset), b.coord.layer]} for b in p.bystanders]
+        if p.otf_rate is not None:
+            d["otf_rate"] = p.otf_rate
+        return d
+
     return {
         "name": model.name,
         "dimension": model.dimension,
@@ -472,18 +515,19 @@ def to_dict(model: Model) -> dict:
         "substrate_layer": model.substrate_layer,
         "cell": [list(r) for r in model.cell],
         "parameters": [[p.name, p.value, p.adjustable, p.min, p.max, p.scale] for p in model.parameters],
-        "processes": [{"name": p.name, "rate_constant": p.rate_constant, "enabled": p.enabled,
-                       "tof_count": p.tof_count, "conditions": [cd(c) for c in p.conditions],
-                       "actions": [cd(a) for a in p.actions]} for p in model.processes],
+        "processes": [proc(p) for p in model.processes],
         "meta": dict(model.meta),
         "representations": dict(model.representations),
     }
 
 
 def from_dict(d: dict) -> Model:
-    def cd(x):
+    def co(x):
         n, off, lay = x["coord"]
-        return Condition(x["species"], Coord(n, tuple(int(v) for v in off), lay), bool(x.get("implicit", False)))
+        return Coord(n, tuple(int(v) for v in off), lay)
+
+    def cd(x):
+        return Condition(x["species"], co(x), bool(x.get("implicit", False)))
 
     return Model(
         name=d["name"],
@@ -496,7 +540,9 @@ def from_dict(d: dict) -> Model:
         cell=tuple(tuple(r) for r in d["cell"]),
         parameters=[Parameter(*p) for p in d["parameters"]],
         processes=[Process(p["name"], p["rate_constant"], [cd(c) for c in p["conditions"]],
-                           [cd(a) for a in p["actions"]], p.get("enabled", True), p.get("tof_count"))
+                           [cd(a) for a in p["actions"]], p.get("enabled", True), p.get("tof_count"),
+                           [Bystander(tuple(b["allowed_species"]), co(b), b.get("flag", ""))
+                            for b in p.get("bystanders", [])], p.get("otf_rate"))
                    for p in d["processes"]],
         meta=dict(d.get("meta", {})),
         representations=dict(d.get("representations", {})),

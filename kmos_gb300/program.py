@@ -115,7 +115,7 @@ from .model import Condition, Coord, Model, Process
 
 MAGIC = 0x4B4D4331
 VERSION = 1
-BACKENDS = {"local_smart": 0, "lat_int": 1}
+BACKENDS = {"local_smart": 0, "lat_int": 1, "otf": 2}
 
 OP_END = 0
 OP_REPLACE = 1
@@ -124,6 +124,7 @@ OP_ADD = 3
 OP_LI_DEL = 4
 OP_LI_ADD = 5
 OP_STRIP = 6
+OP_UPDATE = 7   # otf: if can_do(proc, site): update_rates_matrix with the rate re-evaluated
 
 HEADER_WORDS = 24
 FAST_MAX_SLOTS = 128
@@ -521,6 +522,8 @@ class ProgramBuilder:
                 w.emit(op_header(OP_LI_ADD, 0, op[1]), pack_coord(*op[2]))
             elif kind == "strip":
                 w.emit(op_header(OP_STRIP), pack_coord(*op[1]))
+            elif kind == "update":
+                w.emit(op_header(OP_UPDATE, 0, op[1]), pack_coord(*op[2]))
             else:
                 raise AssertionError(kind)
         w.emit(OP_END)
@@ -664,6 +667,8 @@ class ProgramBuilder:
         site_layer = [m.layer_ids()[ln] for ln, _s in m.site_list()]
         site_default = [self.species_id(m.site_default_species(s)) for _ln, s in m.site_list()]
         ngroups = 0
+        if self.backend == "otf":
+            return self._build_otf(w, site_layer, site_default)
         if self.backend == "local_smart":
             proc_streams, touch_streams = self.local_smart_streams()
             # add conditions carry species names; resolve them to masks
@@ -770,6 +775,60 @@ class ProgramBuilder:
         return Program(self.model, self.backend, arr)
 
 
+    def _build_otf(self, w: _Writer, site_layer, site_default) -> "Program":
+        """Program of the otf backend (kmos_gb300/otf.py): per-process streams, the
+        cell touch-up, one rate record per process; no fast streams."""
+        from . import otf
+        m = self.model
+        P = len(m.processes)
+
+        def resolve(stream):
+            out = []
+            for op in stream:
+                if op[0] == "replace":
+                    out.append(("replace", op[1], op[2], self.species_id(op[3])))
+                elif op[0] == "add":
+                    out.append(("add", op[1], op[2], tuple((c, self.mask_of(s)) for c, s in op[3])))
+                else:
+                    out.append(op)
+            return out
+
+        proc_streams = [resolve(otf.process_ops(m, proc, self.site_ids, self.mask_of)) for proc in m.processes]
+        touch = resolve(otf.touchup_ops(m, self.site_ids))
+        off_proc = len(w.words)
+        w.emit(*([0] * (P + 1)))
+        off_touch = len(w.words)
+        w.emit(0, 0)
+        off_groups = len(w.words)
+        w.emit(0)
+        off_site_layer = len(w.words)
+        w.emit(*site_layer)
+        off_site_default = len(w.words)
+        w.emit(*site_default)
+        max_ops = 0
+        for p, stream in enumerate(proc_streams):
+            w.words[off_proc + p] = len(w.words)
+            max_ops = max(max_ops, self._encode(stream, w))
+        w.words[off_proc + P] = len(w.words)
+        w.words[off_touch] = len(w.words)
+        self._encode(touch, w)
+        w.words[off_touch + 1] = len(w.words)
+        off_rate = len(w.words)
+        w.emit(*([0] * (P + 1)))
+        for p, proc in enumerate(m.processes):
+            w.words[off_rate + p] = len(w.words)
+            w.emit(*otf.rate_record(m, proc, self.species_id, self.site_ids))
+        w.words[off_rate + P] = len(w.words)
+        header = [MAGIC, VERSION, BACKENDS["otf"], P, len(m.species), self.null, m.spuck,
+                  m.dimension, 0, len(m.layers), off_proc, off_touch, off_groups,
+                  off_site_layer, off_site_default, 0, max_ops, 0, 0, 0, 0, 0,
+                  off_rate, len(m.parameters)]
+        w.words[:len(header)] = header
+        w.words[15] = len(w.words)
+        arr = np.array([x if x < 2**31 else x - 2**32 for x in w.words], dtype=np.int64).astype(np.int32)
+        return Program(self.model, self.backend, arr)
+
+
 @dataclass
 class Program:
     model: Model
@@ -815,6 +874,9 @@ def decode_stream(words: np.ndarray, pos: int) -> List[tuple]:
             pos += 2
         elif op == OP_STRIP:
             ops.append(("strip", unpack_coord(int(words[pos + 1]))))
+            pos += 2
+        elif op == OP_UPDATE:
+            ops.append(("update", arg, unpack_coord(int(words[pos + 1]))))
             pos += 2
         else:
             raise ValueError("bad op %d at %d" % (op, pos))

@@ -347,3 +347,97 @@ def tree_coords(tree, out=None):
         for _k, sub in tree[2]:
             tree_coords(sub, out)
     return out
+
+
+# ------------------------------------------------------------------------------ otf
+def _otf_body_ops(body, const):
+    """Ops of a run_proc_<name>(cell) or touchup_cell body of the otf generator
+    (kmos/io/__init__.py:3240-3597): guarded dels and rate updates, replaces, adds under
+    select-case paths.  Coordinates are relative to the process's cell."""
+    ops, stack, i = [], [], 0
+
+    def coord(text):
+        base, off, e = parse_coord(text, const)
+        if base != "cell":
+            raise ValueError(text)
+        return off + (e,)
+
+    while i < len(body):
+        line = body[i]
+        low = line.lower().replace(" ", "")
+        m = re.match(r"^if\(can_do\((\w+),(cell\+\(/.*/\))\)\)then$", low)
+        if m:
+            proc, target = const[m.group(1)], coord(m.group(2))
+            name, args = _call(body[i + 1].lower())
+            if name == "del_proc":
+                ops.append(("gdel", proc, target))
+            elif name == "update_rates_matrix":
+                ops.append(("update", proc, target))
+            else:
+                raise ValueError(body[i + 1])
+            assert body[i + 2].lower().replace(" ", "") == "endif", body[i + 2]
+            i += 3
+            continue
+        name, args = _call(line.lower())
+        if name == "replace_species":
+            old = species_mask([args[1]], const)
+            ops.append(("replace", coord(args[0]), old, const[args[2].strip()]))
+        elif name == "add_proc":
+            conds = sorted((c, mk) for c, mk in stack)
+            ops.append(("add", const[args[0].strip()], coord(args[1]), conds))
+        elif low.startswith("selectcase(get_species("):
+            inner = re.match(r"select case\(get_species\((.*)\)\)$", line.lower()).group(1)
+            stack.append([coord(inner), None])
+        elif low.startswith("case("):
+            stack[-1][1] = species_mask(_split_args(re.match(r"case\((.*)\)$", low).group(1)), const)
+        elif low.startswith("endselect"):
+            stack.pop()
+        elif low.startswith("site=cell+") or low.startswith("doproc_nr=1") or low.startswith("enddo"):
+            pass
+        elif low.startswith("if(avail_sites(proc_nr") or low.startswith("calldel_proc(proc_nr") or low == "endif":
+            pass  # touchup_cell's strip loop
+        elif name is None and low not in ("return",):
+            raise ValueError("unrecognised line %r" % line)
+        i += 1
+    return ops
+
+
+def otf_ops(directory):
+    """{'procs': {proc: ops}, 'touchups': {'1': ops}, 'rates': {proc: rate function}}
+    from an otf export (proclist.f90, run_proc_*.f90, proclist_pars.f90)."""
+    texts = {os.path.basename(f): open(f).read() for f in glob.glob(os.path.join(directory, "*.f90"))}
+    const = parse_constants([texts["proclist_constants.f90"], texts["lattice.f90"]])
+    procs = {}
+    for fname, text in texts.items():
+        if not fname.startswith("run_proc_"):
+            continue
+        for sub, body in subroutines(text).items():
+            procs[const[sub[len("run_proc_"):]]] = _otf_body_ops(body, const)
+    touch = _otf_body_ops(subroutines(texts["proclist.f90"])["touchup_cell"], const)
+    touch = [("strip", (0, 0, 0, 1))] + touch
+    pars = subroutines(texts["proclist_pars.f90"])
+    rates = {}
+    for sub, body in pars.items():
+        if not sub.startswith("gr_"):
+            continue
+        name = sub[3:]
+        byst, cur = [], None
+        for line in body:
+            low = line.lower().replace(" ", "")
+            m = re.match(r"^selectcase\(get_species\((cell\+\(/.*/\))\)\)$", low)
+            if m:
+                base, off, e = parse_coord(m.group(1), const)
+                cur = [off + (e,), []]
+                byst.append(cur)
+                continue
+            m = re.match(r"^case\((\w+)\)$", low)
+            if m:
+                spec = const[m.group(1)]
+                continue
+            m = re.match(r"^nr_vars\((\d+)\)=nr_vars\(\d+\)\+1$", low)
+            if m:
+                cur[1].append((spec, int(m.group(1)) - 1))
+        expr = " ".join(pars["rate_" + name])
+        m = re.search(r"rate_%s\s*=\s*(.*?)\s*return" % name, expr, re.I)
+        rates[const[name]] = {"bystanders": byst, "expr": m.group(1) if m else ""}
+    return {"procs": procs, "touchups": {"1": touch}, "rates": rates}

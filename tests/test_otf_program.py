@@ -1,0 +1,126 @@
+"""The otf backend's program against the reference's own golden otf exports
+(tests/golden/ops/*_otf.json, made by tests/golden/make_otf_golden.py from
+tests/export_test/reference_export_intZGB_otf and reference_export_otf): the op order of
+every run_proc_<name> (guarded dels, replaces, rate updates, adds with their select-case
+conditions), the cell touch-up, and every gr_<name> function -- which bystander species
+count towards which nr variable, and the rate expression, compiled from the generated
+Fortran's own text, giving the same rate program as the model's otf_rate.  Plus the
+expression semantics: Fortran typing and libgcc's integer powering."""
+import json
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, fixture_model
+from kmos_gb300 import otf as OTF, program as PG
+
+CASES = [("intZGB_otf", "intZGB_otf_otf.json"), ("default_xml", "default_xml_otf.json")]
+
+
+def norm(op):
+    if op[0] == "add":
+        return ["add", int(op[1]), list(op[2]), sorted([list(c), int(m)] for c, m in op[3])]
+    return [op[0]] + [list(x) if isinstance(x, (tuple, list)) else int(x) for x in op[1:]]
+
+
+@pytest.mark.parametrize("name,gold", CASES)
+def test_otf_op_order_matches_generated_fortran(name, gold):
+    g = json.load(open(os.path.join(GOLDEN, "ops", gold)))
+    prog = PG.compile_model(fixture_model(name), "otf")
+    assert set(int(p) for p in g["procs"]) == set(range(1, prog.nproc + 1))
+    for p, ops in g["procs"].items():
+        assert [norm(o) for o in prog.proc_stream(int(p))] == [norm(o) for o in ops], "process %s" % p
+    assert [norm(o) for o in prog.touchup_stream(0)] == [norm(o) for o in g["touchups"]["1"]]
+
+
+def records(prog):
+    w = prog.words
+    off = int(w[22])
+    out = {}
+    for p in range(1, prog.nproc + 1):
+        r = int(w[off + p - 1])
+        nb, nv, nc = int(w[r]), int(w[r + 1]), int(w[r + 2])
+        pos, byst = r + 4, []
+        for _ in range(nb):
+            coord, npairs = PG.unpack_coord(int(w[pos])), int(w[pos + 1])
+            pairs = [[int(w[pos + 2 + 2 * j]), int(w[pos + 3 + 2 * j])] for j in range(npairs)]
+            byst.append([list(coord), pairs])
+            pos += 2 + 2 * npairs
+        out[p] = (nv, byst, [int(x) for x in w[pos:pos + nc]])
+        assert pos + nc <= int(w[off + p]) if p < prog.nproc else True
+    return out
+
+
+@pytest.mark.parametrize("name,gold", CASES)
+def test_rate_functions_match_generated_fortran(name, gold):
+    g = json.load(open(os.path.join(GOLDEN, "ops", gold)))
+    model = fixture_model(name)
+    prog = PG.compile_model(model, "otf")
+    recs = records(prog)
+    pid = model.process_ids()
+    for p, ref in g["rates"].items():
+        nv, byst, code = recs[int(p)]
+        assert byst == ref["bystanders"], "process %s" % p
+        proc = model.processes[int(p) - 1]
+        names = OTF.nr_var_names(proc)
+        assert len(names) == nv
+        # the generated Fortran's rate expression, read back into otf_rate syntax
+        text = ref["expr"].replace("&", " ")
+        text = re.sub(r"rates\s*\(\s*\w+\s*\)", "base_rate", text)
+        text = re.sub(r"userpar\s*\(\s*(\w+)\s*\)", r"\1", text)
+        text = re.sub(r"nr_vars\s*\(\s*(\d+)\s*\)", lambda m: names[int(m.group(1)) - 1], text)
+        from kmos_gb300.model import Process
+        twin = Process(proc.name, proc.rate_constant, bystanders=proc.bystanders, otf_rate=text)
+        assert OTF.compile_rate(model, twin)[1] == code, "process %s: %s" % (p, text)
+    assert pid  # numbering is the model's file order
+
+
+def run(expr, base=2.0, par=None, nr=None, model=None):
+    from kmos_gb300.model import Bystander, Coord, Parameter, Process
+    model = model or fixture_model("intZGB_otf")
+    proc = Process("p", "1", bystanders=[Bystander(("O", "CO"), Coord("default", (1, 0, 0), "square"), "f")],
+                   otf_rate=expr)
+    _names, code, _d = OTF.compile_rate(model, proc)
+    par = par if par is not None else [1.5, 0.75, 3.0, 1e-10, 0.5]
+    return OTF.evaluate(code, base, par, nr or [2, 3])
+
+
+def test_expression_semantics():
+    # integer arithmetic stays integer (truncating division) until it meets a real
+    assert run("7/2") == 3.0 and run("-7/2") == -3.0 and run("7/2.0") == 3.5
+    # a real literal is single precision: 0.1 is the float32 value widened
+    assert run("0.1") == float(np.float32(0.1)) and run("0.1d0") == 0.1
+    assert run("base_rate*0.1") == 2.0 * float(np.float32(0.1))
+    # real ** integer by libgcc's binary powering, the reciprocal for negative powers
+    x = 1.1
+    assert run("J_CO_CO**nr_CO_f", par=[x, 0, 0, 0, 0], nr=[5, 0]) == x * ((x * x) * (x * x))
+    assert run("J_CO_CO**(-nr_CO_f)", par=[x, 0, 0, 0, 0], nr=[3, 0]) == 1.0 / (x * (x * x))
+    assert run("J_CO_CO**0", par=[x, 0, 0, 0, 0]) == 1.0
+    # integer ** integer
+    assert run("2**nr_O_f", nr=[0, 10]) == 1024.0
+    # Fortran precedence: unary minus below **, ** right-associative
+    assert run("-2.0d0**2") == -4.0 and run("2**3**2") == 512.0
+    # multi-line expressions with auxiliary (real(8)) variables
+    assert run("a = base_rate*3\notf_rate = a/2") == 3.0
+    # unit constants are the single-precision literal of their %.10e value
+    assert run("kboltzmann") == float(np.float32(float("%.10e" % 1.3806488e-23)))
+    assert math.isclose(run("exp(-J_O_CO)"), math.exp(-0.75), rel_tol=0, abs_tol=0)
+
+
+def test_intzgb_rates_equal_the_formula():
+    model = fixture_model("intZGB_otf")
+    prog = PG.compile_model(model, "otf")
+    recs = records(prog)
+    par = OTF.user_parameter_values(model)
+    assert OTF.user_parameters(model) == ["J_CO_CO", "J_O_CO", "J_O_O", "kDes", "yCO"]
+    par = [1.3, 0.7, 1.9, 1e-10, 0.5]
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        nco, no = (int(v) for v in rng.integers(0, 5, 2))
+        # CO_ads: base * J_O_CO**nr_O_1nn * J_CO_CO**nr_CO_1nn, nr_vars sorted (CO, O)
+        got = OTF.evaluate(recs[1][2], 0.25, par, [nco, no])
+        want = (0.25 * OTF.powi(0.7, no, OTF.K_F64)) * OTF.powi(1.3, nco, OTF.K_F64)
+        assert got == want
