@@ -22,6 +22,15 @@
  *                        get_next_kmc_step (which uses the *time* draw as the site draw)
  *   proclist_generic_subroutines.mpy:113-158 get_occupation
  *   proclist_generic_subroutines.mpy:236-304 initialize_state (reset, defaults, touch-ups)
+ * and, for the otf backend (backend 2), kmos/fortran_src/base_otf.f90:
+ *   221-283 del_proc (the entry's rate moves with it)    286-331 add_proc (with a rate)
+ *   333-364 update_rates_matrix     366-387 reaccumulate_rates_matrix
+ *   687-716 update_accum_rate (each list re-summed left to right every step)
+ *   719-738 update_integ_rate       1213-1277 determine_procsite (process, then the
+ *   entry from the running sum of the chosen list)
+ * with the generated gr_<name> rate functions (kmos/io/__init__.py:2657-2965) run from
+ * the rate programs of kmos_gb300/otf.py by an evaluator written here (otf_eval), the
+ * cell touch-up (io:3240-3285) and recalculate_rates_matrix (io:3786-3830).
  * The process-specific code (generated proclist.f90 / run_proc_*.f90 / nli_*.f90) is
  * taken from the op program that kmos_gb300.program compiles; the op semantics below
  * follow kmos/io/__init__.py:305-465, 1732-2057, 2219-2655.
@@ -60,7 +69,8 @@
 #define ORACLE_RNG_GFORTRAN 0
 #define ORACLE_RNG_PHILOX 1
 
-enum { OP_END = 0, OP_REPLACE = 1, OP_GDEL = 2, OP_ADD = 3, OP_LI_DEL = 4, OP_LI_ADD = 5, OP_STRIP = 6 };
+enum { OP_END = 0, OP_REPLACE = 1, OP_GDEL = 2, OP_ADD = 3, OP_LI_DEL = 4, OP_LI_ADD = 5, OP_STRIP = 6,
+       OP_UPDATE = 7 };
 
 typedef struct {
     /* program */
@@ -86,6 +96,10 @@ typedef struct {
      * (add_proc, del_proc, can_do) and occupation reads/writes, as the Fortran does them */
     int64_t n_as, n_occ;
     int err;
+    /* otf: rates_matrix(P, V+1) column-major like avail_sites, user parameters,
+     * the rate-record table and the running-sum scratch of determine_procsite */
+    double *rm, *userpar, *accum_proc;
+    int nuser, off_rate;
 } oracle_t;
 
 /* ----------------------------------------------------------------- random numbers */
@@ -164,8 +178,13 @@ static void lat_set(oracle_t *o, int site, int s) { o->n_occ++; o->lattice[site 
 
 static int can_do(oracle_t *o, int p, int site) { o->n_as++; return AS(o, p, site, 2) != 0; }
 
+#define RM(o, p, i) (o)->rm[((p) - 1) + (int64_t)(o)->P * ((i) - 1)]
+
+static void add_proc_rate(oracle_t *o, int p, int site, double rate);
+
 static void add_proc(oracle_t *o, int p, int site)
 {
+    if (o->backend == 2) { add_proc_rate(o, p, site, 0.0); return; }
     if (o->backend == 1 && p == 0) return; /* lat_int: nli found no member */
     if (AS(o, p, site, 2) != 0) { o->err = ORACLE_ERR_TABLE; return; }
     o->nr_of_sites[p - 1] += 1;
@@ -184,15 +203,43 @@ static void del_proc(oracle_t *o, int p, int site)
     if (m < n) {
         AS(o, p, m, 1) = AS(o, p, n, 1);
         AS(o, p, n, 1) = 0;
+        if (o->backend == 2) {
+            RM(o, p, o->V + 1) = RM(o, p, o->V + 1) - RM(o, p, m);
+            RM(o, p, m) = RM(o, p, n);
+            RM(o, p, n) = 0.0;
+        }
         AS(o, p, AS(o, p, m, 1), 2) = m;
         o->n_as += 5;
     } else {
         AS(o, p, m, 1) = 0;
+        if (o->backend == 2) {
+            RM(o, p, o->V + 1) = RM(o, p, o->V + 1) - RM(o, p, m);
+            RM(o, p, m) = 0.0;
+        }
         o->n_as += 1;
     }
     AS(o, p, site, 2) = 0;
     o->nr_of_sites[p - 1] = n - 1;
     o->n_as += 2;
+}
+
+static void add_proc_rate(oracle_t *o, int p, int site, double rate)
+{
+    if (AS(o, p, site, 2) != 0) { o->err = ORACLE_ERR_TABLE; return; }
+    o->nr_of_sites[p - 1] += 1;
+    int n = o->nr_of_sites[p - 1];
+    AS(o, p, n, 1) = site;
+    AS(o, p, site, 2) = n;
+    RM(o, p, o->V + 1) = RM(o, p, o->V + 1) + rate;
+    RM(o, p, n) = rate;
+}
+
+static void update_rates_matrix(oracle_t *o, int p, int site, double rate)
+{
+    int m = AS(o, p, site, 2);
+    if (m == 0) { o->err = ORACLE_ERR_TABLE; return; }
+    RM(o, p, o->V + 1) = RM(o, p, o->V + 1) + rate - RM(o, p, m);
+    RM(o, p, m) = rate;
 }
 
 /* -------------------------------------------------------------- lattice mapping */
@@ -254,6 +301,115 @@ static int nli(oracle_t *o, int g, int cx, int cy, int cz)
     return result;
 }
 
+/* --------------------------------------------------------- otf rate programs */
+enum { I_END = 0, I_PUSH_BASE = 1, I_PUSH_PAR = 2, I_PUSH_NR = 3, I_PUSH_INT = 4, I_PUSH_CONST = 5,
+       I_LOAD_AUX = 6, I_STORE_AUX = 7, I_STORE_RESULT = 8, I_ADD = 10, I_SUB, I_MUL, I_DIV, I_NEG,
+       I_POWI, I_POW, I_EXP, I_LOG, I_SQRT, I_ABS, I_CVT };
+enum { K_INT = 0, K_F32 = 1, K_F64 = 2 };
+
+static int32_t wrap32(int64_t v) { return (int32_t)(uint32_t)(uint64_t)v; }
+
+/* x ** m for an integer m: libgcc's __powidf2 / __powisf2 (right-to-left binary powering
+ * in the base's precision, the reciprocal for m < 0); gfortran's pow_i4_i4 for integers. */
+static double powi_kind(double xd, int32_t m, int kind)
+{
+    uint32_t n = m < 0 ? -(uint32_t)m : (uint32_t)m;
+    if (kind == K_F32) {
+        float x = (float)xd, y = (n % 2) ? x : 1.0f;
+        while (n >>= 1) { x = x * x; if (n % 2) y = y * x; }
+        return m < 0 ? (double)(1.0f / y) : (double)y;
+    }
+    if (kind == K_F64) {
+        double x = xd, y = (n % 2) ? x : 1.0;
+        while (n >>= 1) { x = x * x; if (n % 2) y = y * x; }
+        return m < 0 ? 1.0 / y : y;
+    }
+    int64_t x = (int64_t)xd, y = (n % 2) ? x : 1;
+    while (n >>= 1) { x = wrap32(x * x); if (n % 2) y = wrap32(y * x); }
+    if (m < 0) return (y == 1 || y == -1) ? (double)((-(int64_t)m) % 2 ? y : 1) : 0.0;
+    return (double)y;
+}
+
+/* Runs a rate program (kmos_gb300/otf.py) on the stack machine: values are held as
+ * doubles and rounded to their Fortran kind by each instruction. */
+static double otf_eval(oracle_t *o, const int32_t *code, double base, const int32_t *nr)
+{
+    double st[32], aux[8] = {0}, result = 0.0;
+    int sp = 0;
+    for (int pc = 0;;) {
+        uint32_t w = (uint32_t)code[pc++];
+        int op = w & 0xFF, kind = (w >> 8) & 0xFF, arg = (int)(w >> 16);
+        if (sp > 30) { o->err = ORACLE_ERR_PROGRAM; return 0.0; }
+        switch (op) {
+        case I_END: return result;
+        case I_PUSH_BASE: st[sp++] = base; break;
+        case I_PUSH_PAR: st[sp++] = arg < o->nuser ? o->userpar[arg] : 0.0; break;
+        case I_PUSH_NR: st[sp++] = (double)nr[arg]; break;
+        case I_PUSH_INT: st[sp++] = (double)code[pc++]; break;
+        case I_PUSH_CONST: {
+            uint64_t bits = (uint64_t)(uint32_t)code[pc] | ((uint64_t)(uint32_t)code[pc + 1] << 32);
+            double v;
+            memcpy(&v, &bits, 8);
+            st[sp++] = v;
+            pc += 2;
+            break;
+        }
+        case I_LOAD_AUX: st[sp++] = aux[arg & 7]; break;
+        case I_STORE_AUX: aux[arg & 7] = st[--sp]; break;
+        case I_STORE_RESULT: result = st[--sp]; break;
+        case I_ADD: case I_SUB: case I_MUL: case I_DIV: {
+            double b = st[--sp], a = st[sp - 1], r;
+            if (kind == K_INT) {
+                int64_t ia = (int64_t)a, ib = (int64_t)b;
+                r = op == I_ADD ? wrap32(ia + ib) : op == I_SUB ? wrap32(ia - ib) : op == I_MUL ? wrap32(ia * ib)
+                  : (ib == 0 ? 0 : wrap32(ia / ib));
+            } else if (kind == K_F32) {
+                float fa = (float)a, fb = (float)b;
+                r = op == I_ADD ? fa + fb : op == I_SUB ? fa - fb : op == I_MUL ? fa * fb : fa / fb;
+            } else {
+                r = op == I_ADD ? a + b : op == I_SUB ? a - b : op == I_MUL ? a * b : a / b;
+            }
+            st[sp - 1] = r;
+            break;
+        }
+        case I_NEG: st[sp - 1] = kind == K_INT ? (double)wrap32(-(int64_t)st[sp - 1]) : -st[sp - 1]; break;
+        case I_POWI: { double m = st[--sp]; st[sp - 1] = powi_kind(st[sp - 1], (int32_t)m, kind); break; }
+        case I_POW: {
+            double b = st[--sp], a = st[sp - 1];
+            st[sp - 1] = kind == K_F32 ? (double)powf((float)a, (float)b) : pow(a, b);
+            break;
+        }
+        case I_EXP: st[sp - 1] = kind == K_F32 ? (double)expf((float)st[sp - 1]) : exp(st[sp - 1]); break;
+        case I_LOG: st[sp - 1] = kind == K_F32 ? (double)logf((float)st[sp - 1]) : log(st[sp - 1]); break;
+        case I_SQRT: st[sp - 1] = kind == K_F32 ? (double)sqrtf((float)st[sp - 1]) : sqrt(st[sp - 1]); break;
+        case I_ABS: st[sp - 1] = fabs(st[sp - 1]); break;
+        case I_CVT:
+            if (kind == K_INT && arg == K_F32) st[sp - 1] = (double)(float)(int32_t)st[sp - 1];
+            break;  /* int -> double and float -> double are exact */
+        default: o->err = ORACLE_ERR_PROGRAM; return 0.0;
+        }
+    }
+}
+
+/* gr_<p>(cell) (kmos/io/__init__.py:2800-2965): count the bystanders' species into the
+ * nr variables, then the rate program with base_rate = rates(p). */
+static double gr(oracle_t *o, int p, int cx, int cy, int cz)
+{
+    const int32_t *r = o->prog + o->prog[o->off_rate + p - 1];
+    int nb = r[0], nv = r[1];
+    int32_t nr[64] = {0};
+    if (nv > 64) { o->err = ORACLE_ERR_PROGRAM; return 0.0; }
+    const int32_t *b = r + 4;
+    for (int k = 0; k < nb; k++) {
+        int sp = lat_get(o, coord_site(o, cx, cy, cz, b[0]));
+        int npairs = b[1];
+        for (int j = 0; j < npairs; j++)
+            if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
+        b += 2 + 2 * npairs;
+    }
+    return otf_eval(o, b, o->rates[p - 1], nr);
+}
+
 static void run_stream(oracle_t *o, int pos, int bx, int by, int bz)
 {
     const int32_t *w = o->prog;
@@ -284,8 +440,24 @@ static void run_stream(oracle_t *o, int pos, int bx, int by, int bz)
                 int s2 = coord_site(o, bx, by, bz, w[pos + 2 + 2 * c]);
                 ok = in_mask(lat_get(o, s2), w[pos + 3 + 2 * c]);
             }
-            if (ok) add_proc(o, arg, site);
+            if (ok) {
+                if (o->backend == 2) {
+                    int dx, dy, dz, n;
+                    unpack(w[pos + 1], &dx, &dy, &dz, &n);
+                    add_proc_rate(o, arg, site, gr(o, arg, bx + dx, by + dy, bz + dz));
+                } else {
+                    add_proc(o, arg, site);
+                }
+            }
             pos += 2 + 2 * cnt;
+            break;
+        }
+        case OP_UPDATE: {
+            int dx, dy, dz, n;
+            unpack(w[pos + 1], &dx, &dy, &dz, &n);
+            int site = lattice2nr(o, bx + dx, by + dy, bz + dz, n);
+            if (can_do(o, arg, site)) update_rates_matrix(o, arg, site, gr(o, arg, bx + dx, by + dy, bz + dz));
+            pos += 2;
             break;
         }
         case OP_LI_DEL:
@@ -315,6 +487,14 @@ static void run_stream(oracle_t *o, int pos, int bx, int by, int bz)
 /* ---------------------------------------------------------------- base routines */
 static void update_accum_rate(oracle_t *o)
 {
+    if (o->backend == 2) {  /* base_otf.f90:687-716 */
+        for (int i = 1; i <= o->P; i++) {
+            RM(o, i, o->V + 1) = 0.0;
+            for (int j = 1; j <= o->nr_of_sites[i - 1]; j++) RM(o, i, o->V + 1) = RM(o, i, o->V + 1) + RM(o, i, j);
+            o->accum_rates[i - 1] = i == 1 ? RM(o, 1, o->V + 1) : o->accum_rates[i - 2] + RM(o, i, o->V + 1);
+        }
+        return;
+    }
     o->accum_rates[0] = (double)o->nr_of_sites[0] * o->rates[0];
     for (int i = 1; i < o->P; i++)
         o->accum_rates[i] = o->accum_rates[i - 1] + (double)o->nr_of_sites[i] * o->rates[i];
@@ -322,6 +502,11 @@ static void update_accum_rate(oracle_t *o)
 
 static void update_integ_rate(oracle_t *o)
 {
+    if (o->backend == 2) {  /* base_otf.f90:719-738 */
+        for (int i = 0; i < o->P; i++)
+            o->integ_rates[i] = o->integ_rates[i] + RM(o, i + 1, o->V + 1) * o->kmc_time_step;
+        return;
+    }
     for (int i = 0; i < o->P; i++)
         o->integ_rates[i] = o->integ_rates[i] + (double)o->nr_of_sites[i] * o->rates[i] * o->kmc_time_step;
 }
@@ -360,6 +545,15 @@ static int determine_procsite(oracle_t *o, double ran_proc, double ran_site, int
     if (p == 0) return ORACLE_ERR_DEADLOCK;
     int n = o->nr_of_sites[p - 1];
     if (n <= 0) return ORACLE_ERR_DEADLOCK;
+    if (o->backend == 2) {  /* base_otf.f90:1213-1277 */
+        o->accum_proc[0] = RM(o, p, 1);
+        for (int i = 2; i <= n; i++) o->accum_proc[i - 1] = o->accum_proc[i - 2] + RM(o, p, i);
+        int k = interval_search_real(o->accum_proc, n, ran_site * o->accum_proc[n - 1]);
+        if (k == 0) return ORACLE_ERR_DEADLOCK;
+        *proc = p;
+        *site = AS(o, p, k, 1);
+        return ORACLE_OK;
+    }
     int idx = (int)(1.0 + ran_site * (double)n);
     if (idx > n) idx = n;
     *proc = p;
@@ -373,6 +567,7 @@ void oracle_destroy(oracle_t *o)
     if (!o) return;
     free(o->prog); free(o->lattice); free(o->avail_sites); free(o->nr_of_sites);
     free(o->rates); free(o->accum_rates); free(o->integ_rates); free(o->procstat);
+    free(o->rm); free(o->userpar); free(o->accum_proc);
     free(o);
 }
 
@@ -391,7 +586,7 @@ int oracle_touchup(oracle_t *o, int site)
     int x, y, z, n;
     if (site < 1 || site > o->V) return ORACLE_ERR_ARG;
     nr2lattice(o, site, &x, &y, &z, &n);
-    int idx = o->backend == 1 ? 0 : n - 1;
+    int idx = o->backend >= 1 ? 0 : n - 1;  /* lat_int: one touch-up per cell; otf: touchup_cell */
     run_stream(o, o->prog[o->off_touch + idx], x, y, z);
     return o->err;
 }
@@ -421,7 +616,7 @@ static int initialize_state(oracle_t *o, int layer)
     for (int k = 0; k < o->Z; k++)
         for (int j = 0; j < o->Y; j++)
             for (int i = 0; i < o->X; i++) {
-                if (o->backend == 1) {
+                if (o->backend >= 1) {
                     run_stream(o, o->prog[o->off_touch], i, j, k);
                 } else {
                     for (int nr = 1; nr <= o->spuck; nr++)
@@ -457,6 +652,13 @@ oracle_t *oracle_create(const int32_t *prog, int prog_len, int X, int Y, int Z, 
     o->accum_rates = (double *)calloc(o->P, sizeof(double));
     o->integ_rates = (double *)calloc(o->P, sizeof(double));
     o->procstat = (int64_t *)calloc(o->P, sizeof(int64_t));
+    if (o->backend == 2) {
+        o->off_rate = prog[22];
+        o->nuser = prog[23];
+        o->rm = (double *)calloc((size_t)o->P * (o->V + 1), sizeof(double));
+        o->userpar = (double *)calloc(o->nuser > 0 ? o->nuser : 1, sizeof(double));
+        o->accum_proc = (double *)calloc(o->V, sizeof(double));
+    }
     o->rng_kind = rng_kind;
     o->seed = (uint32_t)seed;
     o->traj = traj;
@@ -477,11 +679,12 @@ int oracle_rebuild_tables(oracle_t *o, const int32_t *lattice)
     for (int i = 0; i < o->V; i++) o->lattice[i] = lattice[i];
     memset(o->avail_sites, 0, sizeof(int32_t) * (size_t)o->P * o->V * 2);
     memset(o->nr_of_sites, 0, sizeof(int32_t) * o->P);
+    if (o->backend == 2) memset(o->rm, 0, sizeof(double) * (size_t)o->P * (o->V + 1));
     o->err = 0;
     for (int k = 0; k < o->Z; k++)
         for (int j = 0; j < o->Y; j++)
             for (int i = 0; i < o->X; i++) {
-                if (o->backend == 1) {
+                if (o->backend >= 1) {
                     run_stream(o, o->prog[o->off_touch], i, j, k);
                 } else {
                     for (int nr = 1; nr <= o->spuck; nr++) run_stream(o, o->prog[o->off_touch + nr - 1], i, j, k);
@@ -492,6 +695,33 @@ int oracle_rebuild_tables(oracle_t *o, const int32_t *lattice)
 }
 
 void oracle_set_rate_const(oracle_t *o, int proc, double rate) { o->rates[proc - 1] = rate; }
+
+/* otf: update_user_parameter (proclist_pars, io:2755-2762) */
+void oracle_set_user_parameter(oracle_t *o, int k, double v) { if (k >= 1 && k <= o->nuser) o->userpar[k - 1] = v; }
+
+/* otf: recalculate_rates_matrix (io:3786-3830): every available entry's rate re-evaluated,
+ * then reaccumulate_rates_matrix (base_otf.f90:366-387). */
+int oracle_recalculate_rates_matrix(oracle_t *o)
+{
+    if (o->backend != 2) return ORACLE_ERR_ARG;
+    for (int p = 1; p <= o->P; p++)
+        for (int i = 1; i <= o->nr_of_sites[p - 1]; i++) {
+            int x, y, z, n;
+            nr2lattice(o, AS(o, p, i, 1), &x, &y, &z, &n);
+            RM(o, p, i) = gr(o, p, x, y, z);
+        }
+    for (int p = 1; p <= o->P; p++) {
+        RM(o, p, o->V + 1) = 0.0;
+        for (int i = 1; i <= o->V; i++) {
+            if (AS(o, p, i, 1) > 0) RM(o, p, o->V + 1) = RM(o, p, o->V + 1) + RM(o, p, i);
+            else RM(o, p, i) = 0.0;
+        }
+    }
+    return o->err;
+}
+
+/* otf: get_rate (base_otf.f90:1121-1145): rates_matrix(p, idx), idx = V+1 the total */
+double oracle_get_rates_matrix(oracle_t *o, int p, int idx) { return o->backend == 2 ? RM(o, p, idx) : 0.0; }
 void oracle_update_accum_rate(oracle_t *o) { update_accum_rate(o); }
 void oracle_update_integ_rate(oracle_t *o) { update_integ_rate(o); }
 

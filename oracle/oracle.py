@@ -75,6 +75,10 @@ def lib():
         L.oracle_philox.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
         L.oracle_draws.argtypes = [vp, i64, ctypes.POINTER(dbl)]
         L.oracle_rebuild_tables.argtypes = [vp, P32]
+        L.oracle_set_user_parameter.argtypes = [vp, ctypes.c_int, dbl]
+        L.oracle_recalculate_rates_matrix.argtypes = [vp]
+        L.oracle_get_rates_matrix.restype = dbl
+        L.oracle_get_rates_matrix.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -124,6 +128,29 @@ class Oracle:
 
     def update_accum_rate(self):
         lib().oracle_update_accum_rate(self.h)
+
+    def update_integ_rate(self):
+        lib().oracle_update_integ_rate(self.h)
+
+    # otf backend
+    def set_user_parameters(self, values):
+        for k, v in enumerate(values, start=1):
+            lib().oracle_set_user_parameter(self.h, k, float(v))
+
+    def recalculate_rates_matrix(self):
+        self._check(lib().oracle_recalculate_rates_matrix(self.h))
+
+    def rates_matrix(self):
+        """[P][V+1]: rates_matrix(p, i) of list position i (index 0 unused), and the
+        process total rates_matrix(p, V+1) as a separate [P] vector."""
+        L, V = lib(), self.V
+        out = np.zeros((self.P, V + 1))
+        ns = self.nr_of_sites()
+        for p in range(1, self.P + 1):
+            for i in range(1, int(ns[p - 1]) + 1):
+                out[p - 1, i] = L.oracle_get_rates_matrix(self.h, p, i)
+        tot = np.array([L.oracle_get_rates_matrix(self.h, p, V + 1) for p in range(1, self.P + 1)])
+        return out, tot
 
     def do_kmc_steps(self, n):
         self._check(lib().oracle_do_kmc_steps(self.h, int(n)))
