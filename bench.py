@@ -68,6 +68,8 @@ def parse():
                     help="kMC steps per trajectory of the CPU sample (default: a 10-30 s sample per config)")
     ap.add_argument("--plain", type=int, default=1,
                     help="also time the plain drop-in: one trajectory of the workload through the handle API")
+    ap.add_argument("--otf", type=int, default=1,
+                    help="after the timed region: the otf backend on intZGB (kmc_otf_*)")
     ap.add_argument("--serving", type=int, default=1,
                     help="also run a short serving sample (configuration 5 stream, 1 s of arrivals, steps x 0.05)")
     return ap.parse_args()
@@ -390,6 +392,8 @@ def run_ours(args, dist: Dist):
         line["plain_dropin"] = plain_dropin(wl)
     if line is not None and args.serving and dist.world == 1:
         line["serving"] = serving_sample()
+    if line is not None and args.otf and dist.world == 1:
+        line["otf"] = otf_sample(args.cpu_baseline)
     if line is not None:
         print(json.dumps(line))
     dist.close()
@@ -429,6 +433,50 @@ def serving_sample():
     out = {"requests": len(reqs), "rate_per_s": 500.0, "duration_s": 1.0, "steps_scale": 0.05,
            "served_steps_per_s": srv.kmc_steps / wall, "wall_s": wall, **stats}
     srv.close()
+    return out
+
+
+def otf_sample(cpu: int = 1):
+    """The otf backend (per-entry rates from bystanders) after the timed region: intZGB
+    (tests/golden/models/intZGB_otf.json, the reference's tests/export_test/intZGB_otf.xml)
+    on a 32 x 32 lattice, 2048 Philox trajectories, steps/s over every trajectory from
+    CUDA events around one do_kmc_steps launch (inputs resident), beside the oracle's
+    single-core steps/s on one trajectory of the same configuration."""
+    from kmos_gb300 import engine as E, model as M, otf as OTF, program as PG
+    m = M.load_json(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "models",
+                                 "intZGB_otf.json"))
+    prog = PG.compile_model(m, "otf")
+    rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
+    params = [1.3, 0.7, 1.9, 1e-10, 0.5]
+    ntraj, size = 2048, (32, 32)
+    b = E.OtfBatch(prog, size, ntraj=ntraj, seed=11, rng=E.RNG_PHILOX)
+    b.set_rates(rates)
+    b.set_user_parameters(params)
+    b.recalculate_rates_matrix()
+    b.update_accum_rate()
+    b.do_kmc_steps(300)                       # warm-up: tables leave the initial state
+    b.do_kmc_steps(100)
+    ms100 = b.last_kernel_ms()
+    steps = max(100, min(20000, int(100 * 1500.0 / max(ms100, 1e-3))))
+    b.do_kmc_steps(steps)
+    ms = b.last_kernel_ms()
+    out = {"workload": "intZGB otf, 32x32, 2048 trajectories", "steps_per_traj": steps,
+           "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1}
+    b.close()
+    if cpu:
+        from oracle import oracle as O
+        o = O.Oracle(prog, size, seed=11, rng=O.RNG_PHILOX, traj=0)
+        o.set_rates(rates)
+        o.set_user_parameters(params)
+        o.recalculate_rates_matrix()
+        o.update_accum_rate()
+        o.do_kmc_steps(300)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 2.0:
+            o.do_kmc_steps(500)
+            n += 500
+        out["cpu_baseline"] = {"value": n / (time.perf_counter() - t0), "unit": "steps/s", "cores": 1,
+                               "kind": "port", "sample": "one trajectory, %d steps" % n}
     return out
 
 

@@ -307,6 +307,51 @@ KMC_API int kmc_pool_sample_run(kmc_pool *pool, const int32_t *slots, int32_t n,
                                 double *occ_mean, int64_t *procstat_delta, double *integ_delta, double *times,
                                 int64_t *steps, int32_t *status);
 
+/* ------------------------------------------------------------------------------
+ * otf backend (kmos/fortran_src/base_otf.f90 + the otf generator, kmos/io/__init__.py:
+ * 2657-3723): per-entry rates from bystanders.  A handle holds ntraj independent
+ * trajectories of one otf program (kmos_gb300.otf), trajectory t keyed (seed, traj0 + t)
+ * on the Philox stream, or all on the gfortran stream of `seed`.  Rate constants and
+ * user parameters are shared by the batch.  The f2py module of an otf build exposes the
+ * same routines per trajectory: base.set_rate_const, proclist_pars.update_user_parameter,
+ * proclist.recalculate_rates_matrix, base.update_accum_rate / update_integ_rate,
+ * proclist.do_kmc_steps / get_next_kmc_step / run_proc_nr, base.get_rate.
+ * ------------------------------------------------------------------------------ */
+typedef struct kmc_otf kmc_otf;
+
+/* The checks kmc_otf_create makes on an otf program (no device needed). */
+KMC_API int kmc_otf_check_program(const int32_t *program, int32_t program_len);
+/* allocate_system + initialize_state(layer) (cell touch-ups) for ntraj trajectories. */
+KMC_API int kmc_otf_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer,
+                           int32_t ntraj, int32_t seed, int32_t rng_kind, uint32_t traj0, kmc_otf **out);
+KMC_API int kmc_otf_destroy(kmc_otf *h);
+/* base.set_rate_const (base_otf.f90:665-685) */
+KMC_API int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate);
+/* proclist_pars.update_user_parameter: k = 1.. in sorted parameter-name order */
+KMC_API int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value);
+/* proclist.recalculate_rates_matrix + reaccumulate_rates_matrix (io:3786-3830) */
+KMC_API int kmc_otf_recalculate_rates_matrix(kmc_otf *h);
+/* base.update_accum_rate (base_otf.f90:687-716) / update_integ_rate (719-738) */
+KMC_API int kmc_otf_update_accum_rate(kmc_otf *h);
+KMC_API int kmc_otf_update_integ_rate(kmc_otf *h);
+/* proclist.do_kmc_steps(n) on every trajectory, one launch */
+KMC_API int kmc_otf_do_steps(kmc_otf *h, int64_t n);
+/* n steps of trajectory traj alone, its (proc, site) pairs to out[2n] */
+KMC_API int kmc_otf_trace_steps(kmc_otf *h, int32_t traj, int64_t n, int32_t *out);
+/* proclist.get_next_kmc_step / run_proc_nr of one trajectory */
+KMC_API int kmc_otf_get_next_step(kmc_otf *h, int32_t traj, int32_t *proc, int32_t *site);
+KMC_API int kmc_otf_run_proc_nr(kmc_otf *h, int32_t traj, int32_t proc, int32_t site);
+/* State of one trajectory (NULL skips a field): lattice[V], avail_sites as1/as2[P][V+1],
+ * nr_of_sites[P], procstat[P], integ_rates[P], accum_rates[P], rates_matrix[P][V+1]
+ * (base.get_rate(p, i) of list position i), totals[P] (get_rate(p, -1) as the last
+ * update_accum_rate summed it), clock = {kmc_time, kmc_time_step}, kmc_step. */
+KMC_API int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, int32_t *as2,
+                              int32_t *nr_of_sites, int64_t *procstat, double *integ_rates, double *accum_rates,
+                              double *rates_matrix, double *totals, double clock[2], int64_t *kmc_step);
+/* Device time of the last launch (CUDA events on the handle's stream) and launch count. */
+KMC_API int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms);
+KMC_API int kmc_otf_launch_count(kmc_otf *h, int64_t *n);
+
 #ifdef __cplusplus
 }
 #endif

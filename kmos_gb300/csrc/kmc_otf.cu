@@ -1,0 +1,876 @@
+// kmc_otf.cu -- the otf ("on-the-fly" rates) backend's step engine: the C-ABI
+// kmc_otf_* (include/kmc_gb300.h) over a batch of independent trajectories of one model.
+//
+// Reference: kmos/fortran_src/base_otf.f90 and the otf code generator
+// (kmos/io/__init__.py:2657-3723); the model program is kmos_gb300/otf.py's.
+//
+// State of trajectory t, process p (0-based), list position i (1-based), in HBM:
+//   lat   int8   [T][V]            species per site
+//   as1   int32  [T][P][V+1]       avail_sites(p, i, 1)
+//   as2   int32  [T][P][V+1]       avail_sites(p, s, 2)
+//   rm    double [T][P][V+1]       rates_matrix(p, i): the rate of list entry i
+//   pm    double [T][P][V+1]       running sums of rm left to right: pm(i) = pm(i-1) + rm(i)
+//   dirty int32  [T][P]            first position whose running sum is stale
+//   ns, procstat, integ, accum, tot [T][P];  rates, userpar shared by the batch
+// update_accum_rate (base_otf.f90:687-716) re-sums every list from its first entry each
+// step; a running sum depends only on the entries before it, so only the sums from the
+// first entry an event changed onwards are recomputed -- the values are the reference's
+// left-to-right sums bit for bit, and pm is at once the accum_rates_proc array
+// determine_procsite (base_otf.f90:1213-1277) searches.
+//
+// One warp per trajectory.  A step: lanes re-sum the stale lists (one process per lane,
+// a serial chain each), lane 0 chains the process totals into accum_rates, every lane
+// advances the clock and integ_rates of its processes, lane 0 picks the process and the
+// entry (interval_search_real on accum_rates and on the chosen list's running sums) and
+// runs the process's op stream serially: guarded dels, replaces, rate updates and adds,
+// each rate from the process's rate program (gr_<name>, io:2800-2965).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kmc_gb300.h"
+#include "kmc_device.cuh"
+#include "kmc_host.h"
+
+namespace otfdev {
+using namespace kmc;
+
+constexpr int OTF_PMAX = 256;
+constexpr int OTF_WARPS = 4;  // trajectories per block
+constexpr int OTF_NRMAX = 64;
+constexpr int OTF_STACK = 16;
+constexpr int OTF_AUX = 8;
+enum { OP_UPDATE = 7 };
+enum { I_END = 0, I_PUSH_BASE = 1, I_PUSH_PAR = 2, I_PUSH_NR = 3, I_PUSH_INT = 4, I_PUSH_CONST = 5,
+       I_LOAD_AUX = 6, I_STORE_AUX = 7, I_STORE_RESULT = 8, I_ADD = 10, I_SUB = 11, I_MUL = 12,
+       I_DIV = 13, I_NEG = 14, I_POWI = 15, I_POW = 16, I_EXP = 17, I_LOG = 18, I_SQRT = 19,
+       I_ABS = 20, I_CVT = 21 };
+enum { K_INT = 0, K_F32 = 1, K_F64 = 2 };
+
+struct Traj {
+  double kmc_time, kmc_time_step;
+  int64_t kmc_step;
+  uint64_t rng[4];
+  uint32_t seed, traj;
+  int32_t rng_kind, status;
+};
+
+struct Dev {
+  const int32_t *prog;
+  int P, nspecies, null_species, spuck, nuser, off_proc, off_touch, off_rate, off_site_layer, off_site_default;
+  int X, Y, Z, V, T;
+  int8_t *lat;
+  int32_t *as1, *as2, *dirty, *ns;
+  double *rm, *pm, *integ, *accum, *tot;
+  int64_t *procstat;
+  const double *rates, *userpar;
+  Traj *traj;
+};
+
+// One trajectory's view.
+struct View {
+  const Dev *d;
+  int8_t *lat;
+  int32_t *as1, *as2, *dirty, *ns;
+  double *rm, *pm, *integ, *accum, *tot;
+  int64_t *procstat;
+  Geometry g;
+  int stride, err;
+  __device__ inline size_t row(int p) const { return (size_t)p * stride; }  // p 0-based
+};
+
+__device__ inline View view_of(const Dev &d, int t) {
+  View v;
+  v.d = &d;
+  const size_t PV = (size_t)d.P * (d.V + 1);
+  v.lat = d.lat + (size_t)t * d.V;
+  v.as1 = d.as1 + (size_t)t * PV;
+  v.as2 = d.as2 + (size_t)t * PV;
+  v.rm = d.rm + (size_t)t * PV;
+  v.pm = d.pm + (size_t)t * PV;
+  v.dirty = d.dirty + (size_t)t * d.P;
+  v.ns = d.ns + (size_t)t * d.P;
+  v.integ = d.integ + (size_t)t * d.P;
+  v.accum = d.accum + (size_t)t * d.P;
+  v.tot = d.tot + (size_t)t * d.P;
+  v.procstat = d.procstat + (size_t)t * d.P;
+  v.g = Geometry{d.X, d.Y, d.Z, d.spuck};
+  v.stride = d.V + 1;
+  v.err = ST_OK;
+  return v;
+}
+
+// ---------------------------------------------------------------- rate programs
+// x ** m for an integer m by libgcc's __powidf2 / __powisf2 (right-to-left binary
+// powering in the base's precision, the reciprocal for m < 0); integers as gfortran's
+// pow_i4_i4.
+__device__ inline double powi_kind(double xd, int32_t m, int kind) {
+  uint32_t n = m < 0 ? 0u - (uint32_t)m : (uint32_t)m;
+  if (kind == K_F32) {
+    float x = (float)xd, y = (n & 1u) ? x : 1.0f;
+    while (n >>= 1) { x = __fmul_rn(x, x); if (n & 1u) y = __fmul_rn(y, x); }
+    return m < 0 ? (double)__fdiv_rn(1.0f, y) : (double)y;
+  }
+  if (kind == K_F64) {
+    double x = xd, y = (n & 1u) ? x : 1.0;
+    while (n >>= 1) { x = __dmul_rn(x, x); if (n & 1u) y = __dmul_rn(y, x); }
+    return m < 0 ? __ddiv_rn(1.0, y) : y;
+  }
+  int32_t x = (int32_t)xd, y = (n & 1u) ? x : 1;
+  while (n >>= 1) { x = (int32_t)((uint32_t)x * (uint32_t)x); if (n & 1u) y = (int32_t)((uint32_t)y * (uint32_t)x); }
+  if (m < 0) return (y == 1 || y == -1) ? (double)((((uint32_t)0 - (uint32_t)m) & 1u) ? y : 1) : 0.0;
+  return (double)y;
+}
+
+// gr_<p>(cell): bystander counts, then the rate program with base_rate = rates(p).
+__device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
+  const Dev &d = *v.d;
+  const int32_t *r = d.prog + d.prog[d.off_rate + p - 1];
+  const int nb = r[0], nv = r[1];
+  int32_t nr[OTF_NRMAX];
+  for (int k = 0; k < nv; k++) nr[k] = 0;
+  const int32_t *b = r + 4;
+  for (int k = 0; k < nb; k++) {
+    const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
+    const int npairs = b[1];
+    for (int j = 0; j < npairs; j++)
+      if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
+    b += 2 + 2 * npairs;
+  }
+  const int32_t *code = b;
+  double st[OTF_STACK], aux[OTF_AUX], result = 0.0;
+  for (int k = 0; k < OTF_AUX; k++) aux[k] = 0.0;
+  int sp = 0;
+  for (int pc = 0;;) {
+    const uint32_t w = (uint32_t)code[pc++];
+    const int op = w & 0xFF, kind = (w >> 8) & 0xFF, arg = (int)(w >> 16);
+    switch (op) {
+      case I_END: return result;
+      case I_PUSH_BASE: st[sp++] = d.rates[p - 1]; break;
+      case I_PUSH_PAR: st[sp++] = d.userpar[arg]; break;
+      case I_PUSH_NR: st[sp++] = (double)nr[arg]; break;
+      case I_PUSH_INT: st[sp++] = (double)code[pc++]; break;
+      case I_PUSH_CONST:
+        st[sp++] = __hiloint2double(code[pc + 1], code[pc]);
+        pc += 2;
+        break;
+      case I_LOAD_AUX: st[sp++] = aux[arg]; break;
+      case I_STORE_AUX: aux[arg] = st[--sp]; break;
+      case I_STORE_RESULT: result = st[--sp]; break;
+      case I_ADD: case I_SUB: case I_MUL: case I_DIV: {
+        const double b2 = st[--sp], a = st[sp - 1];
+        double r2;
+        if (kind == K_INT) {
+          const int32_t ia = (int32_t)a, ib = (int32_t)b2;
+          r2 = op == I_ADD ? (double)(int32_t)((uint32_t)ia + (uint32_t)ib)
+             : op == I_SUB ? (double)(int32_t)((uint32_t)ia - (uint32_t)ib)
+             : op == I_MUL ? (double)(int32_t)((uint32_t)ia * (uint32_t)ib)
+             : (ib == 0 ? 0.0 : (ib == -1 ? (double)(int32_t)(0u - (uint32_t)ia) : (double)(ia / ib)));
+        } else if (kind == K_F32) {
+          const float fa = (float)a, fb = (float)b2;
+          r2 = op == I_ADD ? __fadd_rn(fa, fb) : op == I_SUB ? __fsub_rn(fa, fb)
+             : op == I_MUL ? __fmul_rn(fa, fb) : __fdiv_rn(fa, fb);
+        } else {
+          r2 = op == I_ADD ? __dadd_rn(a, b2) : op == I_SUB ? __dsub_rn(a, b2)
+             : op == I_MUL ? __dmul_rn(a, b2) : __ddiv_rn(a, b2);
+        }
+        st[sp - 1] = r2;
+        break;
+      }
+      case I_NEG:
+        st[sp - 1] = kind == K_INT ? (double)(int32_t)(0u - (uint32_t)(int32_t)st[sp - 1]) : -st[sp - 1];
+        break;
+      case I_POWI: { const double m = st[--sp]; st[sp - 1] = powi_kind(st[sp - 1], (int32_t)m, kind); break; }
+      case I_POW: {
+        const double b2 = st[--sp], a = st[sp - 1];
+        st[sp - 1] = kind == K_F32 ? (double)powf((float)a, (float)b2) : pow(a, b2);
+        break;
+      }
+      case I_EXP: st[sp - 1] = kind == K_F32 ? (double)expf((float)st[sp - 1]) : exp(st[sp - 1]); break;
+      case I_LOG: st[sp - 1] = kind == K_F32 ? (double)logf((float)st[sp - 1]) : log(st[sp - 1]); break;
+      case I_SQRT: st[sp - 1] = kind == K_F32 ? (double)__fsqrt_rn((float)st[sp - 1]) : __dsqrt_rn(st[sp - 1]); break;
+      case I_ABS: st[sp - 1] = fabs(st[sp - 1]); break;
+      case I_CVT:
+        if (kind == K_INT && arg == K_F32) st[sp - 1] = (double)(float)(int32_t)st[sp - 1];
+        break;
+      default: v.err = ST_PROGRAM; return 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- table operations
+__device__ inline void mark(View &v, int p0, int pos) {
+  if (pos < v.dirty[p0]) v.dirty[p0] = pos;
+}
+
+// add_proc (base_otf.f90:286-331)
+__device__ inline void add_entry(View &v, int p, int site, double rate) {
+  const int p0 = p - 1;
+  int32_t *a1 = v.as1 + v.row(p0), *a2 = v.as2 + v.row(p0);
+  if (site < 1 || site > v.d->V || a2[site] != 0) { v.err = ST_TABLE; return; }
+  const int n = v.ns[p0] + 1;
+  if (n > v.d->V) { v.err = ST_TABLE; return; }
+  v.ns[p0] = n;
+  a1[n] = site;
+  a2[site] = n;
+  v.rm[v.row(p0) + n] = rate;
+  mark(v, p0, n);
+}
+
+// del_proc (base_otf.f90:221-283): the last entry and its rate fill the hole.
+__device__ inline void del_entry(View &v, int p, int site) {
+  const int p0 = p - 1;
+  int32_t *a1 = v.as1 + v.row(p0), *a2 = v.as2 + v.row(p0);
+  double *r = v.rm + v.row(p0);
+  const int m = a2[site];
+  const int n = v.ns[p0];
+  if (m < 1 || m > n) { v.err = ST_TABLE; return; }
+  if (m < n) {
+    const int last = a1[n];
+    if (last < 1 || last > v.d->V) { v.err = ST_TABLE; return; }
+    a1[m] = last;
+    a1[n] = 0;
+    r[m] = r[n];
+    r[n] = 0.0;
+    a2[last] = m;
+  } else {
+    a1[m] = 0;
+    r[m] = 0.0;
+  }
+  a2[site] = 0;
+  v.ns[p0] = n - 1;
+  mark(v, p0, m);
+}
+
+__device__ inline bool can_do(const View &v, int p, int site) { return v.as2[v.row(p - 1) + site] != 0; }
+
+// One op stream (run_proc_<name> or touchup_cell) at cell (bx, by, bz), serially.
+__device__ void run_stream(View &v, int pos, int bx, int by, int bz) {
+  const int32_t *w = v.d->prog;
+  for (;;) {
+    if (v.err) return;
+    const uint32_t h = (uint32_t)w[pos];
+    const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+    switch (op) {
+      case OP_END: return;
+      case OP_REPLACE: {
+        const int site = v.g.site(bx, by, bz, w[pos + 1]);
+        if (!in_mask(v.lat[site - 1], w[pos + 2])) { v.err = ST_SPECIES; return; }
+        v.lat[site - 1] = (int8_t)w[pos + 3];
+        pos += 4;
+        break;
+      }
+      case OP_GDEL: {
+        const int site = v.g.site(bx, by, bz, w[pos + 1]);
+        if (can_do(v, arg, site)) del_entry(v, arg, site);
+        pos += 2;
+        break;
+      }
+      case OP_ADD: {
+        const int site = v.g.site(bx, by, bz, w[pos + 1]);
+        bool ok = true;
+        for (int c = 0; c < cnt && ok; c++)
+          ok = in_mask(v.lat[v.g.site(bx, by, bz, w[pos + 2 + 2 * c]) - 1], w[pos + 3 + 2 * c]);
+        if (ok) {
+          int cx, cy, cz;
+          v.g.cell(bx, by, bz, w[pos + 1], cx, cy, cz);
+          add_entry(v, arg, site, rate_of(v, arg, cx, cy, cz));
+        }
+        pos += 2 + 2 * cnt;
+        break;
+      }
+      case OP_UPDATE: {  // update_rates_matrix (base_otf.f90:333-364)
+        const int site = v.g.site(bx, by, bz, w[pos + 1]);
+        if (can_do(v, arg, site)) {
+          int cx, cy, cz;
+          v.g.cell(bx, by, bz, w[pos + 1], cx, cy, cz);
+          const int m = v.as2[v.row(arg - 1) + site];
+          v.rm[v.row(arg - 1) + m] = rate_of(v, arg, cx, cy, cz);
+          mark(v, arg - 1, m);
+        }
+        pos += 2;
+        break;
+      }
+      case OP_STRIP: {
+        const int site = v.g.site(bx, by, bz, w[pos + 1]);
+        for (int p = 1; p <= v.d->P; p++)
+          if (can_do(v, p, site)) del_entry(v, p, site);
+        pos += 2;
+        break;
+      }
+      default: v.err = ST_PROGRAM; return;
+    }
+  }
+}
+
+// interval_search_real (base_otf.f90:1386-1490) on arr[1..size]: bisection, the scan
+// right past zeros, the scan left over equal values; 0 when no entry is positive.
+__device__ inline int interval_search(const double *arr, int size, double value) {
+  int left = 1, right = size, mid;
+  for (;;) {
+    mid = (right + left) >> 1;
+    if (left >= right) break;
+    if (value < arr[mid]) right = mid; else left = mid + 1;
+  }
+  if (arr[mid] == 0.0) {
+    for (;;) {
+      if (arr[mid] > 0.0) break;
+      if (mid >= size) return 0;
+      mid = mid + 1;
+    }
+  }
+  while (mid != 1 && arr[mid - 1] >= arr[mid]) mid = mid - 1;
+  return mid;
+}
+
+// update_accum_rate: stale running sums re-summed (lanes: processes), then the totals
+// chained into accum_rates on lane 0.  sacc is the warp's accum_rates (1-based).
+__device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
+  const int P = v.d->P;
+  for (int p0 = lane; p0 < P; p0 += 32) {
+    const int n = v.ns[p0];
+    const int lo = v.dirty[p0];
+    double *pm = v.pm + v.row(p0);
+    if (lo <= n) {
+      const double *rm = v.rm + v.row(p0);
+      double s = lo > 1 ? pm[lo - 1] : 0.0;
+      for (int j = lo; j <= n; j++) {
+        s = __dadd_rn(s, rm[j]);
+        pm[j] = s;
+      }
+    }
+    v.dirty[p0] = 0x7FFFFFFF;
+    const double t = n > 0 ? pm[n] : 0.0;
+    stot[p0] = t;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    double acc = stot[0];
+    sacc[1] = acc;
+    for (int p0 = 1; p0 < P; p0++) {
+      acc = __dadd_rn(acc, stot[p0]);
+      sacc[p0 + 1] = acc;
+    }
+  }
+  __syncwarp();
+}
+
+struct Smem {
+  double acc[OTF_WARPS][OTF_PMAX + 1];
+  double tot[OTF_WARPS][OTF_PMAX];
+};
+
+// cmd: 0 = do_kmc_steps(n) on every trajectory (trace: only trajectory `only`, pairs to
+// trace); 1 = update_accum_rate; 2 = update_integ_rate; 3 = get_next_kmc_step of `only`
+// (out[0..1]); 4 = run_proc_nr(out[0], out[1]) on `only`; 5 = initialize_state(layer = n);
+// 6 = recalculate_rates_matrix.
+__global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
+  __shared__ Smem sm;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * OTF_WARPS + warp;
+  if (t >= d.T || (only >= 0 && t != only)) return;
+  View v = view_of(d, t);
+  Traj tr = d.traj[t];
+  if (tr.status && cmd != 5) return;
+  double *sacc = sm.acc[warp], *stot = sm.tot[warp];
+  const int P = d.P;
+  if (cmd == 5) {  // initialize_state (proclist_generic_subroutines.mpy:236-304), the cell touch-up
+    if (lane == 0) {
+      const int32_t *site_layer = d.prog + d.off_site_layer, *site_def = d.prog + d.off_site_default;
+      for (int s = 1; s <= d.V; s++) {
+        const int nr = (s - 1) % d.spuck + 1;
+        v.lat[s - 1] = (int8_t)(site_layer[nr - 1] == (int)n ? site_def[nr - 1] : d.null_species);
+      }
+      for (int k = 0; k < d.Z && !v.err; k++)
+        for (int j = 0; j < d.Y && !v.err; j++)
+          for (int i = 0; i < d.X && !v.err; i++) run_stream(v, d.prog[d.off_touch], i, j, k);
+      tr.status = v.err;
+      d.traj[t] = tr;
+    }
+    return;
+  }
+  if (cmd == 6) {  // recalculate_rates_matrix: every entry's rate from the current lattice
+    for (int p0 = 0; p0 < P; p0++) {
+      const int nn = v.ns[p0];
+      for (int i = 1 + lane; i <= nn; i += 32) {
+        int x, y, z, s;
+        v.g.coords(v.as1[v.row(p0) + i], x, y, z, s);
+        v.rm[v.row(p0) + i] = rate_of(v, p0 + 1, x, y, z);
+      }
+      if (lane == 0) v.dirty[p0] = 1;
+    }
+    if (lane == 0 && v.err) { tr.status = v.err; d.traj[t] = tr; }
+    return;
+  }
+  if (cmd == 1 || cmd == 3) {
+    double r0 = 0, r1 = 0, r2 = 0;
+    if (cmd == 3) draw3(tr.rng_kind, tr.rng, tr.seed, tr.traj, r0, r1, r2);
+    accum_step(v, sacc, stot, lane);
+    for (int p0 = lane; p0 < P; p0 += 32) { v.accum[p0] = sacc[p0 + 1]; v.tot[p0] = stot[p0]; }
+    if (cmd == 3 && lane == 0) {  // get_next_kmc_step: the time draw picks the entry
+      int proc = interval_search(sacc, P, __dmul_rn(r1, sacc[P]));
+      int site = 0;
+      if (proc) {
+        const int nn = v.ns[proc - 1];
+        const double *pm = v.pm + v.row(proc - 1);
+        const int k = nn > 0 ? interval_search(pm, nn, __dmul_rn(r0, pm[nn])) : 0;
+        site = k ? v.as1[v.row(proc - 1) + k] : 0;
+      }
+      io[0] = proc;
+      io[1] = site;
+      d.traj[t] = tr;
+    }
+    return;
+  }
+  if (cmd == 2) {
+    for (int p0 = lane; p0 < P; p0 += 32)
+      v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(v.tot[p0], tr.kmc_time_step));
+    return;
+  }
+  if (cmd == 4) {
+    if (lane == 0) {
+      const int proc = io[0], site = io[1];
+      v.procstat[proc - 1] += 1;
+      int x, y, z, s;
+      v.g.coords(site, x, y, z, s);
+      run_stream(v, d.prog[d.off_proc + proc - 1], x, y, z);
+      tr.status = v.err;
+      d.traj[t] = tr;
+    }
+    return;
+  }
+  // cmd 0: do_kmc_steps (proclist_generic_subroutines.mpy:1-44)
+  for (int64_t step = 0; step < n; step++) {
+    double r0, r1, r2;
+    draw3(tr.rng_kind, tr.rng, tr.seed, tr.traj, r0, r1, r2);
+    accum_step(v, sacc, stot, lane);
+    const double total = sacc[P];
+    if (!(total > 0.0)) { tr.status = ST_DEADLOCK; break; }
+    // update_clocks (base_otf.f90:1280-1320), update_integ_rate (719-738)
+    tr.kmc_time_step = __ddiv_rn(-log(r0), total);
+    tr.kmc_time = __dadd_rn(tr.kmc_time, tr.kmc_time_step);
+    tr.kmc_step += 1;
+    for (int p0 = lane; p0 < P; p0 += 32)
+      v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(stot[p0], tr.kmc_time_step));
+    int err = 0;
+    if (lane == 0) {
+      const int proc = interval_search(sacc, P, __dmul_rn(r1, total));
+      const int nn = proc ? v.ns[proc - 1] : 0;
+      if (!proc || nn <= 0) {
+        err = ST_DEADLOCK;
+      } else {
+        const double *pm = v.pm + v.row(proc - 1);
+        const int k = interval_search(pm, nn, __dmul_rn(r2, pm[nn]));
+        if (!k) {
+          err = ST_DEADLOCK;
+        } else {
+          const int site = v.as1[v.row(proc - 1) + k];
+          if (io) { io[2 * step] = proc; io[2 * step + 1] = site; }
+          v.procstat[proc - 1] += 1;
+          int x, y, z, s;
+          v.g.coords(site, x, y, z, s);
+          run_stream(v, d.prog[d.off_proc + proc - 1], x, y, z);
+          err = v.err;
+        }
+      }
+    }
+    err = __shfl_sync(0xFFFFFFFFu, err, 0);
+    __syncwarp();
+    if (err) { tr.status = err; break; }
+  }
+  for (int p0 = lane; p0 < P; p0 += 32) { v.accum[p0] = sacc[p0 + 1]; v.tot[p0] = stot[p0]; }
+  if (lane == 0) d.traj[t] = tr;
+}
+
+}  // namespace otfdev
+
+// ==================================================================================
+// host side
+// ==================================================================================
+using namespace kmc_host;
+using otfdev::Dev;
+using otfdev::Traj;
+
+struct kmc_otf {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<int32_t> prog;
+  Dev d{};
+  std::vector<double> rates, userpar;
+  double *d_rates = nullptr, *d_userpar = nullptr;
+  int32_t *d_io = nullptr;
+  size_t io_cap = 0;
+  void *mem = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.0f;
+  int64_t launches = 0;
+};
+
+namespace {
+
+bool span_ok(int64_t off, int64_t len, int64_t total) { return off >= 0 && len >= 0 && off + len <= total; }
+
+// Simulates a rate program's stack on the host: every instruction known, every index in
+// range, depth within the device stack, exactly one final END.
+int check_code(const int32_t *c, int64_t len, int nvars, int nuser) {
+  int depth = 0;
+  for (int64_t pc = 0; pc < len;) {
+    const uint32_t w = (uint32_t)c[pc++];
+    const int op = w & 0xFF, kind = (w >> 8) & 0xFF, arg = (int)(w >> 16);
+    if (kind > 2) return 0;
+    switch (op) {
+      case otfdev::I_END: return depth >= 0 && pc == len;
+      case otfdev::I_PUSH_BASE: depth++; break;
+      case otfdev::I_PUSH_PAR: if (arg >= nuser) return 0; depth++; break;
+      case otfdev::I_PUSH_NR: if (arg >= nvars) return 0; depth++; break;
+      case otfdev::I_PUSH_INT: if (pc + 1 > len) return 0; pc += 1; depth++; break;
+      case otfdev::I_PUSH_CONST: if (pc + 2 > len) return 0; pc += 2; depth++; break;
+      case otfdev::I_LOAD_AUX: if (arg >= otfdev::OTF_AUX) return 0; depth++; break;
+      case otfdev::I_STORE_AUX: if (arg >= otfdev::OTF_AUX || depth < 1) return 0; depth--; break;
+      case otfdev::I_STORE_RESULT: if (depth < 1) return 0; depth--; break;
+      case otfdev::I_ADD: case otfdev::I_SUB: case otfdev::I_MUL: case otfdev::I_DIV:
+      case otfdev::I_POWI: case otfdev::I_POW:
+        if (depth < 2) return 0; depth--; break;
+      case otfdev::I_NEG: case otfdev::I_EXP: case otfdev::I_LOG: case otfdev::I_SQRT:
+      case otfdev::I_ABS: case otfdev::I_CVT:
+        if (depth < 1) return 0; break;
+      default: return 0;
+    }
+    if (depth > otfdev::OTF_STACK) return 0;
+  }
+  return 0;
+}
+
+bool coord_ok(int32_t w, int spuck) {
+  const int n = (int)((uint32_t)w >> 24);
+  return n >= 1 && n <= spuck;
+}
+
+// An op stream of the otf program: ops known, arguments and coordinates in range,
+// ending inside the program.
+bool check_stream(const int32_t *w, int64_t len, int64_t pos, int P, int ns, int spuck, bool touch) {
+  for (int guard = 0; guard < 1 << 20; guard++) {
+    if (!span_ok(pos, 1, len)) return false;
+    const uint32_t h = (uint32_t)w[pos];
+    const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+    switch (op) {
+      case OP_END: return true;
+      case OP_REPLACE:
+        if (!span_ok(pos, 4, len) || !coord_ok(w[pos + 1], spuck) || w[pos + 3] < -1 || w[pos + 3] > ns) return false;
+        pos += 4;
+        break;
+      case OP_GDEL: case otfdev::OP_UPDATE:
+        if (!span_ok(pos, 2, len) || arg < 1 || arg > P || !coord_ok(w[pos + 1], spuck)) return false;
+        pos += 2;
+        break;
+      case OP_ADD:
+        if (!span_ok(pos, 2 + 2 * (int64_t)cnt, len) || arg < 1 || arg > P || !coord_ok(w[pos + 1], spuck)) return false;
+        for (int c = 0; c < cnt; c++) if (!coord_ok(w[pos + 2 + 2 * c], spuck)) return false;
+        pos += 2 + 2 * cnt;
+        break;
+      case OP_STRIP:
+        if (!touch || !span_ok(pos, 2, len) || !coord_ok(w[pos + 1], spuck)) return false;
+        pos += 2;
+        break;
+      default: return false;
+    }
+  }
+  return false;
+}
+
+int validate_otf(const int32_t *w, int32_t len) {
+  if (!w || len < 24) return fail(KMC_ERR_PROGRAM, "program too short");
+  if ((uint32_t)w[0] != 0x4B4D4331u || w[1] != 1 || w[2] != 2) return fail(KMC_ERR_PROGRAM, "not an otf program");
+  const int P = w[3], ns = w[4], spuck = w[6], nuser = w[23];
+  if (P < 1 || P > otfdev::OTF_PMAX || ns < 1 || ns > 30 || spuck < 1 || spuck > 255 || nuser < 0 || nuser > 4096)
+    return fail(KMC_ERR_PROGRAM, "otf program sizes out of range");
+  if (w[5] != -1 && w[5] != ns) return fail(KMC_ERR_PROGRAM, "bad null species");
+  const int64_t off_proc = w[10], off_touch = w[11], off_sl = w[13], off_sd = w[14], off_rate = w[22];
+  if (!span_ok(off_proc, P + 1, len) || !span_ok(off_touch, 2, len) || !span_ok(off_sl, spuck, len) ||
+      !span_ok(off_sd, spuck, len) || !span_ok(off_rate, P + 1, len))
+    return fail(KMC_ERR_PROGRAM, "otf program section out of range");
+  for (int s = 0; s < spuck; s++)
+    if (w[off_sd + s] < -1 || w[off_sd + s] > ns) return fail(KMC_ERR_PROGRAM, "bad default species");
+  for (int p = 0; p < P; p++)
+    if (!check_stream(w, len, w[off_proc + p], P, ns, spuck, false)) return fail(KMC_ERR_PROGRAM, "bad process stream");
+  if (!check_stream(w, len, w[off_touch], P, ns, spuck, true)) return fail(KMC_ERR_PROGRAM, "bad touch-up stream");
+  for (int p = 0; p < P; p++) {
+    const int64_t r = w[off_rate + p];
+    if (!span_ok(r, 4, len)) return fail(KMC_ERR_PROGRAM, "bad rate record");
+    const int nb = w[r], nv = w[r + 1], nc = w[r + 2];
+    if (nb < 0 || nb > 4096 || nv < 0 || nv > otfdev::OTF_NRMAX || nc < 1) return fail(KMC_ERR_PROGRAM, "bad rate record");
+    int64_t pos = r + 4;
+    for (int k = 0; k < nb; k++) {
+      if (!span_ok(pos, 2, len) || !coord_ok(w[pos], spuck)) return fail(KMC_ERR_PROGRAM, "bad bystander");
+      const int np = w[pos + 1];
+      if (np < 0 || !span_ok(pos + 2, 2 * (int64_t)np, len)) return fail(KMC_ERR_PROGRAM, "bad bystander");
+      for (int j = 0; j < np; j++)
+        if (w[pos + 2 + 2 * j] < -1 || w[pos + 2 + 2 * j] > ns || w[pos + 3 + 2 * j] < 0 || w[pos + 3 + 2 * j] >= nv)
+          return fail(KMC_ERR_PROGRAM, "bad bystander species or variable");
+      pos += 2 + 2 * (int64_t)np;
+    }
+    if (!span_ok(pos, nc, len) || !check_code(w + pos, nc, nv, nuser)) return fail(KMC_ERR_PROGRAM, "bad rate program");
+  }
+  return KMC_OK;
+}
+
+int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
+  const int blocks = only >= 0 ? 1 : (h->d.T + otfdev::OTF_WARPS - 1) / otfdev::OTF_WARPS;
+  Dev d = h->d;
+  if (only >= 0) {
+    // one block whose first warp is trajectory `only`: shift the trajectory base
+    const size_t PV = (size_t)d.P * (d.V + 1);
+    d.lat += (size_t)only * d.V; d.as1 += only * PV; d.as2 += only * PV; d.rm += only * PV; d.pm += only * PV;
+    d.dirty += (size_t)only * d.P; d.ns += (size_t)only * d.P; d.integ += (size_t)only * d.P;
+    d.accum += (size_t)only * d.P; d.tot += (size_t)only * d.P; d.procstat += (size_t)only * d.P;
+    d.traj += only; d.T = 1;
+  }
+  CK(cudaEventRecord(h->ev0, h->stream));
+  otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, 0, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev1, h->stream));
+  h->launches++;
+  return KMC_OK;
+}
+
+int sync_timed(kmc_otf *h) {
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+  return KMC_OK;
+}
+
+int io_buffer(kmc_otf *h, size_t words) {
+  if (words <= h->io_cap) return KMC_OK;
+  if (h->d_io) CK(cudaFree(h->d_io));
+  h->d_io = nullptr;
+  CK(cudaMalloc(&h->d_io, words * 4));
+  h->io_cap = words;
+  return KMC_OK;
+}
+
+int traj_status(kmc_otf *h, int traj) {
+  Traj tr;
+  CK(cudaMemcpy(&tr, h->d.traj + traj, sizeof(Traj), cudaMemcpyDeviceToHost));
+  return tr.status ? fail(tr.status, "trajectory stopped with a table, species or dead-lock error") : KMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kmc_otf_check_program(const int32_t *program, int32_t len) { return validate_otf(program, len); }
+
+int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], int32_t layer, int32_t ntraj,
+                   int32_t seed, int32_t rng_kind, uint32_t traj0, kmc_otf **out) {
+  if (!program || !dims || !out || ntraj < 1 || (rng_kind != 0 && rng_kind != 1)) return fail(KMC_ERR_ARG, "bad arguments");
+  int rc = validate_otf(program, len);
+  if (rc) return rc;
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(KMC_ERR_ARG, "bad system size");
+  const int64_t V = (int64_t)dims[0] * dims[1] * dims[2] * program[6];
+  if (V > (1 << 24)) return fail(KMC_ERR_ARG, "lattice too large");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(KMC_ERR_NODEVICE, "no CUDA device");
+  kmc_otf *h = new kmc_otf();
+  h->prog.assign(program, program + len);
+  const int P = program[3], T = ntraj;
+  Dev &d = h->d;
+  d.P = P; d.nspecies = program[4]; d.null_species = program[5]; d.spuck = program[6];
+  d.nuser = program[23]; d.off_proc = program[10]; d.off_touch = program[11]; d.off_rate = program[22];
+  d.off_site_layer = program[13]; d.off_site_default = program[14];
+  d.X = dims[0]; d.Y = dims[1]; d.Z = dims[2]; d.V = (int)V; d.T = T;
+  const size_t PV = (size_t)P * (V + 1), TP = (size_t)T * P;
+  const size_t sizes[] = {(size_t)len * 4, (size_t)T * V, T * PV * 4, T * PV * 4, T * PV * 8, T * PV * 8,
+                          TP * 4, TP * 4, TP * 8, TP * 8, TP * 8, TP * 8, (size_t)T * sizeof(Traj),
+                          (size_t)P * 8, (size_t)(d.nuser > 0 ? d.nuser : 1) * 8};
+  size_t offs[15], total = 0;
+  for (int i = 0; i < 15; i++) { offs[i] = total; total = align_up(total + sizes[i], 256); }
+  auto cleanup = [&](int code) { if (h->mem) cudaFree(h->mem); if (h->stream) cudaStreamDestroy(h->stream);
+                                 if (h->ev0) cudaEventDestroy(h->ev0); if (h->ev1) cudaEventDestroy(h->ev1);
+                                 delete h; return code; };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+    return cleanup(fail(KMC_ERR_CUDA, "stream or event creation failed"));
+  if (cudaMalloc(&h->mem, total) != cudaSuccess) return cleanup(fail(KMC_ERR_NOMEM, "device memory"));
+  if (cudaMemsetAsync(h->mem, 0, total, h->stream) != cudaSuccess) return cleanup(fail(KMC_ERR_CUDA, "memset"));
+  char *base = (char *)h->mem;
+  int32_t *dprog = (int32_t *)(base + offs[0]);
+  d.prog = dprog;
+  d.lat = (int8_t *)(base + offs[1]);
+  d.as1 = (int32_t *)(base + offs[2]); d.as2 = (int32_t *)(base + offs[3]);
+  d.rm = (double *)(base + offs[4]); d.pm = (double *)(base + offs[5]);
+  d.dirty = (int32_t *)(base + offs[6]); d.ns = (int32_t *)(base + offs[7]);
+  d.integ = (double *)(base + offs[8]); d.accum = (double *)(base + offs[9]);
+  d.tot = (double *)(base + offs[10]); d.procstat = (int64_t *)(base + offs[11]);
+  d.traj = (Traj *)(base + offs[12]);
+  h->d_rates = (double *)(base + offs[13]); h->d_userpar = (double *)(base + offs[14]);
+  d.rates = h->d_rates; d.userpar = h->d_userpar;
+  h->rates.assign(P, 0.0);
+  h->userpar.assign(d.nuser, 0.0);
+  std::vector<Traj> tr(T);
+  for (int t = 0; t < T; t++) {
+    std::memset(&tr[t], 0, sizeof(Traj));
+    tr[t].seed = (uint32_t)seed; tr[t].traj = traj0 + (uint32_t)t; tr[t].rng_kind = rng_kind;
+    if (rng_kind == RNG_GFORTRAN) gfortran_seed(tr[t].rng, seed);
+  }
+  if (cudaMemcpyAsync(dprog, program, (size_t)len * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(d.traj, tr.data(), (size_t)T * sizeof(Traj), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    return cleanup(fail(KMC_ERR_CUDA, "upload"));
+  std::vector<int32_t> dirty(TP, 0x7FFFFFFF);
+  if (cudaMemcpyAsync(d.dirty, dirty.data(), TP * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    return cleanup(fail(KMC_ERR_CUDA, "upload"));
+  rc = launch(h, 5, layer, -1, nullptr);
+  if (rc) return cleanup(rc);
+  rc = sync_timed(h);
+  if (rc) return cleanup(rc);
+  for (int t = 0; t < T; t++) {
+    rc = traj_status(h, t);
+    if (rc) return cleanup(rc);
+  }
+  *out = h;
+  return KMC_OK;
+}
+
+int kmc_otf_destroy(kmc_otf *h) {
+  if (!h) return KMC_OK;
+  if (h->d_io) cudaFree(h->d_io);
+  if (h->mem) cudaFree(h->mem);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return KMC_OK;
+}
+
+int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate) {
+  if (!h || proc < 1 || proc > h->d.P) return fail(KMC_ERR_ARG, "bad process");
+  h->rates[proc - 1] = rate;
+  CK(cudaMemcpyAsync(h->d_rates, h->rates.data(), h->rates.size() * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return KMC_OK;
+}
+
+int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value) {
+  if (!h || k < 1 || k > h->d.nuser) return fail(KMC_ERR_ARG, "bad user parameter");
+  h->userpar[k - 1] = value;
+  CK(cudaMemcpyAsync(h->d_userpar, h->userpar.data(), h->userpar.size() * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return KMC_OK;
+}
+
+int kmc_otf_recalculate_rates_matrix(kmc_otf *h) {
+  if (!h) return fail(KMC_ERR_ARG, "bad handle");
+  int rc = launch(h, 6, 0, -1, nullptr);
+  return rc ? rc : sync_timed(h);
+}
+
+int kmc_otf_update_accum_rate(kmc_otf *h) {
+  if (!h) return fail(KMC_ERR_ARG, "bad handle");
+  int rc = launch(h, 1, 0, -1, nullptr);
+  return rc ? rc : sync_timed(h);
+}
+
+int kmc_otf_update_integ_rate(kmc_otf *h) {
+  if (!h) return fail(KMC_ERR_ARG, "bad handle");
+  int rc = launch(h, 2, 0, -1, nullptr);
+  return rc ? rc : sync_timed(h);
+}
+
+int kmc_otf_do_steps(kmc_otf *h, int64_t n) {
+  if (!h || n < 0) return fail(KMC_ERR_ARG, "bad arguments");
+  int rc = launch(h, 0, n, -1, nullptr);
+  if (rc) return rc;
+  rc = sync_timed(h);
+  if (rc) return rc;
+  std::vector<Traj> tr(h->d.T);
+  CK(cudaMemcpy(tr.data(), h->d.traj, tr.size() * sizeof(Traj), cudaMemcpyDeviceToHost));
+  for (const Traj &x : tr)
+    if (x.status) return fail(x.status, "a trajectory stopped with a table, species or dead-lock error");
+  return KMC_OK;
+}
+
+int kmc_otf_trace_steps(kmc_otf *h, int32_t traj, int64_t n, int32_t *out) {
+  if (!h || traj < 0 || traj >= h->d.T || n < 0 || !out) return fail(KMC_ERR_ARG, "bad arguments");
+  int rc = io_buffer(h, (size_t)(2 * n + 2));
+  if (rc) return rc;
+  rc = launch(h, 0, n, traj, h->d_io);
+  if (rc) return rc;
+  rc = sync_timed(h);
+  if (rc) return rc;
+  CK(cudaMemcpy(out, h->d_io, (size_t)n * 8, cudaMemcpyDeviceToHost));
+  return traj_status(h, traj);
+}
+
+int kmc_otf_get_next_step(kmc_otf *h, int32_t traj, int32_t *proc, int32_t *site) {
+  if (!h || traj < 0 || traj >= h->d.T || !proc || !site) return fail(KMC_ERR_ARG, "bad arguments");
+  int rc = io_buffer(h, 2);
+  if (rc) return rc;
+  rc = launch(h, 3, 0, traj, h->d_io);
+  if (rc) return rc;
+  rc = sync_timed(h);
+  if (rc) return rc;
+  int32_t v[2];
+  CK(cudaMemcpy(v, h->d_io, 8, cudaMemcpyDeviceToHost));
+  if (!v[0] || !v[1]) return fail(KMC_ERR_DEADLOCK, "no process available");
+  *proc = v[0];
+  *site = v[1];
+  return KMC_OK;
+}
+
+int kmc_otf_run_proc_nr(kmc_otf *h, int32_t traj, int32_t proc, int32_t site) {
+  if (!h || traj < 0 || traj >= h->d.T || proc < 1 || proc > h->d.P || site < 1 || site > h->d.V)
+    return fail(KMC_ERR_ARG, "bad arguments");
+  int rc = io_buffer(h, 2);
+  if (rc) return rc;
+  const int32_t v[2] = {proc, site};
+  CK(cudaMemcpyAsync(h->d_io, v, 8, cudaMemcpyHostToDevice, h->stream));
+  rc = launch(h, 4, 0, traj, h->d_io);
+  if (rc) return rc;
+  rc = sync_timed(h);
+  return rc ? rc : traj_status(h, traj);
+}
+
+int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, int32_t *as2, int32_t *nsites,
+                      int64_t *procstat, double *integ, double *accum, double *rates_matrix, double *totals,
+                      double clock[2], int64_t *kmc_step) {
+  if (!h || traj < 0 || traj >= h->d.T) return fail(KMC_ERR_ARG, "bad arguments");
+  const Dev &d = h->d;
+  const size_t PV = (size_t)d.P * (d.V + 1);
+  CK(cudaStreamSynchronize(h->stream));
+  if (lattice) {
+    std::vector<int8_t> l(d.V);
+    CK(cudaMemcpy(l.data(), d.lat + (size_t)traj * d.V, d.V, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < d.V; i++) lattice[i] = l[i];
+  }
+  if (as1) CK(cudaMemcpy(as1, d.as1 + traj * PV, PV * 4, cudaMemcpyDeviceToHost));
+  if (as2) CK(cudaMemcpy(as2, d.as2 + traj * PV, PV * 4, cudaMemcpyDeviceToHost));
+  if (rates_matrix) CK(cudaMemcpy(rates_matrix, d.rm + traj * PV, PV * 8, cudaMemcpyDeviceToHost));
+  if (nsites) CK(cudaMemcpy(nsites, d.ns + (size_t)traj * d.P, d.P * 4, cudaMemcpyDeviceToHost));
+  if (procstat) CK(cudaMemcpy(procstat, d.procstat + (size_t)traj * d.P, d.P * 8, cudaMemcpyDeviceToHost));
+  if (integ) CK(cudaMemcpy(integ, d.integ + (size_t)traj * d.P, d.P * 8, cudaMemcpyDeviceToHost));
+  if (accum) CK(cudaMemcpy(accum, d.accum + (size_t)traj * d.P, d.P * 8, cudaMemcpyDeviceToHost));
+  if (totals) CK(cudaMemcpy(totals, d.tot + (size_t)traj * d.P, d.P * 8, cudaMemcpyDeviceToHost));
+  if (clock || kmc_step) {
+    Traj tr;
+    CK(cudaMemcpy(&tr, d.traj + traj, sizeof(Traj), cudaMemcpyDeviceToHost));
+    if (clock) { clock[0] = tr.kmc_time; clock[1] = tr.kmc_time_step; }
+    if (kmc_step) *kmc_step = tr.kmc_step;
+  }
+  return KMC_OK;
+}
+
+int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms) {
+  if (!h || !ms) return fail(KMC_ERR_ARG, "bad arguments");
+  *ms = h->last_ms;
+  return KMC_OK;
+}
+
+int kmc_otf_launch_count(kmc_otf *h, int64_t *n) {
+  if (!h || !n) return fail(KMC_ERR_ARG, "bad arguments");
+  *n = h->launches;
+  return KMC_OK;
+}
+
+}  // extern "C"

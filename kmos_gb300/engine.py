@@ -110,6 +110,21 @@ SIGNATURES = {
     "kmc_pool_sample": (_i32, [_vp, _p32, _i32]),
     "kmc_pool_sample_end": (_i32, [_vp, _p32, _i32, _i32, _i32, _pd, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_sample_run": (_i32, [_vp, _p32, _i32, _i32, _i64, _i32, _i32, _pd, _p64, _pd, _pd, _p64, _p32]),
+    "kmc_otf_check_program": (_i32, [_p32, _i32]),
+    "kmc_otf_create": (_i32, [_p32, _i32, _p32, _i32, _i32, _i32, _i32, _u32, _P(_vp)]),
+    "kmc_otf_destroy": (_i32, [_vp]),
+    "kmc_otf_set_rate_const": (_i32, [_vp, _i32, _dbl]),
+    "kmc_otf_set_user_parameter": (_i32, [_vp, _i32, _dbl]),
+    "kmc_otf_recalculate_rates_matrix": (_i32, [_vp]),
+    "kmc_otf_update_accum_rate": (_i32, [_vp]),
+    "kmc_otf_update_integ_rate": (_i32, [_vp]),
+    "kmc_otf_do_steps": (_i32, [_vp, _i64]),
+    "kmc_otf_trace_steps": (_i32, [_vp, _i32, _i64, _p32]),
+    "kmc_otf_get_next_step": (_i32, [_vp, _i32, _p32, _p32]),
+    "kmc_otf_run_proc_nr": (_i32, [_vp, _i32, _i32, _i32]),
+    "kmc_otf_get_state": (_i32, [_vp, _i32, _p32, _p32, _p32, _p32, _p64, _pd, _pd, _pd, _pd, _pd, _p64]),
+    "kmc_otf_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
+    "kmc_otf_launch_count": (_i32, [_vp, _p64]),
 }
 
 _lib = None
@@ -629,3 +644,111 @@ class Pool:
         _check(load().kmc_pool_sample_run(self.h, _ptr(slots, _i32), len(slots), int(samples), int(steps_per_sample),
                                           os_, ps_, *self._out_args(out)))
         return out
+
+
+def check_otf_program(words) -> None:
+    """The checks kmc_otf_create makes on an otf program, on the CPU."""
+    w = _a32(getattr(words, "words", words))
+    _check(load().kmc_otf_check_program(_ptr(w, _i32), len(w)))
+
+
+class OtfBatch:
+    """``ntraj`` independent trajectories of one otf program on the GPU (``kmc_otf_*``):
+    trajectory t draws Philox numbers keyed (seed, traj0 + t), or all share the gfortran
+    stream of ``seed``.  Rate constants and user parameters apply to every trajectory."""
+
+    def __init__(self, program, size, ntraj: int = 1, layer: int = 0, seed: int = 1, rng: int = RNG_PHILOX,
+                 traj0: int = 0):
+        L = load()
+        words = _a32(getattr(program, "words", program))
+        self._words = words
+        dims = _dims3(size)
+        h = ctypes.c_void_p()
+        _check(L.kmc_otf_create(_ptr(words, _i32), len(words), _ptr(dims, _i32), int(layer), int(ntraj),
+                                int(np.int32(seed)), int(rng), int(traj0) & 0xFFFFFFFF, ctypes.byref(h)))
+        self.h = h
+        self.P = int(words[3])
+        self.spuck = int(words[6])
+        self.size = [int(x) for x in dims]
+        self.V = int(np.prod(self.size)) * self.spuck
+        self.ntraj = int(ntraj)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().kmc_otf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_rates(self, rates: Iterable[float]):
+        for p, r in enumerate(rates, start=1):
+            _check(load().kmc_otf_set_rate_const(self.h, p, float(r)))
+
+    def set_user_parameters(self, values: Iterable[float]):
+        for k, v in enumerate(values, start=1):
+            _check(load().kmc_otf_set_user_parameter(self.h, k, float(v)))
+
+    def recalculate_rates_matrix(self):
+        _check(load().kmc_otf_recalculate_rates_matrix(self.h))
+
+    def update_accum_rate(self):
+        _check(load().kmc_otf_update_accum_rate(self.h))
+
+    def update_integ_rate(self):
+        _check(load().kmc_otf_update_integ_rate(self.h))
+
+    def do_kmc_steps(self, n: int):
+        _check(load().kmc_otf_do_steps(self.h, int(n)))
+
+    def trace(self, traj: int, n: int) -> np.ndarray:
+        out = np.zeros(2 * int(n), dtype=np.int32)
+        _check(load().kmc_otf_trace_steps(self.h, int(traj), int(n), _ptr(out, _i32)))
+        return out.reshape(-1, 2)
+
+    def get_next_kmc_step(self, traj: int = 0):
+        p, s = _i32(), _i32()
+        _check(load().kmc_otf_get_next_step(self.h, int(traj), ctypes.byref(p), ctypes.byref(s)))
+        return p.value, s.value
+
+    def run_proc_nr(self, proc: int, site: int, traj: int = 0):
+        _check(load().kmc_otf_run_proc_nr(self.h, int(traj), int(proc), int(site)))
+
+    def state(self, traj: int = 0) -> dict:
+        """lattice, as1, as2, nsites, procstat, integ, accum, rates_matrix ([P][V+1]),
+        totals, kmc_time, kmc_time_step, kmc_step of one trajectory."""
+        P, V = self.P, self.V
+        lat = np.zeros(V, np.int32)
+        as1 = np.zeros(P * (V + 1), np.int32)
+        as2 = np.zeros(P * (V + 1), np.int32)
+        ns = np.zeros(P, np.int32)
+        ps = np.zeros(P, np.int64)
+        ig, ac, tot = np.zeros(P), np.zeros(P), np.zeros(P)
+        rm = np.zeros(P * (V + 1))
+        clock = np.zeros(2)
+        step = _i64()
+        _check(load().kmc_otf_get_state(self.h, int(traj), _ptr(lat, _i32), _ptr(as1, _i32), _ptr(as2, _i32),
+                                        _ptr(ns, _i32), _ptr(ps, _i64), _ptr(ig, _dbl), _ptr(ac, _dbl),
+                                        _ptr(rm, _dbl), _ptr(tot, _dbl), _ptr(clock, _dbl), ctypes.byref(step)))
+        return dict(lattice=lat, as1=as1.reshape(P, V + 1), as2=as2.reshape(P, V + 1), nsites=ns, procstat=ps,
+                    integ=ig, accum=ac, rates_matrix=rm.reshape(P, V + 1), totals=tot, kmc_time=clock[0],
+                    kmc_time_step=clock[1], kmc_step=step.value)
+
+    def last_kernel_ms(self) -> float:
+        ms = ctypes.c_float()
+        _check(load().kmc_otf_last_kernel_ms(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def launch_count(self) -> int:
+        n = _i64()
+        _check(load().kmc_otf_launch_count(self.h, ctypes.byref(n)))
+        return n.value

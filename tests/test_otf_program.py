@@ -124,3 +124,48 @@ def test_intzgb_rates_equal_the_formula():
         got = OTF.evaluate(recs[1][2], 0.25, par, [nco, no])
         want = (0.25 * OTF.powi(0.7, no, OTF.K_F64)) * OTF.powi(1.3, nco, OTF.K_F64)
         assert got == want
+
+
+def fuzz_otf(seed: int, trials: int):
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from kmos_gb300 import engine as E
+    progs = [PG.compile_model(fixture_model(n), "otf") for n in ("intZGB_otf", "default_xml", "AB_model")]
+    rng = np.random.default_rng(seed)
+    accepted = refused = 0
+    for trial in range(trials):
+        w = np.array(progs[trial % len(progs)].words, dtype=np.int32)
+        for _ in range(int(rng.integers(1, 4))):
+            i = int(rng.integers(0, len(w)))
+            how = int(rng.integers(0, 4))
+            if how == 0:
+                w[i] = int(rng.integers(-2**31, 2**31, dtype=np.int64))
+            elif how == 1:
+                w[i] = (int(w[i]) + int(rng.integers(-4, 5)) + 2**31) % 2**32 - 2**31
+            elif how == 2:
+                w[i] = np.uint32((int(w[i]) & 0xFFFFFFFF) ^ (1 << int(rng.integers(0, 32)))).view(np.int32)
+            else:
+                w[i] = -int(rng.integers(1, 8))
+        try:
+            E.check_otf_program(w)
+            accepted += 1
+        except E.KMCError as e:
+            if e.code != 5:
+                raise SystemExit("refused with status %d" % e.code)
+            refused += 1
+    return accepted, refused
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_malformed_otf_programs_never_crash_the_check(seed):
+    """kmc_otf_check_program (run by kmc_otf_create) on randomly corrupted otf programs:
+    refused with KMC_ERR_PROGRAM or accepted, never a crash (child process)."""
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = ("import sys; sys.path[:0] = [%r, %r]; import test_otf_program as T; print(*T.fuzz_otf(%d, 2000))"
+            % (here, os.path.dirname(here), seed))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=here)
+    assert r.returncode == 0, r.stderr[-2000:]
+    accepted, refused = map(int, r.stdout.split()[-2:])
+    assert refused > 0 and accepted + refused == 2000
