@@ -216,6 +216,7 @@ __device__ inline void add_entry(View &v, int p, int site, double rate) {
   v.ns[p0] = n;
   a1[n] = site;
   a2[site] = n;
+  v.tot[p0] = __dadd_rn(v.tot[p0], rate);  // the running rates_matrix(p, V+1)
   v.rm[v.row(p0) + n] = rate;
   mark(v, p0, n);
 }
@@ -228,6 +229,7 @@ __device__ inline void del_entry(View &v, int p, int site) {
   const int m = a2[site];
   const int n = v.ns[p0];
   if (m < 1 || m > n) { v.err = ST_TABLE; return; }
+  v.tot[p0] = __dsub_rn(v.tot[p0], r[m]);
   if (m < n) {
     const int last = a1[n];
     if (last < 1 || last > v.d->V) { v.err = ST_TABLE; return; }
@@ -288,7 +290,10 @@ __device__ void run_stream(View &v, int pos, int bx, int by, int bz) {
           int cx, cy, cz;
           v.g.cell(bx, by, bz, w[pos + 1], cx, cy, cz);
           const int m = v.as2[v.row(arg - 1) + site];
-          v.rm[v.row(arg - 1) + m] = rate_of(v, arg, cx, cy, cz);
+          const double rate = rate_of(v, arg, cx, cy, cz);
+          double *r = v.rm + v.row(arg - 1);
+          v.tot[arg - 1] = __dsub_rn(__dadd_rn(v.tot[arg - 1], rate), r[m]);
+          r[m] = rate;
           mark(v, arg - 1, m);
         }
         pos += 2;
@@ -345,6 +350,7 @@ __device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
     v.dirty[p0] = 0x7FFFFFFF;
     const double t = n > 0 ? pm[n] : 0.0;
     stot[p0] = t;
+    v.tot[p0] = t;
   }
   __syncwarp();
   if (lane == 0) {
@@ -402,6 +408,9 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
       }
       if (lane == 0) v.dirty[p0] = 1;
     }
+    __syncwarp();
+    // reaccumulate_rates_matrix (base_otf.f90:366-387): the totals re-summed
+    accum_step(v, sacc, stot, lane);
     if (lane == 0 && v.err) { tr.status = v.err; d.traj[t] = tr; }
     return;
   }
@@ -409,7 +418,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     double r0 = 0, r1 = 0, r2 = 0;
     if (cmd == 3) draw3(tr.rng_kind, tr.rng, tr.seed, tr.traj, r0, r1, r2);
     accum_step(v, sacc, stot, lane);
-    for (int p0 = lane; p0 < P; p0 += 32) { v.accum[p0] = sacc[p0 + 1]; v.tot[p0] = stot[p0]; }
+    for (int p0 = lane; p0 < P; p0 += 32) v.accum[p0] = sacc[p0 + 1];
     if (cmd == 3 && lane == 0) {  // get_next_kmc_step: the time draw picks the entry
       int proc = interval_search(sacc, P, __dmul_rn(r1, sacc[P]));
       int site = 0;
@@ -481,7 +490,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     __syncwarp();
     if (err) { tr.status = err; break; }
   }
-  for (int p0 = lane; p0 < P; p0 += 32) { v.accum[p0] = sacc[p0 + 1]; v.tot[p0] = stot[p0]; }
+  for (int p0 = lane; p0 < P; p0 += 32) v.accum[p0] = sacc[p0 + 1];
   if (lane == 0) d.traj[t] = tr;
 }
 
