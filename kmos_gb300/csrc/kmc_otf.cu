@@ -311,6 +311,112 @@ __device__ void run_stream(View &v, int pos, int bx, int by, int bz) {
   }
 }
 
+constexpr int OTF_RATE_OPS = 128;  // rate evaluations of one event done warp-parallel
+
+struct EventSmem {
+  double rate[OTF_RATE_OPS];
+  int32_t off[OTF_RATE_OPS];
+  int8_t ok[OTF_RATE_OPS];
+};
+
+// run_proc_<name> of a step with the whole warp.  Every rate and every add condition
+// of the stream reads the lattice only after all of the stream's replaces (the
+// generator puts the replaces after the dels and before the updates and adds, and dels
+// do not read the lattice), so: (1) lane 0 applies the replaces and lists the update /
+// add ops; (2) lanes evaluate their conditions and rates in parallel, from the final
+// lattice; (3) lane 0 replays the table operations in program order with those values.
+// Ops past the first OTF_RATE_OPS are evaluated by lane 0 during the replay.
+__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane) {
+  const int32_t *w = v.d->prog;
+  int nrate = 0;
+  if (lane == 0) {
+    for (int p = pos;;) {
+      const uint32_t h = (uint32_t)w[p];
+      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF;
+      if (op == OP_END) break;
+      if (op == OP_REPLACE) {
+        const int site = v.g.site(bx, by, bz, w[p + 1]);
+        if (!in_mask(v.lat[site - 1], w[p + 2])) { v.err = ST_SPECIES; break; }
+        v.lat[site - 1] = (int8_t)w[p + 3];
+        p += 4;
+      } else if (op == OP_ADD || op == OP_UPDATE) {
+        if (nrate < OTF_RATE_OPS) es.off[nrate++] = p;
+        p += op == OP_ADD ? 2 + 2 * cnt : 2;
+      } else if (op == OP_GDEL) {
+        p += 2;
+      } else {
+        v.err = ST_PROGRAM;
+        break;
+      }
+    }
+  }
+  nrate = __shfl_sync(0xFFFFFFFFu, nrate, 0);
+  const int err0 = __shfl_sync(0xFFFFFFFFu, v.err, 0);
+  __syncwarp();
+  if (err0) return;
+  for (int k = lane; k < nrate; k += 32) {
+    const int p = es.off[k];
+    const uint32_t h = (uint32_t)w[p];
+    const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+    bool ok = true;
+    if (op == OP_ADD)
+      for (int c = 0; c < cnt && ok; c++)
+        ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
+    double rate = 0.0;
+    if (ok) {
+      int cx, cy, cz;
+      v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
+      rate = rate_of(v, arg, cx, cy, cz);
+    }
+    es.rate[k] = rate;
+    es.ok[k] = ok ? 1 : 0;
+  }
+  __syncwarp();
+  if (lane != 0) return;
+  int k = 0;
+  for (int p = pos;;) {
+    if (v.err) return;
+    const uint32_t h = (uint32_t)w[p];
+    const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+    if (op == OP_END) return;
+    if (op == OP_REPLACE) { p += 4; continue; }
+    const int site = v.g.site(bx, by, bz, w[p + 1]);
+    if (op == OP_GDEL) {
+      if (can_do(v, arg, site)) del_entry(v, arg, site);
+      p += 2;
+      continue;
+    }
+    bool ok;
+    double rate;
+    if (k < nrate) {
+      ok = es.ok[k] != 0;
+      rate = es.rate[k];
+    } else {
+      ok = true;
+      if (op == OP_ADD)
+        for (int c = 0; c < cnt && ok; c++)
+          ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
+      int cx, cy, cz;
+      v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
+      rate = ok ? rate_of(v, arg, cx, cy, cz) : 0.0;
+    }
+    k++;
+    if (op == OP_ADD) {
+      if (ok) add_entry(v, arg, site, rate);
+      p += 2 + 2 * cnt;
+    } else {  // OP_UPDATE
+      if (can_do(v, arg, site)) {
+        const int m = v.as2[v.row(arg - 1) + site];
+        double *r = v.rm + v.row(arg - 1);
+        v.tot[arg - 1] = __dsub_rn(__dadd_rn(v.tot[arg - 1], rate), r[m]);
+        r[m] = rate;
+        mark(v, arg - 1, m);
+      }
+      p += 2;
+    }
+  }
+}
+
 // interval_search_real (base_otf.f90:1386-1490) on arr[1..size]: bisection, the scan
 // right past zeros, the scan left over equal values; 0 when no entry is positive.
 __device__ inline int interval_search(const double *arr, int size, double value) {
@@ -340,9 +446,21 @@ __device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
     const int lo = v.dirty[p0];
     double *pm = v.pm + v.row(p0);
     if (lo <= n) {
+      // the chain is serial; its loads are not: 16 entries are fetched before their adds
       const double *rm = v.rm + v.row(p0);
       double s = lo > 1 ? pm[lo - 1] : 0.0;
-      for (int j = lo; j <= n; j++) {
+      int j = lo;
+      for (; j + 15 <= n; j += 16) {
+        double r[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) r[u] = rm[j + u];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+          s = __dadd_rn(s, r[u]);
+          pm[j + u] = s;
+        }
+      }
+      for (; j <= n; j++) {
         s = __dadd_rn(s, rm[j]);
         pm[j] = s;
       }
@@ -367,6 +485,7 @@ __device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
 struct Smem {
   double acc[OTF_WARPS][OTF_PMAX + 1];
   double tot[OTF_WARPS][OTF_PMAX];
+  EventSmem ev[OTF_WARPS];
 };
 
 // cmd: 0 = do_kmc_steps(n) on every trajectory (trace: only trajectory `only`, pairs to
@@ -464,9 +583,9 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     tr.kmc_step += 1;
     for (int p0 = lane; p0 < P; p0 += 32)
       v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(stot[p0], tr.kmc_time_step));
-    int err = 0;
+    int err = 0, proc = 0, site = 0;
     if (lane == 0) {
-      const int proc = interval_search(sacc, P, __dmul_rn(r1, total));
+      proc = interval_search(sacc, P, __dmul_rn(r1, total));
       const int nn = proc ? v.ns[proc - 1] : 0;
       if (!proc || nn <= 0) {
         err = ST_DEADLOCK;
@@ -476,17 +595,22 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
         if (!k) {
           err = ST_DEADLOCK;
         } else {
-          const int site = v.as1[v.row(proc - 1) + k];
+          site = v.as1[v.row(proc - 1) + k];
           if (io) { io[2 * step] = proc; io[2 * step + 1] = site; }
           v.procstat[proc - 1] += 1;
-          int x, y, z, s;
-          v.g.coords(site, x, y, z, s);
-          run_stream(v, d.prog[d.off_proc + proc - 1], x, y, z);
-          err = v.err;
         }
       }
     }
     err = __shfl_sync(0xFFFFFFFFu, err, 0);
+    if (err) { tr.status = err; break; }
+    proc = __shfl_sync(0xFFFFFFFFu, proc, 0);
+    site = __shfl_sync(0xFFFFFFFFu, site, 0);
+    {
+      int x, y, z, s;
+      v.g.coords(site, x, y, z, s);
+      run_event(v, sm.ev[warp], d.prog[d.off_proc + proc - 1], x, y, z, lane);
+    }
+    err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
     if (err) { tr.status = err; break; }
   }
