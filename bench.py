@@ -70,6 +70,10 @@ def parse():
                     help="also time the plain drop-in: one trajectory of the workload through the handle API")
     ap.add_argument("--otf", type=int, default=1,
                     help="after the timed region: the otf backend on intZGB (kmc_otf_*)")
+    ap.add_argument("--otf-only", type=int, default=0,
+                    help="run only the otf sample (--otf-ntraj trajectories, --otf-steps timed steps) and print it")
+    ap.add_argument("--otf-ntraj", type=int, default=2048)
+    ap.add_argument("--otf-steps", type=int, default=0, help="timed otf steps per trajectory (0: about 1.5 s)")
     ap.add_argument("--serving", type=int, default=1,
                     help="also run a short serving sample (configuration 5 stream, 1 s of arrivals, steps x 0.05)")
     return ap.parse_args()
@@ -393,7 +397,7 @@ def run_ours(args, dist: Dist):
     if line is not None and args.serving and dist.world == 1:
         line["serving"] = serving_sample()
     if line is not None and args.otf and dist.world == 1:
-        line["otf"] = otf_sample(args.cpu_baseline)
+        line["otf"] = otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps)
     if line is not None:
         print(json.dumps(line))
     dist.close()
@@ -436,7 +440,7 @@ def serving_sample():
     return out
 
 
-def otf_sample(cpu: int = 1):
+def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
     """The otf backend (per-entry rates from bystanders) after the timed region: intZGB
     (tests/golden/models/intZGB_otf.json, the reference's tests/export_test/intZGB_otf.xml)
     on a 32 x 32 lattice, 2048 Philox trajectories, steps/s over every trajectory from
@@ -448,19 +452,22 @@ def otf_sample(cpu: int = 1):
     prog = PG.compile_model(m, "otf")
     rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
     params = [1.3, 0.7, 1.9, 1e-10, 0.5]
-    ntraj, size = 2048, (32, 32)
+    size = (32, 32)
     b = E.OtfBatch(prog, size, ntraj=ntraj, seed=11, rng=E.RNG_PHILOX)
     b.set_rates(rates)
     b.set_user_parameters(params)
     b.recalculate_rates_matrix()
     b.update_accum_rate()
     b.do_kmc_steps(300)                       # warm-up: tables leave the initial state
-    b.do_kmc_steps(100)
-    ms100 = b.last_kernel_ms()
-    steps = max(100, min(20000, int(100 * 1500.0 / max(ms100, 1e-3))))
+    if fixed_steps:
+        steps = fixed_steps
+    else:
+        b.do_kmc_steps(100)
+        ms100 = b.last_kernel_ms()
+        steps = max(100, min(20000, int(100 * 1500.0 / max(ms100, 1e-3))))
     b.do_kmc_steps(steps)
     ms = b.last_kernel_ms()
-    out = {"workload": "intZGB otf, 32x32, 2048 trajectories", "steps_per_traj": steps,
+    out = {"workload": "intZGB otf, 32x32, %d trajectories" % ntraj, "steps_per_traj": steps,
            "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1}
     b.close()
     if cpu:
@@ -482,6 +489,9 @@ def otf_sample(cpu: int = 1):
 
 def main():
     args = parse()
+    if args.otf_only:
+        print(json.dumps(otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps)))
+        return
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
