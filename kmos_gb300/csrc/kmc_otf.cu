@@ -206,11 +206,11 @@ __device__ inline void mark(View &v, int p0, int pos) {
   if (pos < v.dirty[p0]) v.dirty[p0] = pos;
 }
 
-// add_proc (base_otf.f90:286-331)
-__device__ inline void add_entry(View &v, int p, int site, double rate) {
+// add_proc (base_otf.f90:286-331); m0 = avail_sites(p, site, 2) as the caller read it
+__device__ inline void add_at(View &v, int p, int site, double rate, int m0) {
   const int p0 = p - 1;
   int32_t *a1 = v.as1 + v.row(p0), *a2 = v.as2 + v.row(p0);
-  if (site < 1 || site > v.d->V || a2[site] != 0) { v.err = ST_TABLE; return; }
+  if (site < 1 || site > v.d->V || m0 != 0) { v.err = ST_TABLE; return; }
   const int n = v.ns[p0] + 1;
   if (n > v.d->V) { v.err = ST_TABLE; return; }
   v.ns[p0] = n;
@@ -221,12 +221,17 @@ __device__ inline void add_entry(View &v, int p, int site, double rate) {
   mark(v, p0, n);
 }
 
-// del_proc (base_otf.f90:221-283): the last entry and its rate fill the hole.
-__device__ inline void del_entry(View &v, int p, int site) {
+__device__ inline void add_entry(View &v, int p, int site, double rate) {
+  if (site < 1 || site > v.d->V) { v.err = ST_TABLE; return; }
+  add_at(v, p, site, rate, v.as2[v.row(p - 1) + site]);
+}
+
+// del_proc (base_otf.f90:221-283): the last entry and its rate fill the hole; m =
+// avail_sites(p, site, 2) as the caller read it.
+__device__ inline void del_at(View &v, int p, int site, int m) {
   const int p0 = p - 1;
   int32_t *a1 = v.as1 + v.row(p0), *a2 = v.as2 + v.row(p0);
   double *r = v.rm + v.row(p0);
-  const int m = a2[site];
   const int n = v.ns[p0];
   if (m < 1 || m > n) { v.err = ST_TABLE; return; }
   v.tot[p0] = __dsub_rn(v.tot[p0], r[m]);
@@ -246,6 +251,8 @@ __device__ inline void del_entry(View &v, int p, int site) {
   v.ns[p0] = n - 1;
   mark(v, p0, m);
 }
+
+__device__ inline void del_entry(View &v, int p, int site) { del_at(v, p, site, v.as2[v.row(p - 1) + site]); }
 
 __device__ inline bool can_do(const View &v, int p, int site) { return v.as2[v.row(p - 1) + site] != 0; }
 
@@ -316,19 +323,25 @@ constexpr int OTF_RATE_OPS = 128;  // rate evaluations of one event done warp-pa
 struct EventSmem {
   double rate[OTF_RATE_OPS];
   int32_t off[OTF_RATE_OPS];
+  int32_t m0[OTF_RATE_OPS];   // avail_sites(p, site, 2) before the event
   int8_t ok[OTF_RATE_OPS];
 };
 
 // run_proc_<name> of a step with the whole warp.  Every rate and every add condition
 // of the stream reads the lattice only after all of the stream's replaces (the
 // generator puts the replaces after the dels and before the updates and adds, and dels
-// do not read the lattice), so: (1) lane 0 applies the replaces and lists the update /
-// add ops; (2) lanes evaluate their conditions and rates in parallel, from the final
-// lattice; (3) lane 0 replays the table operations in program order with those values.
-// Ops past the first OTF_RATE_OPS are evaluated by lane 0 during the replay.
+// do not read the lattice), so: (1) lane 0 applies the replaces and lists the table
+// ops; (2) lanes load each op's avail_sites(p, site, 2) as it stands before the event
+// and evaluate the add conditions and the rates in parallel, from the final lattice;
+// (3) lane 0 replays the table operations in program order with those values.  A
+// position loaded in (2) is used while no earlier op of the event has deleted or added
+// an entry of that process (updates move no entry); after that the replay reads the
+// table.  Updates come before adds in every stream, so an update whose entry was absent
+// before the event is absent at its turn too and needs no rate.  Ops past the first
+// OTF_RATE_OPS are done by lane 0 alone.
 __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane) {
   const int32_t *w = v.d->prog;
-  int nrate = 0;
+  int nops = 0;
   if (lane == 0) {
     for (int p = pos;;) {
       const uint32_t h = (uint32_t)w[p];
@@ -339,26 +352,25 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
         if (!in_mask(v.lat[site - 1], w[p + 2])) { v.err = ST_SPECIES; break; }
         v.lat[site - 1] = (int8_t)w[p + 3];
         p += 4;
-      } else if (op == OP_ADD || op == OP_UPDATE) {
-        if (nrate < OTF_RATE_OPS) es.off[nrate++] = p;
+      } else if (op == OP_ADD || op == OP_UPDATE || op == OP_GDEL) {
+        if (nops < OTF_RATE_OPS) es.off[nops++] = p;
         p += op == OP_ADD ? 2 + 2 * cnt : 2;
-      } else if (op == OP_GDEL) {
-        p += 2;
       } else {
         v.err = ST_PROGRAM;
         break;
       }
     }
   }
-  nrate = __shfl_sync(0xFFFFFFFFu, nrate, 0);
+  nops = __shfl_sync(0xFFFFFFFFu, nops, 0);
   const int err0 = __shfl_sync(0xFFFFFFFFu, v.err, 0);
   __syncwarp();
   if (err0) return;
-  for (int k = lane; k < nrate; k += 32) {
+  for (int k = lane; k < nops; k += 32) {
     const int p = es.off[k];
     const uint32_t h = (uint32_t)w[p];
     const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-    bool ok = true;
+    const int m0 = v.as2[v.row(arg - 1) + v.g.site(bx, by, bz, w[p + 1])];
+    bool ok = op == OP_ADD || (op == OP_UPDATE && m0 != 0);
     if (op == OP_ADD)
       for (int c = 0; c < cnt && ok; c++)
         ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
@@ -368,11 +380,13 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
       v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
       rate = rate_of(v, arg, cx, cy, cz);
     }
+    es.m0[k] = m0;
     es.rate[k] = rate;
     es.ok[k] = ok ? 1 : 0;
   }
   __syncwarp();
   if (lane != 0) return;
+  uint64_t moved = 0;  // processes (0-based, < 64) an op of this event deleted or added
   int k = 0;
   for (int p = pos;;) {
     if (v.err) return;
@@ -381,39 +395,53 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     if (op == OP_END) return;
     if (op == OP_REPLACE) { p += 4; continue; }
     const int site = v.g.site(bx, by, bz, w[p + 1]);
+    const int p0 = arg - 1;
+    const bool pre = k < nops && p0 < 64 && !((moved >> p0) & 1ull);
+    const int m = pre ? es.m0[k] : v.as2[v.row(p0) + site];
+    const bool have = k < nops;
+    const bool ok0 = have && es.ok[k] != 0;
+    const double rate0 = have ? es.rate[k] : 0.0;
+    k++;
     if (op == OP_GDEL) {
-      if (can_do(v, arg, site)) del_entry(v, arg, site);
+      if (m != 0) {
+        del_at(v, arg, site, m);
+        if (p0 < 64) moved |= 1ull << p0;
+      }
       p += 2;
       continue;
     }
-    bool ok;
-    double rate;
-    if (k < nrate) {
-      ok = es.ok[k] != 0;
-      rate = es.rate[k];
-    } else {
-      ok = true;
-      if (op == OP_ADD)
+    if (op == OP_ADD) {
+      bool ok = ok0;
+      double rate = rate0;
+      if (!have) {
+        ok = true;
         for (int c = 0; c < cnt && ok; c++)
           ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
-      int cx, cy, cz;
-      v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
-      rate = ok ? rate_of(v, arg, cx, cy, cz) : 0.0;
-    }
-    k++;
-    if (op == OP_ADD) {
-      if (ok) add_entry(v, arg, site, rate);
-      p += 2 + 2 * cnt;
-    } else {  // OP_UPDATE
-      if (can_do(v, arg, site)) {
-        const int m = v.as2[v.row(arg - 1) + site];
-        double *r = v.rm + v.row(arg - 1);
-        v.tot[arg - 1] = __dsub_rn(__dadd_rn(v.tot[arg - 1], rate), r[m]);
-        r[m] = rate;
-        mark(v, arg - 1, m);
+        int cx, cy, cz;
+        v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
+        rate = ok ? rate_of(v, arg, cx, cy, cz) : 0.0;
       }
-      p += 2;
+      if (ok) {
+        add_at(v, arg, site, rate, m);
+        if (p0 < 64) moved |= 1ull << p0;
+      }
+      p += 2 + 2 * cnt;
+      continue;
     }
+    // OP_UPDATE (base_otf.f90:333-364)
+    if (m != 0) {
+      double rate = rate0;
+      if (!ok0) {  // not evaluated ahead (past the listed ops)
+        int cx, cy, cz;
+        v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
+        rate = rate_of(v, arg, cx, cy, cz);
+      }
+      double *r = v.rm + v.row(p0);
+      v.tot[p0] = __dsub_rn(__dadd_rn(v.tot[p0], rate), r[m]);
+      r[m] = rate;
+      mark(v, p0, m);
+    }
+    p += 2;
   }
 }
 
