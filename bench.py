@@ -392,12 +392,20 @@ def run_ours(args, dist: Dist):
             "gpu_launches": launches,
         }
     pool.close()
+    # samples measured after the timed region; a failure in one is recorded in its key
+    # and never costs the line itself
+    extras = []
     if line is not None and args.plain:
-        line["plain_dropin"] = plain_dropin(wl)
+        extras.append(("plain_dropin", lambda: plain_dropin(wl)))
     if line is not None and args.serving and dist.world == 1:
-        line["serving"] = serving_sample()
+        extras.append(("serving", serving_sample))
     if line is not None and args.otf and dist.world == 1:
-        line["otf"] = otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps)
+        extras.append(("otf", lambda: otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps)))
+    for key, fn in extras:
+        try:
+            line[key] = fn()
+        except Exception as e:  # noqa: BLE001
+            line[key] = {"error": "%s: %s" % (type(e).__name__, e)}
     if line is not None:
         print(json.dumps(line))
     dist.close()
