@@ -169,3 +169,41 @@ def test_malformed_otf_programs_never_crash_the_check(seed):
     assert r.returncode == 0, r.stderr[-2000:]
     accepted, refused = map(int, r.stdout.split()[-2:])
     assert refused > 0 and accepted + refused == 2000
+
+
+def test_otf_check_refuses_what_the_device_cannot_run():
+    """kmc_otf_check_program refuses, with KMC_ERR_PROGRAM: a rate program deeper than
+    the device stack, one reading an nr variable or user parameter that does not exist,
+    an unknown instruction, a touch-up strip inside a process stream, a local_smart
+    program."""
+    from kmos_gb300 import engine as E
+    from kmos_gb300.model import Bystander, Coord, Process
+    m = fixture_model("intZGB_otf")
+    E.check_otf_program(PG.compile_model(m, "otf"))
+
+    def refused(words):
+        with pytest.raises(E.KMCError) as e:
+            E.check_otf_program(words)
+        assert e.value.code == 5
+
+    deep = "+".join(["(base_rate*J_O_O"] * 17) + ")" * 17
+    m2 = fixture_model("intZGB_otf")
+    m2.processes[1].otf_rate = deep
+    with pytest.raises(OTF.ExprError):
+        PG.compile_model(m2, "otf")              # the compiler refuses it first
+    prog = PG.compile_model(m, "otf")
+    w = np.array(prog.words, dtype=np.int32)
+    r = int(w[int(w[22])])                      # rate record of process 1 (CO_ads)
+    nb = int(w[r])
+    pos = r + 4
+    for _ in range(nb):
+        pos += 2 + 2 * int(w[pos + 1])
+    code0 = pos                                  # first instruction: PUSH_BASE
+    for bad in (OTF.ins(OTF.I_PUSH_NR, 0, 9), OTF.ins(OTF.I_PUSH_PAR, 0, 5), 99):
+        v = w.copy()
+        v[code0] = bad
+        refused(v)
+    v = w.copy()
+    v[int(w[int(w[10])])] = PG.op_header(PG.OP_STRIP)   # first op of process 1
+    refused(v)
+    refused(PG.compile_model(m, "local_smart").words)
