@@ -329,7 +329,7 @@ KMC_API int kmc_otf_destroy(kmc_otf *h);
 KMC_API int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate);
 /* proclist_pars.update_user_parameter: k = 1.. in sorted parameter-name order */
 KMC_API int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value);
-/* proclist.recalculate_rates_matrix + reaccumulate_rates_matrix (io:3786-3830) */
+/* proclist.recalculate_rates_matrix + reaccumulate_rates_matrix (proclist_generic_subroutines.mpy:307-325) */
 KMC_API int kmc_otf_recalculate_rates_matrix(kmc_otf *h);
 /* base.update_accum_rate (base_otf.f90:687-716) / update_integ_rate (719-738) */
 KMC_API int kmc_otf_update_accum_rate(kmc_otf *h);

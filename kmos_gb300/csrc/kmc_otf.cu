@@ -656,7 +656,6 @@ using otfdev::Dev;
 using otfdev::Traj;
 
 struct kmc_otf {
-  int device = 0;
   cudaStream_t stream = nullptr;
   std::vector<int32_t> prog;
   Dev d{};

@@ -30,7 +30,7 @@
  *   entry from the running sum of the chosen list)
  * with the generated gr_<name> rate functions (kmos/io/__init__.py:2657-2965) run from
  * the rate programs of kmos_gb300/otf.py by an evaluator written here (otf_eval), the
- * cell touch-up (io:3240-3285) and recalculate_rates_matrix (io:3786-3830).
+ * cell touch-up (io:3240-3285) and recalculate_rates_matrix (proclist_generic_subroutines.mpy:307-325).
  * The process-specific code (generated proclist.f90 / run_proc_*.f90 / nli_*.f90) is
  * taken from the op program that kmos_gb300.program compiles; the op semantics below
  * follow kmos/io/__init__.py:305-465, 1732-2057, 2219-2655.
@@ -699,7 +699,7 @@ void oracle_set_rate_const(oracle_t *o, int proc, double rate) { o->rates[proc -
 /* otf: update_user_parameter (proclist_pars, io:2755-2762) */
 void oracle_set_user_parameter(oracle_t *o, int k, double v) { if (k >= 1 && k <= o->nuser) o->userpar[k - 1] = v; }
 
-/* otf: recalculate_rates_matrix (io:3786-3830): every available entry's rate re-evaluated,
+/* otf: recalculate_rates_matrix (proclist_generic_subroutines.mpy:307-325): every available entry's rate re-evaluated,
  * then reaccumulate_rates_matrix (base_otf.f90:366-387). */
 int oracle_recalculate_rates_matrix(oracle_t *o)
 {
