@@ -207,3 +207,43 @@ def test_otf_check_refuses_what_the_device_cannot_run():
     v[int(w[int(w[10])])] = PG.op_header(PG.OP_STRIP)   # first op of process 1
     refused(v)
     refused(PG.compile_model(m, "local_smart").words)
+
+
+def test_ini_bystanders_and_otf_rate_read_like_the_xml():
+    """The .ini form kmos writes for otf models (kmos/types.py:418-428: ``bystanders =
+    ['O', 'CO']@default.(1, 0, 0)|1nn + ...``, ``otf_rate = ...``) reads back into the same
+    processes as the .xml; the JSON form keeps bystanders and otf_rate."""
+    from kmos_gb300 import model as M
+    xml = fixture_model("intZGB_otf")
+    lines = ["[Meta]", "model_name = IntZGB", "model_dimension = 2", "",
+             "[SpeciesList]", "default_species = empty", ""]
+    for sp in xml.species:
+        lines += ["[Species %s]" % sp, "representation = ", ""]
+    lines += ["[Lattice]", "cell_size = 1.0 1.0 1.0", "default_layer = square", "",
+              "[Layer square]", "site default = (0.5, 0.5, 0.5); default_species; ", ""]
+    for p in xml.parameters:
+        lines += ["[Parameter %s]" % p.name, "value = %s" % p.value, "adjustable = False", "min = 0.0",
+                  "max = 0.0", "scale = linear", ""]
+
+    def sh(species, c):
+        off = tuple(c.offset)
+        return "%s@%s%s" % (species, c.name, ".%s" % (off,) if any(off) else "")
+
+    for p in xml.processes:
+        lines += ["[Process %s]" % p.name, "rate_constant = %s" % p.rate_constant,
+                  "enabled = True",
+                  "conditions = " + " + ".join(sh(c.species, c.coord) for c in p.conditions),
+                  "actions = " + " + ".join(sh(a.species, a.coord) for a in p.actions)]
+        if p.bystanders:
+            lines.append("bystanders = " + " + ".join("%s|%s" % (sh(list(b.allowed_species), b.coord), b.flag)
+                                                      for b in p.bystanders))
+        lines.append("otf_rate = %s" % p.otf_rate)
+        lines.append("")
+    ini = M.load_ini("\n".join(lines))
+    assert [p.name for p in ini.processes] == [p.name for p in xml.processes]
+    for a, b in zip(ini.processes, xml.processes):
+        assert a.bystanders == b.bystanders and a.otf_rate == b.otf_rate
+        assert a.conditions == b.conditions and a.actions == b.actions
+    assert (PG.compile_model(ini, "otf").words == PG.compile_model(xml, "otf").words).all()
+    back = M.from_dict(M.to_dict(xml))
+    assert [(p.bystanders, p.otf_rate) for p in back.processes] == [(p.bystanders, p.otf_rate) for p in xml.processes]
