@@ -690,13 +690,19 @@ class OtfBatch:
     def __exit__(self, *exc):
         self.close()
 
+    def set_rate_const(self, proc: int, rate: float):
+        _check(load().kmc_otf_set_rate_const(self.h, int(proc), float(rate)))
+
     def set_rates(self, rates: Iterable[float]):
         for p, r in enumerate(rates, start=1):
-            _check(load().kmc_otf_set_rate_const(self.h, p, float(r)))
+            self.set_rate_const(p, r)
+
+    def set_user_parameter(self, k: int, value: float):
+        _check(load().kmc_otf_set_user_parameter(self.h, int(k), float(value)))
 
     def set_user_parameters(self, values: Iterable[float]):
         for k, v in enumerate(values, start=1):
-            _check(load().kmc_otf_set_user_parameter(self.h, k, float(v)))
+            self.set_user_parameter(k, v)
 
     def recalculate_rates_matrix(self):
         _check(load().kmc_otf_recalculate_rates_matrix(self.h))
@@ -723,25 +729,35 @@ class OtfBatch:
     def run_proc_nr(self, proc: int, site: int, traj: int = 0):
         _check(load().kmc_otf_run_proc_nr(self.h, int(traj), int(proc), int(site)))
 
-    def state(self, traj: int = 0) -> dict:
+    STATE_FIELDS = ("lattice", "as1", "as2", "nsites", "procstat", "integ", "accum", "rates_matrix", "totals",
+                    "clock")
+
+    def state(self, traj: int = 0, fields: Optional[Sequence[str]] = None) -> dict:
         """lattice, as1, as2, nsites, procstat, integ, accum, rates_matrix ([P][V+1]),
-        totals, kmc_time, kmc_time_step, kmc_step of one trajectory."""
+        totals, kmc_time, kmc_time_step, kmc_step of one trajectory (``fields``: copy only
+        those of STATE_FIELDS; "clock" is kmc_time, kmc_time_step and kmc_step)."""
         P, V = self.P, self.V
-        lat = np.zeros(V, np.int32)
-        as1 = np.zeros(P * (V + 1), np.int32)
-        as2 = np.zeros(P * (V + 1), np.int32)
-        ns = np.zeros(P, np.int32)
-        ps = np.zeros(P, np.int64)
-        ig, ac, tot = np.zeros(P), np.zeros(P), np.zeros(P)
-        rm = np.zeros(P * (V + 1))
-        clock = np.zeros(2)
+        want = set(self.STATE_FIELDS if fields is None else fields)
+        shapes = {"lattice": (V, np.int32), "as1": (P * (V + 1), np.int32), "as2": (P * (V + 1), np.int32),
+                  "nsites": (P, np.int32), "procstat": (P, np.int64), "integ": (P, np.float64),
+                  "accum": (P, np.float64), "rates_matrix": (P * (V + 1), np.float64), "totals": (P, np.float64),
+                  "clock": (2, np.float64)}
+        ctype = {np.int32: _i32, np.int64: _i64, np.float64: _dbl}
+        arrs = {k: np.zeros(n, dt) for k, (n, dt) in shapes.items() if k in want}
+        ptr = {k: (_ptr(arrs[k], ctype[shapes[k][1]]) if k in arrs else None) for k in shapes}
         step = _i64()
-        _check(load().kmc_otf_get_state(self.h, int(traj), _ptr(lat, _i32), _ptr(as1, _i32), _ptr(as2, _i32),
-                                        _ptr(ns, _i32), _ptr(ps, _i64), _ptr(ig, _dbl), _ptr(ac, _dbl),
-                                        _ptr(rm, _dbl), _ptr(tot, _dbl), _ptr(clock, _dbl), ctypes.byref(step)))
-        return dict(lattice=lat, as1=as1.reshape(P, V + 1), as2=as2.reshape(P, V + 1), nsites=ns, procstat=ps,
-                    integ=ig, accum=ac, rates_matrix=rm.reshape(P, V + 1), totals=tot, kmc_time=clock[0],
-                    kmc_time_step=clock[1], kmc_step=step.value)
+        _check(load().kmc_otf_get_state(self.h, int(traj), ptr["lattice"], ptr["as1"], ptr["as2"], ptr["nsites"],
+                                        ptr["procstat"], ptr["integ"], ptr["accum"], ptr["rates_matrix"],
+                                        ptr["totals"], ptr["clock"], ctypes.byref(step) if "clock" in want else None))
+        out = {}
+        for k, a in arrs.items():
+            if k in ("as1", "as2", "rates_matrix"):
+                out[k] = a.reshape(P, V + 1)
+            elif k == "clock":
+                out.update(kmc_time=float(a[0]), kmc_time_step=float(a[1]), kmc_step=step.value)
+            else:
+                out[k] = a
+        return out
 
     def last_kernel_ms(self) -> float:
         ms = ctypes.c_float()

@@ -23,6 +23,7 @@ copy what they return.  Where the Fortran would ``stop``, a ``KMCError`` is rais
 """
 from __future__ import annotations
 
+import time
 import types
 from typing import Optional
 
@@ -31,6 +32,112 @@ import numpy as np
 from . import engine as E
 from .model import Model, from_dict, load
 from .program import compile_model
+
+
+class _OtfTrajectory:
+    """One otf trajectory (``engine.OtfBatch`` of one, on the gfortran stream of the
+    seed) behind the calls the base / lattice / proclist namespaces make.  Lattice edits
+    (replace_species, touch-ups), reload files and setting the clock are not offered by
+    the otf engine and raise KMCError."""
+
+    def __init__(self, program, size, layer: int, seed: int):
+        self.b = E.OtfBatch(program, size, ntraj=1, layer=layer, seed=seed, rng=E.RNG_GFORTRAN)
+        self.P, self.V, self.spuck = self.b.P, self.b.V, self.b.spuck
+        self.nspecies = int(program.words[4])
+        self.cells = self.V // self.spuck
+        self._rates = np.zeros(self.P)
+        self._t0 = time.time()
+
+    def close(self):
+        self.b.close()
+
+    def _get(self, *fields):
+        return self.b.state(0, fields)
+
+    def set_rate_const(self, proc: int, rate: float):
+        self.b.set_rate_const(proc, rate)
+        self._rates[proc - 1] = rate
+
+    def update_accum_rate(self):
+        self.b.update_accum_rate()
+
+    def update_integ_rate(self):
+        self.b.update_integ_rate()
+
+    def recalculate_rates_matrix(self):
+        self.b.recalculate_rates_matrix()
+
+    def do_kmc_steps(self, n: int):
+        self.b.do_kmc_steps(n)
+
+    def get_next_kmc_step(self):
+        return self.b.get_next_kmc_step(0)
+
+    def run_proc_nr(self, proc: int, site: int):
+        self.b.run_proc_nr(proc, site, 0)
+
+    @property
+    def kmc_time(self) -> float:
+        return self._get("clock")["kmc_time"]
+
+    @kmc_time.setter
+    def kmc_time(self, t: float):
+        raise E.KMCError(1, "set_kmc_time is not offered by the otf engine")
+
+    @property
+    def kmc_time_step(self) -> float:
+        return self._get("clock")["kmc_time_step"]
+
+    @property
+    def kmc_step(self) -> int:
+        return self._get("clock")["kmc_step"]
+
+    @property
+    def walltime(self) -> float:
+        return time.time() - self._t0
+
+    def procstat(self):
+        return self._get("procstat")["procstat"]
+
+    def rates(self):
+        return self._rates.copy()
+
+    def integ_rates(self):
+        return self._get("integ")["integ"]
+
+    def accum_rates(self):
+        return self._get("accum")["accum"]
+
+    def nr_of_sites(self):
+        return self._get("nsites")["nsites"]
+
+    def get_rate(self, proc: int, site: int = -1) -> float:
+        """base.get_rate (base_otf.f90:1121-1145): rates_matrix(proc, site), or the
+        process total rates_matrix(proc, V+1) for site -1."""
+        if site == -1:
+            return float(self._get("totals")["totals"][proc - 1])
+        return float(self._get("rates_matrix")["rates_matrix"][proc - 1, site])
+
+    def avail_site(self, proc: int, idx: int, sw: int) -> int:
+        key = "as1" if sw == 1 else "as2"
+        return int(self._get(key)[key][proc - 1, idx])
+
+    def get_species(self, nr: int) -> int:
+        return int(self._get("lattice")["lattice"][nr - 1])
+
+    def occupation(self) -> np.ndarray:
+        """get_occupation (proclist_generic_subroutines.mpy:113-158): species per site
+        index, divided by the number of cells."""
+        lat = self._get("lattice")["lattice"].reshape(-1, self.spuck)
+        occ = np.zeros((self.nspecies, self.spuck))
+        for sp in range(self.nspecies):
+            occ[sp] = (lat == sp).sum(axis=0) / self.cells
+        return occ
+
+    def _refuse(self, *_a, **_k):
+        raise E.KMCError(1, "lattice edits, touch-ups and reload files are not offered by the otf engine")
+
+    replace_species = touchup_many = save_reload = load_reload = _refuse
 
 
 class _State:
@@ -94,7 +201,10 @@ def _base(S: _State) -> types.SimpleNamespace:
 
     ns.set_kmc_time = set_kmc_time
     ns.get_procstat = lambda proc: int(S.t().procstat()[int(proc) - 1])
-    ns.get_rate = lambda proc: float(S.t().rates()[int(proc) - 1])
+    if S.backend == "otf":
+        ns.get_rate = lambda proc, site_nr=-1: S.t().get_rate(int(proc), int(site_nr))
+    else:
+        ns.get_rate = lambda proc: float(S.t().rates()[int(proc) - 1])
     ns.get_integ_rate = lambda proc: float(S.t().integ_rates()[int(proc) - 1])
     ns.get_accum_rate = lambda proc: float(S.t().accum_rates()[int(proc) - 1])
     ns.get_nrofsites = lambda proc: int(S.t().nr_of_sites()[int(proc) - 1])
@@ -190,8 +300,8 @@ def _proclist(S: _State) -> types.SimpleNamespace:
     ns.seed_size = 12
     ns.seed = S.seed
     ns.representation_length = max([len(r) for r in m.representations.values()] + [1])
-    if S.backend == "lat_int":
-        ns.backend = "lat_int"
+    if S.backend in ("lat_int", "otf"):
+        ns.backend = S.backend
 
     def init(input_system_size, system_name="kmc_model", layer=None, seed_in=1, no_banner=True):
         """proclist.init (proclist_generic_subroutines.mpy:166-230)."""
@@ -204,7 +314,12 @@ def _proclist(S: _State) -> types.SimpleNamespace:
         S.system_name = str(system_name)
         ns.seed = S.seed
         layer = ns_default_layer if layer is None else int(layer)
-        S.traj = E.Trajectory(S.program, size, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
+        if S.backend == "otf":
+            S.traj = _OtfTrajectory(S.program, size, layer, S.seed)
+            for k, v in enumerate(_pars(S).userpar[:len(S.model.parameters)], start=1):
+                S.traj.b.set_user_parameter(k, float(v))
+        else:
+            S.traj = E.Trajectory(S.program, size, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
 
     ns_default_layer = m.layer_ids()[m.default_layer]
     ns.init = init
@@ -220,11 +335,48 @@ def _proclist(S: _State) -> types.SimpleNamespace:
         return S.t().occupation()
 
     ns.get_occupation = get_occupation
-    if S.backend == "lat_int":
+    if S.backend == "otf":
+        # recalculate_rates_matrix (proclist_generic_subroutines.mpy:307-325) and the
+        # proclist_pars routines kmos.run reaches through proclist
+        ns.recalculate_rates_matrix = lambda: S.t().recalculate_rates_matrix()
+        pars = _pars(S)
+        for k, v in vars(pars).items():
+            if not hasattr(ns, k):
+                setattr(ns, k, v)
+        ns.touchup_cell = lambda cell: S.t().touchup_many([cell])
+    elif S.backend == "lat_int":
         ns.touchup_cell = lambda cell: S.touchup([cell[0], cell[1], cell[2], 1])
     else:
         for (lname, sname), n in m.site_ids().items():
             setattr(ns, ("touchup_%s_%s" % (lname, sname)).lower(), lambda site: S.touchup(site))
+    return ns
+
+
+def _pars(S: _State) -> types.SimpleNamespace:
+    """proclist_pars of an otf build (kmos/io/__init__.py:2657-2800): the user
+    parameters (1-based, sorted by name) and their update / get routines, and the
+    byst_<process> strings of nr variable names."""
+    if getattr(S, "pars", None) is not None:
+        return S.pars
+    from . import otf
+    ns = types.SimpleNamespace()
+    S.pars = ns
+    names = otf.user_parameters(S.model)
+    values = np.zeros(max(len(names), 1))
+    for k, n in enumerate(names, start=1):
+        setattr(ns, n.lower(), k)
+
+    def update_user_parameter(param, val):
+        if not 1 <= int(param) <= len(names):
+            raise E.KMCError(1, "user parameter %s out of range" % param)
+        values[int(param) - 1] = float(val)
+        S.t().b.set_user_parameter(int(param), float(val))
+
+    ns.update_user_parameter = update_user_parameter
+    ns.get_user_parameter = lambda param: float(values[int(param) - 1])
+    ns.userpar = values
+    for proc in S.model.processes:
+        setattr(ns, "byst_%s" % proc.name.lower(), " ".join(otf.nr_var_names(proc)))
     return ns
 
 
@@ -241,11 +393,15 @@ def configure(model, backend: str = "local_smart"):
     b, l, p = _base(S), _lattice(S), _proclist(S)
     g = globals()
     g["base"], g["lattice"], g["proclist"], g["_state"] = b, l, p, S
+    if backend == "otf":
+        g["proclist_pars"] = _pars(S)
+    else:
+        g.pop("proclist_pars", None)
     return b, l, p
 
 
 def __getattr__(name):
-    if name in ("base", "lattice", "proclist"):
+    if name in ("base", "lattice", "proclist", "proclist_pars"):
         import importlib
         import os
         settings = importlib.import_module("kmc_settings")
@@ -258,5 +414,7 @@ def __getattr__(name):
         else:
             raise AttributeError("kmc_settings has neither model_json nor xml to configure %s from" % name)
         configure(model, backend)
+        if name not in globals():
+            raise AttributeError(name)   # proclist_pars exists for otf builds only
         return globals()[name]
     raise AttributeError(name)

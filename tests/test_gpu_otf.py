@@ -127,3 +127,37 @@ def test_trace_matches_oracle():
     np.testing.assert_array_equal(tr, oracles[2].trace(1200))
     compare(b, 2, oracles[2])
     assert b.state(0)["kmc_step"] == 0   # the other trajectories did not move
+
+
+def test_dropin_module_otf_build():
+    """kmos_gb300.kmc_model configured for otf: the KMC_Model sequence on the GPU equals
+    the oracle run the same way (gfortran stream of the seed)."""
+    from kmos_gb300 import kmc_model
+    m = fixture_model("intZGB_otf")
+    params = dict(zip(OTF.user_parameters(m), INTZGB_PARAMS))
+    base, lattice, proclist = kmc_model.configure(m, "otf")
+    proclist.init((12, 10), "IntZGB", lattice.default_layer, 7, True)
+    for p, r in enumerate(INTZGB_RATES, start=1):
+        base.set_rate_const(p, r)
+    for name, v in params.items():
+        proclist.update_user_parameter(getattr(proclist, name.lower()), v)
+    proclist.recalculate_rates_matrix()
+    base.update_accum_rate()
+    base.update_integ_rate()
+    proclist.do_kmc_steps(900)
+    prog = PG.compile_model(m, "otf")
+    o = O.Oracle(prog, (12, 10), seed=7, rng=O.RNG_GFORTRAN)
+    o.set_rates(INTZGB_RATES)
+    o.set_user_parameters(INTZGB_PARAMS)
+    o.recalculate_rates_matrix()
+    o.update_accum_rate()
+    o.update_integ_rate()
+    o.do_kmc_steps(900)
+    _rm, tot = o.rates_matrix()
+    assert base.get_kmc_step() == 900
+    np.testing.assert_allclose(base.get_kmc_time(), o.kmc_time, rtol=1e-12)
+    for p in range(1, len(INTZGB_RATES) + 1):
+        assert base.get_procstat(p) == o.procstat()[p - 1]
+        assert base.get_rate(p) == tot[p - 1]
+    np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
+    lattice.deallocate_system()

@@ -1,0 +1,108 @@
+"""The drop-in module's otf build (kmos_gb300/kmc_model.py) on the CPU: the sequence
+kmos.run's KMC_Model runs for an otf model (init, set_rate_const, update_user_parameter
+through proclist, recalculate_rates_matrix, update_accum_rate / update_integ_rate,
+do_kmc_steps, the getters) with the engine's otf batch replaced by an oracle-backed
+stand-in, so that the namespaces' argument conventions and read-outs are checked
+without a GPU.  The engine's otf calls themselves are checked on the GPU
+(tests/test_gpu_otf.py)."""
+import numpy as np
+
+from conftest import fixture_model
+from kmos_gb300 import engine as E, kmc_model, otf as OTF, program as PG
+from oracle import oracle as O
+
+
+class OracleOtfBatch:
+    """engine.OtfBatch's interface for one trajectory, run by the oracle (test only)."""
+
+    def __init__(self, program, size, ntraj=1, layer=0, seed=1, rng=E.RNG_PHILOX, traj0=0):
+        assert ntraj == 1
+        self.o = O.Oracle(program, size, layer=layer, seed=seed, rng=rng, traj=traj0)
+        self.P, self.V, self.spuck = self.o.P, self.o.V, self.o.spuck
+
+    def close(self):
+        pass
+
+    def set_rate_const(self, proc, rate):
+        O.lib().oracle_set_rate_const(self.o.h, int(proc), float(rate))
+
+    def set_user_parameter(self, k, value):
+        O.lib().oracle_set_user_parameter(self.o.h, int(k), float(value))
+
+    def recalculate_rates_matrix(self):
+        self.o.recalculate_rates_matrix()
+
+    def update_accum_rate(self):
+        self.o.update_accum_rate()
+
+    def update_integ_rate(self):
+        self.o.update_integ_rate()
+
+    def do_kmc_steps(self, n):
+        self.o.do_kmc_steps(n)
+
+    def get_next_kmc_step(self, traj=0):
+        return self.o.get_next_kmc_step()
+
+    def run_proc_nr(self, proc, site, traj=0):
+        self.o.run_proc_nr(proc, site)
+
+    def state(self, traj=0, fields=None):
+        ex = self.o.export()
+        rm, tot = self.o.rates_matrix()
+        return dict(lattice=ex["lattice"], as1=ex["as1"], as2=ex["as2"], nsites=ex["nsites"],
+                    procstat=ex["procstat"], integ=ex["integ"], accum=self.o.accum_rates(), rates_matrix=rm,
+                    totals=tot, kmc_time=self.o.kmc_time, kmc_time_step=self.o.kmc_time_step,
+                    kmc_step=self.o.kmc_step)
+
+
+def test_otf_dropin_sequence(monkeypatch):
+    monkeypatch.setattr(E, "OtfBatch", OracleOtfBatch)
+    m = fixture_model("intZGB_otf")
+    rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
+    params = {"J_CO_CO": 1.3, "J_O_CO": 0.7, "J_O_O": 1.9, "kDes": 1e-10, "yCO": 0.5}
+    base, lattice, proclist = kmc_model.configure(m, "otf")
+    assert proclist.backend == "otf" and kmc_model.proclist_pars.byst_co_ads == "nr_CO_1nn nr_O_1nn"
+    proclist.init((12, 10), "IntZGB", lattice.default_layer, 7, True)
+    for p, r in enumerate(rates, start=1):
+        base.set_rate_const(p, r)
+    for name, v in params.items():                      # set_rate_constants, run:2416-2427
+        proclist.update_user_parameter(getattr(proclist, name.lower()), v)
+    assert kmc_model.proclist_pars.get_user_parameter(proclist.j_o_co) == 0.7
+    proclist.recalculate_rates_matrix()
+    base.update_accum_rate()
+    base.update_integ_rate()
+    proclist.do_kmc_steps(800)
+
+    prog = PG.compile_model(m, "otf")
+    o = O.Oracle(prog, (12, 10), seed=7, rng=O.RNG_GFORTRAN)
+    o.set_rates(rates)
+    o.set_user_parameters([params[n] for n in OTF.user_parameters(m)])
+    o.recalculate_rates_matrix()
+    o.update_accum_rate()
+    o.update_integ_rate()
+    o.do_kmc_steps(800)
+    rm, tot = o.rates_matrix()
+    ex = o.export()
+    assert base.get_kmc_step() == 800 and base.get_kmc_time() == o.kmc_time
+    for p in range(1, len(rates) + 1):
+        assert base.get_procstat(p) == ex["procstat"][p - 1]
+        assert base.get_nrofsites(p) == ex["nsites"][p - 1]
+        assert base.get_rate(p) == tot[p - 1]
+        if ex["nsites"][p - 1]:
+            assert base.get_rate(p, 1) == rm[p - 1, 1]
+            assert base.get_avail_site(p, 1, 1) == ex["as1"][p - 1, 1]
+        assert base.get_integ_rate(p) == ex["integ"][p - 1]
+        assert base.get_accum_rate(p) == o.accum_rates()[p - 1]
+    np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
+    assert lattice.get_species((3, 4, 0, 1)) == ex["lattice"][3 + 12 * 4]
+    p, s = proclist.get_next_kmc_step()
+    assert (p, s) == o.get_next_kmc_step()
+    proclist.run_proc_nr(p, s)
+    o.run_proc_nr(p, s)
+    np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
+    import pytest
+    with pytest.raises(E.KMCError):
+        lattice.replace_species((0, 0, 0, 1), 0, 1)
+    lattice.deallocate_system()
+    assert not base.is_allocated()
