@@ -7,7 +7,9 @@ Fortran and the f2py build, a ``kmc_model.py`` that configures the engine's drop
 ``kmos.run`` reads: parameters, rate_constants, tof_count, site_names, representations,
 lattice_representation, species_tags, simulation_size, random_seed, setup_model.
 
-    python -m kmos_gb300.export model.ini out_dir [local_smart|lat_int]
+    python -m kmos_gb300.export model.ini out_dir [local_smart|lat_int|otf]
+
+An otf export's ``kmc_model`` also has ``proclist_pars`` (kmos.run imports it when present).
 """
 from __future__ import annotations
 
@@ -28,6 +30,8 @@ def export(model_path: str, out_dir: str, backend: str = "local_smart") -> None:
         fh.write("import kmc_settings as _settings\n")
         fh.write("from kmos_gb300.kmc_model import configure as _configure\n\n")
         fh.write("base, lattice, proclist = _configure(_settings.model_json, _settings.backend)\n")
+        if backend == "otf":
+            fh.write("from kmos_gb300.kmc_model import proclist_pars  # noqa: E402\n")
     out = []
     out.append("model_name = %r\n" % m.name)
     out.append("simulation_size = 20\nrandom_seed = 1\nbackend = %r\n\n" % backend)

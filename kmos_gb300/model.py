@@ -429,9 +429,12 @@ def load_xml(path: str) -> Model:
 
 
 def load(path: str) -> Model:
-    """Read a kmos project file by extension (``.ini`` or ``.xml``)."""
+    """Read a kmos project file by extension (``.ini`` or ``.xml``; ``.json``: this
+    package's JSON form)."""
     if path.endswith(".xml"):
         return load_xml(path)
+    if path.endswith(".json"):
+        return load_json(path)
     return load_ini(path)
 
 

@@ -106,3 +106,35 @@ def test_otf_dropin_sequence(monkeypatch):
         lattice.replace_species((0, 0, 0, 1), 0, 1)
     lattice.deallocate_system()
     assert not base.is_allocated()
+
+
+def test_otf_build_has_every_attribute_kmos_run_reads(tmp_path):
+    """The attributes kmos.run and the CLI read (tests/golden/kmc_model_attrs.json), on an
+    otf build, but the chemical-potential update (not offered) and names from docstring
+    examples; and an otf export directory imports with proclist_pars."""
+    import importlib
+    import json
+    import os
+    import sys
+    from conftest import GOLDEN
+    from kmos_gb300 import export
+    want = json.load(open(os.path.join(GOLDEN, "kmc_model_attrs.json")))
+    skip = {"lattice_bridge", "site", "co", "touchup_", "update_chempot"}
+    base, lattice, proclist = kmc_model.configure(fixture_model("intZGB_otf"), "otf")
+    for mod, obj in {"base": base, "lattice": lattice, "proclist": proclist}.items():
+        missing = [a for a in want[mod] if a not in skip and not hasattr(obj, a)]
+        assert not missing, (mod, missing)
+    out = os.path.join(str(tmp_path), "out")
+    export.export(os.path.join(GOLDEN, "models", "intZGB_otf.json"), out, "otf")
+    sys.path.insert(0, out)
+    for mod in ("kmc_settings", "kmc_model"):
+        sys.modules.pop(mod, None)
+    try:
+        drop_in = importlib.import_module("kmc_model")
+        assert drop_in.proclist.backend == "otf"
+        assert drop_in.proclist_pars.byst_co_ads == "nr_CO_1nn nr_O_1nn"
+        assert drop_in.proclist_pars.j_o_co == drop_in.proclist.j_o_co == 2
+    finally:
+        sys.path.remove(out)
+        for mod in ("kmc_settings", "kmc_model"):
+            sys.modules.pop(mod, None)
