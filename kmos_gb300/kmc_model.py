@@ -375,8 +375,18 @@ def _pars(S: _State) -> types.SimpleNamespace:
     ns.update_user_parameter = update_user_parameter
     ns.get_user_parameter = lambda param: float(values[int(param) - 1])
     ns.userpar = values
+    pid = S.model.process_ids()
     for proc in S.model.processes:
         setattr(ns, "byst_%s" % proc.name.lower(), " ".join(otf.nr_var_names(proc)))
+
+        def rate(nr_vars=(), _code=otf.compile_rate(S.model, proc)[1], _p=pid[proc.name]):
+            """rate_<name>(nr_vars) (io:2920-2965): the otf rate for given bystander
+            counts, from the current rate constant and user parameters (what
+            kmos.run's Model_Rate_Constants_OTF prints, run:1848-1882)."""
+            base = float(S.traj.rates()[_p - 1]) if S.traj is not None else 0.0
+            return otf.evaluate(_code, base, values, [int(v) for v in np.atleast_1d(nr_vars)])
+
+        setattr(ns, "rate_%s" % proc.name.lower(), rate)
     return ns
 
 

@@ -138,3 +138,24 @@ def test_otf_build_has_every_attribute_kmos_run_reads(tmp_path):
         sys.path.remove(out)
         for mod in ("kmc_settings", "kmc_model"):
             sys.modules.pop(mod, None)
+
+
+def test_rate_functions_of_proclist_pars(monkeypatch):
+    """proclist_pars.rate_<name>(nr_vars) and byst_<name>, as kmos.run's
+    Model_Rate_Constants_OTF calls them (run:1868-1882): the rate for given bystander
+    counts from the current rate constant and user parameters."""
+    monkeypatch.setattr(E, "OtfBatch", OracleOtfBatch)
+    m = fixture_model("intZGB_otf")
+    base, lattice, proclist = kmc_model.configure(m, "otf")
+    pars = kmc_model.proclist_pars
+    proclist.init((6, 6), "IntZGB", lattice.default_layer, 1, True)
+    base.set_rate_const(proclist.co_ads, 0.25)
+    for name, v in {"J_CO_CO": 1.3, "J_O_CO": 0.7}.items():
+        proclist.update_user_parameter(getattr(proclist, name.lower()), v)
+    nr_vars = pars.byst_co_ads.split()            # ['nr_CO_1nn', 'nr_O_1nn']
+    counts = np.zeros(len(nr_vars), int)
+    counts[nr_vars.index("nr_CO_1nn")], counts[nr_vars.index("nr_O_1nn")] = 2, 1
+    want = (0.25 * OTF.powi(0.7, 1, OTF.K_F64)) * OTF.powi(1.3, 2, OTF.K_F64)
+    assert pars.rate_co_ads(counts) == want
+    assert pars.rate_co_des() == 0.0 and pars.byst_co_des == ""
+    lattice.deallocate_system()
