@@ -50,7 +50,8 @@ def records(prog):
             byst.append([list(coord), pairs])
             pos += 2 + 2 * npairs
         out[p] = (nv, byst, [int(x) for x in w[pos:pos + nc]])
-        assert pos + nc <= int(w[off + p]) if p < prog.nproc else True
+        if p < prog.nproc:
+            assert pos + nc <= int(w[off + p])
     return out
 
 
@@ -60,7 +61,6 @@ def test_rate_functions_match_generated_fortran(name, gold):
     model = fixture_model(name)
     prog = PG.compile_model(model, "otf")
     recs = records(prog)
-    pid = model.process_ids()
     for p, ref in g["rates"].items():
         nv, byst, code = recs[int(p)]
         assert byst == ref["bystanders"], "process %s" % p
@@ -75,7 +75,6 @@ def test_rate_functions_match_generated_fortran(name, gold):
         from kmos_gb300.model import Process
         twin = Process(proc.name, proc.rate_constant, bystanders=proc.bystanders, otf_rate=text)
         assert OTF.compile_rate(model, twin)[1] == code, "process %s: %s" % (p, text)
-    assert pid  # numbering is the model's file order
 
 
 def run(expr, base=2.0, par=None, nr=None, model=None):
@@ -114,8 +113,8 @@ def test_intzgb_rates_equal_the_formula():
     model = fixture_model("intZGB_otf")
     prog = PG.compile_model(model, "otf")
     recs = records(prog)
-    par = OTF.user_parameter_values(model)
     assert OTF.user_parameters(model) == ["J_CO_CO", "J_O_CO", "J_O_O", "kDes", "yCO"]
+    assert OTF.user_parameter_values(model) == [1.0, 1.0, 1.0, 1e-10, 0.5]
     par = [1.3, 0.7, 1.9, 1e-10, 0.5]
     rng = np.random.default_rng(0)
     for _ in range(50):
