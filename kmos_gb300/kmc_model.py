@@ -316,7 +316,8 @@ def _proclist(S: _State) -> types.SimpleNamespace:
         layer = ns_default_layer if layer is None else int(layer)
         if S.backend == "otf":
             S.traj = _OtfTrajectory(S.program, size, layer, S.seed)
-            for k, v in enumerate(_pars(S).userpar[:len(S.model.parameters)], start=1):
+            pars = _pars(S)
+            for k, v in enumerate(pars.userpar[:int(S.program.words[23])], start=1):
                 S.traj.b.set_user_parameter(k, float(v))
         else:
             S.traj = E.Trajectory(S.program, size, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
@@ -362,7 +363,8 @@ def _pars(S: _State) -> types.SimpleNamespace:
     ns = types.SimpleNamespace()
     S.pars = ns
     names = otf.user_parameters(S.model)
-    values = np.zeros(max(len(names), 1))
+    mus = otf.chempot_names(S.model)
+    values = np.zeros(max(len(names) + len(mus), 1))   # user parameters, then chempots
     for k, n in enumerate(names, start=1):
         setattr(ns, n.lower(), k)
 
@@ -370,10 +372,26 @@ def _pars(S: _State) -> types.SimpleNamespace:
         if not 1 <= int(param) <= len(names):
             raise E.KMCError(1, "user parameter %s out of range" % param)
         values[int(param) - 1] = float(val)
-        S.t().b.set_user_parameter(int(param), float(val))
+        if S.traj is not None:
+            S.traj.b.set_user_parameter(int(param), float(val))
 
     ns.update_user_parameter = update_user_parameter
     ns.get_user_parameter = lambda param: float(values[int(param) - 1])
+    if mus:
+        # update_chempot(index, val) and the mu_* index constants (io:2740-2790)
+        for j, mu in enumerate(mus, start=1):
+            setattr(ns, mu.lower(), j)
+
+        def update_chempot(index, val):
+            if not 1 <= int(index) <= len(mus):
+                raise E.KMCError(1, "chemical potential %s out of range" % index)
+            k = len(names) + int(index)
+            values[k - 1] = float(val)
+            if S.traj is not None:
+                S.traj.b.set_user_parameter(k, float(val))
+
+        ns.update_chempot = update_chempot
+        ns.chempots = values[len(names):]
     ns.userpar = values
     pid = S.model.process_ids()
     for proc in S.model.processes:

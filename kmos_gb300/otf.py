@@ -35,7 +35,9 @@ OP_ADD (the add evaluates the rate), OP_STRIP and::
     OP_UPDATE   [h(arg=proc), coord]     if can_do(proc, site): update_rates_matrix(
                                          proc, site, gr_proc(cell of coord))
 
-Header word 22 = offset of P+1 rate-record offsets, word 23 = number of user parameters.
+Header word 22 = offset of P+1 rate-record offsets, word 23 = number of user parameters
+plus chemical potentials (``mu_*``, the generator's chempots array, which follow the
+parameters in the engine's parameter vector).
 Rate record of process p::
 
     [nbyst, nvars, ncode, stack, (coord, npairs, (species, var) * npairs) * nbyst, code...]
@@ -346,6 +348,24 @@ def nr_var_names(proc: Process) -> List[str]:
     return sorted(nr_vars, key=lambda x: (x.split("_")[2], x.split("_")[1]))
 
 
+def chempot_names(model: Model) -> List[str]:
+    """The ``mu_<species>`` chemical potentials any rate_constant or otf_rate names, sorted
+    (io:2966-2998): the generated module's ``chempots`` array, set by update_chempot.
+    Here they follow the user parameters in the engine's parameter vector."""
+    params = {p.name for p in model.parameters}
+    found = set()
+    for proc in model.processes:
+        for expr in (proc.rate_constant or "", proc.otf_rate or ""):
+            for line in expr.split("\n"):
+                try:
+                    toks = _tokens(line.replace("beta", "(1/(kboltzmann*T))"))
+                except ExprError:
+                    continue
+                found.update(t for ty, t, _a in toks if ty == tokenize.NAME and t.startswith("mu_")
+                             and t not in params)
+    return sorted(found)
+
+
 def compile_rate(model: Model, proc: Process) -> Tuple[List[str], List[int], int]:
     """(nr variable names, code, stack depth) of gr_<proc> (io:2800-2965, 3000-3122)."""
     params = sorted(p.name for p in model.parameters)
@@ -353,6 +373,8 @@ def compile_rate(model: Model, proc: Process) -> Tuple[List[str], List[int], int
     names: Dict[str, tuple] = {}
     for k, pn in enumerate(params):
         names[pn] = ("par", k)
+    for j, mu in enumerate(chempot_names(model)):   # chempots(mu) after the parameters
+        names[mu] = ("par", len(params) + j)
     for v, nv in enumerate(nr_vars):
         names[nv] = ("nr", v)
     c = _Compiler(names)

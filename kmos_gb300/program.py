@@ -822,7 +822,7 @@ class ProgramBuilder:
         header = [MAGIC, VERSION, BACKENDS["otf"], P, len(m.species), self.null, m.spuck,
                   m.dimension, 0, len(m.layers), off_proc, off_touch, off_groups,
                   off_site_layer, off_site_default, 0, max_ops, 0, 0, 0, 0, 0,
-                  off_rate, len(m.parameters)]
+                  off_rate, len(m.parameters) + len(otf.chempot_names(m))]
         w.words[:len(header)] = header
         w.words[15] = len(w.words)
         arr = np.array([x if x < 2**31 else x - 2**32 for x in w.words], dtype=np.int64).astype(np.int32)

@@ -159,3 +159,36 @@ def test_rate_functions_of_proclist_pars(monkeypatch):
     assert pars.rate_co_ads(counts) == want
     assert pars.rate_co_des() == 0.0 and pars.byst_co_des == ""
     lattice.deallocate_system()
+
+
+def test_chemical_potentials(monkeypatch):
+    """mu_* in an otf_rate: the generator's chempots array, set by update_chempot
+    (io:2740-2790), here the entries after the user parameters.  Every CO_ads entry's
+    rate after recalculate_rates_matrix is base_rate * exp(-mu_CO * nr_CO_1nn) of its cell."""
+    import math
+    monkeypatch.setattr(E, "OtfBatch", OracleOtfBatch)
+    m = fixture_model("intZGB_otf")
+    m.processes[0].otf_rate = "base_rate*exp(-mu_CO*nr_CO_1nn)"
+    assert OTF.chempot_names(m) == ["mu_CO"]
+    assert int(PG.compile_model(m, "otf").words[23]) == len(m.parameters) + 1
+    base, lattice, proclist = kmc_model.configure(m, "otf")
+    pars = kmc_model.proclist_pars
+    proclist.init((8, 8), "IntZGB", lattice.default_layer, 3, True)
+    rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
+    for p, r in enumerate(rates, start=1):
+        base.set_rate_const(p, r)
+    pars.update_chempot(pars.mu_co, 0.35)
+    assert pars.chempots[0] == 0.35
+    proclist.recalculate_rates_matrix()
+    proclist.do_kmc_steps(300)        # every event keeps the touched rates current
+    st = kmc_model._state.traj.b.state(0)
+    lat = st["lattice"]
+    co = proclist.co
+    n = base.get_nrofsites(proclist.co_ads)
+    assert n > 0
+    for i in range(1, n + 1):
+        site = base.get_avail_site(proclist.co_ads, i, 1)
+        x, y = (site - 1) % 8, (site - 1) // 8
+        nco = sum(lat[((x + dx) % 8) + 8 * ((y + dy) % 8)] == co for dx, dy in ((1, 0), (0, 1), (-1, 0), (0, -1)))
+        assert base.get_rate(proclist.co_ads, i) == 0.4 * math.exp(-(0.35 * nco))
+    lattice.deallocate_system()
