@@ -212,6 +212,43 @@ def cpu_sample(config: int, rounds: int = 1, steps: int = 0):
     return total / wall, cores, sample
 
 
+OTF_RATES = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
+OTF_PARAMS = [1.3, 0.7, 1.9, 1e-10, 0.5]   # J_CO_CO, J_O_CO, J_O_O, kDes, yCO
+
+
+def _otf_model_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "models", "intZGB_otf.json")
+
+
+def _otf_cpu_worker(args):
+    traj, steps = args
+    from kmos_gb300 import model as M, program as PG
+    from oracle import oracle as O
+    prog = PG.compile_model(M.load_json(_otf_model_path()), "otf")
+    o = O.Oracle(prog, (32, 32), seed=11, rng=O.RNG_PHILOX, traj=traj)
+    o.set_rates(OTF_RATES)
+    o.set_user_parameters(OTF_PARAMS)
+    o.recalculate_rates_matrix()
+    o.update_accum_rate()
+    o.do_kmc_steps(300)
+    t0 = time.perf_counter()
+    o.do_kmc_steps(steps)
+    return steps, time.perf_counter() - t0
+
+
+def otf_cpu_sample(steps: int = 800_000):
+    """The oracle's otf backend on all host cores, one intZGB trajectory (32 x 32) per
+    core process: (aggregate steps/s, cores, sample)."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_otf_cpu_worker, [(i, steps) for i in range(cores)])
+    wall = max(t for _, t in res)
+    sample = "%d trajectories x %d otf steps (intZGB 32x32), one process per core" % (cores, steps)
+    return sum(s for s, _ in res) / wall, cores, sample
+
+
 def replica_trajs(trajs, rank: int):
     """Philox trajectory ids of one rank's replica batch: the same workload with ids
     offset by rank * batch size, so ranks run disjoint, reproducible trajectories."""
@@ -453,13 +490,11 @@ def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
     (tests/golden/models/intZGB_otf.json, the reference's tests/export_test/intZGB_otf.xml)
     on a 32 x 32 lattice, 2048 Philox trajectories, steps/s over every trajectory from
     CUDA events around one do_kmc_steps launch (inputs resident), beside the oracle's
-    single-core steps/s on one trajectory of the same configuration."""
+    otf backend on every host core (one trajectory of the same configuration each)."""
     from kmos_gb300 import engine as E, model as M, otf as OTF, program as PG
-    m = M.load_json(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "models",
-                                 "intZGB_otf.json"))
+    m = M.load_json(_otf_model_path())
     prog = PG.compile_model(m, "otf")
-    rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
-    params = [1.3, 0.7, 1.9, 1e-10, 0.5]
+    rates, params = OTF_RATES, OTF_PARAMS
     size = (32, 32)
     b = E.OtfBatch(prog, size, ntraj=ntraj, seed=11, rng=E.RNG_PHILOX)
     b.set_rates(rates)
@@ -479,19 +514,8 @@ def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
            "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1}
     b.close()
     if cpu:
-        from oracle import oracle as O
-        o = O.Oracle(prog, size, seed=11, rng=O.RNG_PHILOX, traj=0)
-        o.set_rates(rates)
-        o.set_user_parameters(params)
-        o.recalculate_rates_matrix()
-        o.update_accum_rate()
-        o.do_kmc_steps(300)
-        n, t0 = 0, time.perf_counter()
-        while time.perf_counter() - t0 < 2.0:
-            o.do_kmc_steps(500)
-            n += 500
-        out["cpu_baseline"] = {"value": n / (time.perf_counter() - t0), "unit": "steps/s", "cores": 1,
-                               "kind": "port", "sample": "one trajectory, %d steps" % n}
+        value, cores, sample = otf_cpu_sample()
+        out["cpu_baseline"] = {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
     return out
 
 
