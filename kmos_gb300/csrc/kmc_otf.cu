@@ -21,9 +21,11 @@
 // One warp per trajectory.  A step: lanes re-sum the stale lists (one process per lane,
 // a serial chain each), lane 0 chains the process totals into accum_rates, every lane
 // advances the clock and integ_rates of its processes, lane 0 picks the process and the
-// entry (interval_search_real on accum_rates and on the chosen list's running sums) and
-// runs the process's op stream serially: guarded dels, replaces, rate updates and adds,
-// each rate from the process's rate program (gr_<name>, io:2800-2965).
+// entry (interval_search_real on accum_rates and on the chosen list's running sums), and
+// the event runs (run_event): lane 0 writes the lattice, the lanes load the table
+// positions and evaluate the add conditions and the rate programs (gr_<name>,
+// io:2800-2965) in parallel, lane 0 replays guarded dels, rate updates and adds in
+// program order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
