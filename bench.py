@@ -79,7 +79,9 @@ def parse():
     return ap.parse_args()
 
 
-DEFAULT_CHUNK = {1: 100000, 2: 20000, 3: 20000, 4: 10000}
+# kMC steps per trajectory per bench step.  Config 3's 40 000 make the default
+# --steps 20 --warmup 5 run (25 bench steps) the configuration's 1e6 steps per trajectory.
+DEFAULT_CHUNK = {1: 100000, 2: 20000, 3: 40000, 4: 10000}
 
 
 # ------------------------------------------------------------------ distributed
@@ -174,42 +176,88 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ CPU side
+def stratified(wl, k: int):
+    """k trajectory indices spread over the workload's parameters: the trajectories
+    sorted by (lattice side, T) for config 3, by y for config 2 and by T for config 4,
+    then taken at evenly spaced ranks (config 1 has one trajectory)."""
+    n = wl.n
+    notes = wl.notes
+    if "side" in notes:
+        key = lambda i: (int(notes["side"][i]), float(notes["T"][i]))  # noqa: E731
+    elif "y" in notes:
+        key = lambda i: float(notes["y"][i])  # noqa: E731
+    elif "T" in notes:
+        key = lambda i: float(notes["T"][i])  # noqa: E731
+    else:
+        key = lambda i: i  # noqa: E731
+    order = sorted(range(n), key=key)
+    return [order[min(n - 1, int((j + 0.5) * n / k))] for j in range(k)]
+
+
 def _cpu_worker(args):
-    config, idx, steps = args
+    """One trajectory of the workload on the oracle: `start` untimed steps (the part of
+    the run before the GPU's timed region), then `steps` timed ones with the book-keeping
+    access counters on.  Returns (steps done, seconds, int32 table accesses, occupation
+    accesses) of the timed part."""
+    config, ntraj, sides, idx, start, steps = args
     from kmos_gb300 import configs
     from oracle import oracle as O
-    wl = configs.build(config, n=idx + 1, steps=steps)
+    wl = configs.build(config, n=ntraj, sides=sides)
     o = O.Oracle(wl.program, wl.sizes[idx], seed=wl.seeds[idx], rng=O.RNG_PHILOX, traj=wl.trajs[idx])
     o.set_rates(wl.rates[idx])
     o.update_accum_rate()
+    try:
+        o.do_kmc_steps(start)
+    except O.OracleError:
+        return 0, 0.0, 0, 0  # absorbing state reached before the sample: nothing to time
+    k0 = o.kmc_step
+    o.reset_counters()
     t0 = time.perf_counter()
     try:
         o.do_kmc_steps(steps)
     except O.OracleError:
         pass  # absorbing state reached: the trajectory ends, as in the reference
-    return o.kmc_step, time.perf_counter() - t0
+    dt = time.perf_counter() - t0
+    n_as, n_occ = o.counters()
+    return o.kmc_step - k0, dt, n_as, n_occ
 
 
-CPU_STEPS = {1: 2_000_000, 2: 1_000_000, 3: 300_000, 4: 1_000_000}
+CPU_STEPS = {1: 2_000_000, 2: 1_000_000, 3: 800_000, 4: 1_000_000}
+AUTOTUNE_PROBE_STEPS = 9 * 500   # steps the default autotune run advances every trajectory
 
 
-def cpu_sample(config: int, rounds: int = 1, steps: int = 0):
-    """The oracle (the CPU restatement of the reference loop, one process per core, each
-    on its own trajectory) on all host cores.  Returns (steps/s aggregate, cores, sample)."""
+def cpu_sample(config: int, start: int, steps: int, ntraj=None, sides=None):
+    """The oracle (the CPU restatement of the reference loop) on all host cores, one
+    process per core, on a stratified sample of the workload's trajectories (at least 16),
+    each run through the same phase as the GPU's timed region: `start` untimed steps, then
+    `steps` timed ones.  Returns (aggregate steps/s, cores, sample text, B_step, N_as, N_occ)
+    with the per-step bytes averaged over the sampled trajectories."""
+    from kmos_gb300 import configs
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    steps = steps or CPU_STEPS[config]
+    wl = configs.build(config, n=ntraj, sides=sides)
+    k = max(16, cores)
+    idxs = stratified(wl, k)
     ctx = mp.get_context("spawn")
-    total, wall = 0, 0.0
+    total, wall, per_step = 0, 0.0, []
+    sum_as = sum_occ = 0.0
     with ctx.Pool(cores) as pool:
-        for r in range(rounds):
-            # all workers run at once; the slowest one's own timer bounds the round
-            res = pool.map(_cpu_worker, [(config, (r * cores + i) % 64, steps) for i in range(cores)])
-            wall += max(t for _, t in res)
-            total += sum(s for s, _ in res)
-    sample = "%d trajectories x %d kMC steps of config %d, one process per core" % (cores * rounds, steps, config)
-    return total / wall, cores, sample
+        for r in range(0, k, cores):
+            # all workers of a round run at once; the slowest one's own timer bounds it
+            res = pool.map(_cpu_worker, [(config, ntraj, sides, i, start, steps) for i in idxs[r:r + cores]])
+            wall += max(t for _, t, _a, _o in res)
+            total += sum(s for s, _t, _a, _o in res)
+            for s_, _t, a_, o_ in res:
+                if s_ > 0:
+                    per_step.append((a_ / s_, o_ / s_))
+    P = wl.program.nproc
+    n_as = sum(a for a, _ in per_step) / max(1, len(per_step))
+    n_occ = sum(o for _, o in per_step) / max(1, len(per_step))
+    bstep = 20 * P + 28 * P + 28 + 4 * n_as + wl.occupation_bytes * n_occ
+    sample = ("%d trajectories of config %d (stratified over the workload's parameters), each %d untimed then "
+              "%d timed kMC steps, one process per core" % (k, config, start, steps))
+    return total / wall, cores, sample, bstep, n_as, n_occ
 
 
 OTF_RATES = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
@@ -256,33 +304,25 @@ def replica_trajs(trajs, rank: int):
     return [int(t) + rank * n for t in trajs]
 
 
-def step_bytes(config: int, chunk: int = 50000):
-    """Algorithmic bytes per kMC step: 20P + 28P + 28 + 4*N_as + b_occ*N_occ, with N_as /
-    N_occ the mean int32 book-keeping / occupation accesses of run_proc_nr counted by
-    the instrumented oracle on this workload (int8 occupation, b_occ = 1)."""
-    from kmos_gb300 import configs
-    from oracle import oracle as O
-    wl = configs.build(config, n=1, steps=chunk)
-    o = O.Oracle(wl.program, wl.sizes[0], seed=wl.seeds[0], rng=O.RNG_PHILOX, traj=wl.trajs[0])
-    o.set_rates(wl.rates[0])
-    o.update_accum_rate()
-    o.do_kmc_steps(chunk)
-    o.reset_counters()
-    o.do_kmc_steps(chunk)
-    n_as, n_occ = o.counters()
-    P = wl.program.nproc
-    n_as, n_occ = n_as / chunk, n_occ / chunk
-    return 20 * P + 28 * P + 28 + 4 * n_as + 1 * n_occ, n_as, n_occ
+def timed_phase(args):
+    """(untimed steps before the GPU's timed region, timed steps) per trajectory for
+    the arguments given, with the default autotune run."""
+    chunk = args.chunk or DEFAULT_CHUNK[args.config]
+    return AUTOTUNE_PROBE_STEPS + args.warmup * chunk, args.steps * chunk
 
 
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         dist.close()
         return
-    warm = [cpu_sample(args.config, steps=args.cpu_steps) for _ in range(min(args.warmup, 1))]
-    vals = [cpu_sample(args.config, steps=args.cpu_steps) for _ in range(max(1, min(args.steps, 3)))]
-    value = statistics.median(v for v, _c, _s in vals)
-    _v, cores, sample = vals[0]
+    start, length = timed_phase(args)
+    steps = args.cpu_steps or min(length, CPU_STEPS[args.config])
+    sides = [int(x) for x in args.sides.split(",")] if args.sides else None
+    ntraj = args.ntraj or None
+    warm = [cpu_sample(args.config, start, steps, ntraj, sides) for _ in range(min(args.warmup, 1))]
+    vals = [cpu_sample(args.config, start, steps, ntraj, sides) for _ in range(max(1, min(args.steps, 3)))]
+    value = statistics.median(v[0] for v in vals)
+    cores, sample = vals[0][1], vals[0][2]
     from kmos_gb300 import configs
     wl = configs.build(args.config, n=1, steps=1)
     line = {
@@ -308,7 +348,6 @@ def run_ours(args, dist: Dist):
     wl = configs.build(args.config, n=args.ntraj or None, sides=sides)
     n = wl.n
     dev = dist.local
-    pool_probe = None
     E.load()
     # size the arena from the per-slot byte counts
     pool = E.Pool(arena_bytes=1 << 20, max_slots=1, device=dev)
@@ -333,20 +372,32 @@ def run_ours(args, dist: Dist):
     slots = [slots[i] for i in order]
     P = wl.program.nproc
 
+    spl = chunk  # kMC steps per launch; a bench step is chunk / spl launches
+
     def launch():
-        if args.graph:
-            pool.run_graph(slots, chunk, sync=False)
-        else:
-            pool.run(slots, chunk, sync=False)
+        for _ in range(chunk // spl):
+            if args.graph:
+                pool.run_graph(slots, spl, sync=False)
+            else:
+                pool.run(slots, spl, sync=False)
 
     tuned = None
+    nwarm = args.warmup
     if args.autotune and not (args.warps >= 0 or args.bps or not args.fast):
         # part of the warm-up: probes advance the real trajectories (results do not
         # depend on the launch shape)
         from kmos_gb300 import autotune
         tuned = autotune.tune(pool, slots)
         tuned.pop("trials", None)
-    for _ in range(args.warmup):
+        if args.graph and args.warmup >= 1:
+            # the first warm-up bench steps are the steps-per-launch trials: each runs
+            # one bench step's chunk as 1, 2 or 4 launches
+            t2 = autotune.tune_steps_per_launch(pool, slots, chunk, splits=(1, 2, 4)[:args.warmup])
+            spl = t2["steps_per_launch"]
+            nwarm -= len(t2["trials"])
+            tuned["steps_per_launch"] = spl
+            tuned["steps_per_launch_trials"] = [{k: r[k] for k in ("launches", "steps_per_s")} for r in t2["trials"]]
+    for _ in range(max(0, nwarm)):
         launch()
     pool.sync()
     _ps, _ig, _t, ksteps0, _st = pool.results(slots, P)
@@ -382,7 +433,8 @@ def run_ours(args, dist: Dist):
     k_before = ksteps
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        pool.run(slots, chunk, sync=False)
+        for _l in range(chunk // spl):
+            pool.run(slots, spl, sync=False)
         res = pool.results(slots, P)
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = dist.sum(int((res[3] - k_before).sum())) / e2e_s
@@ -397,23 +449,30 @@ def run_ours(args, dist: Dist):
         if os.path.exists(pk):
             peaks = _json.load(open(pk))
         peak = peaks.get("hbm_gbs", 6800.0)
-        bstep, n_as, n_occ = step_bytes(args.config)
-        per_launch_s = (ms / 1e3) / args.steps
-        achieved = bstep * (kmc_steps_rank / args.steps) / per_launch_s / 1e9
+        # the oracle on a stratified sample of the workload, through the same phase of the
+        # run as the timed region: B_step (mean over the sample) and the CPU baseline
+        import numpy as _np
+        start = int(_np.median(ksteps0))
+        cpu_steps = args.cpu_steps or min(args.steps * chunk, CPU_STEPS[args.config])
+        v, cores, sample, bstep, n_as, n_occ = cpu_sample(args.config, start, cpu_steps, args.ntraj or None, sides)
+        # per launch: the kernel's bytes over its average duration
+        launches_timed = args.steps * (chunk // spl)
+        per_launch_s = (ms / 1e3) / launches_timed
+        achieved = bstep * (kmc_steps_rank / launches_timed) / per_launch_s / 1e9
         traffic = None
         prof = os.path.join(ROOT, "profiles", "traffic_config%d.json" % args.config)
         if os.path.exists(prof):
             tr = _json.load(open(prof))
-            traffic = tr.get("bytes_per_kmc_step", 0) * kmc_steps_rank / args.steps
+            traffic = tr.get("bytes_per_kmc_step", 0) * kmc_steps_rank / launches_timed
         cpu = None
         if args.cpu_baseline:
-            v, cores, sample = cpu_sample(args.config, steps=args.cpu_steps)
             cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": wl.name, "trajectories_per_gpu": n, "kmc_steps_per_traj_per_step": chunk,
+                       "timed_kmc_steps_per_traj": [start, start + args.steps * chunk],
                        "active_at_end": active,
                        "lattice": "x".join(str(v) for v in wl.sizes[0][:2]) if args.config != 3 else "uneven 16..256",
                        "nproc": P, "backend": wl.backend, "rng": "philox4x32-10",
@@ -423,6 +482,7 @@ def run_ours(args, dist: Dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "bytes_per_kmc_step": bstep, "n_as": n_as, "n_occ": n_occ,
+                         "bytes_sample": "mean over the cpu_baseline sample's trajectories",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -469,7 +529,7 @@ def plain_dropin(wl):
 def serving_sample():
     """A short run of the serving loop on the configuration-5 request stream (1 s of
     Poisson arrivals at 500/s, steps x 0.05), after the timed region: p50 / p99 request
-    latency and served steps/s.  profiles/serving_config5.md has the full-size runs."""
+    latency and served steps/s."""
     from kmos_gb300 import configs, serving
     reqs, progs = configs.serving_requests(rate=500.0, duration=1.0, steps_scale=0.05)
     srv = serving.Server(arena_bytes=16 << 30, max_slots=4096, quantum=20000, policy="fifo")

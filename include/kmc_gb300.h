@@ -191,7 +191,9 @@ KMC_API int kmc_pool_get_tables(kmc_pool *pool, int32_t slot, int32_t *as1, int3
  * partial pressures) for a trajectory that keeps its lattice, tables and clock. */
 KMC_API int kmc_pool_set_rates(kmc_pool *pool, int32_t slot, const double *rates);
 /* Occupation counts of many slots at once, reduced on the device: out[i] holds the
- * [nspecies][spuck] counts of slots[i] (int64), with stride `stride` int64 per slot. */
+ * [nspecies][spuck] counts of slots[i] (int64), with stride `stride` int64 per slot.
+ * A stride below nspecies * spuck of any listed slot's model returns KMC_ERR_ARG.
+ * Replaces get_occupation (proclist_generic_subroutines.mpy:113-158) for many slots. */
 KMC_API int kmc_pool_occupation_counts(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride, int64_t *out);
 /* Results of many slots in one device gather and one copy: for slots[i], procstat
  * (int64) and integ_rates (double) into rows of `stride` entries, kmc_time and
@@ -200,15 +202,17 @@ KMC_API int kmc_pool_get_results(kmc_pool *pool, const int32_t *slots, int32_t n
                                  int64_t *procstat, double *integ, double *times, int64_t *steps,
                                  int32_t *status);
 /* kmc_pool_occupation_counts for callers that must not allocate device memory: code
- * running under a fixed device-memory budget that is already spent, or in a stream-ordered
- * section where a cudaMalloc would synchronise the device or is forbidden (an allocator's
- * own callback, a real-time serving loop).  It has no counterpart in the reference.  Its
+ * running under a fixed device-memory budget that is already spent (a serving process
+ * that has given all of it to resident trajectories), or a real-time loop where a
+ * cudaMalloc would synchronise the device.  It has no counterpart in the reference.  Its
  * scratch (slot list and counters) is one static device array of about 2 MB that every
  * call shares: at most KMC_STATIC_OCC_MAX_SLOTS slots and KMC_STATIC_OCC_MAX_STRIDE
- * counters per slot (larger requests return KMC_ERR_ARG).  The first call on a device
- * looks the array's address up (cudaGetSymbolAddress), so make that call before any
- * stream capture.  Calls whose work overlaps on the GPU (other threads, other pools'
- * streams) race on the array: serialise them. */
+ * counters per slot (larger requests, and strides below nspecies * spuck of a listed
+ * slot's model, return KMC_ERR_ARG).  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress).  Every call copies to and from host memory and
+ * synchronises the pool's stream, so it must not be made during a stream capture or
+ * from a CUDA host callback.  Calls whose work overlaps on the GPU (other threads, other
+ * pools' streams) race on the array: serialise them. */
 #define KMC_STATIC_OCC_MAX_SLOTS 4096
 #define KMC_STATIC_OCC_MAX_STRIDE 64
 KMC_API int kmc_pool_occupation_counts_static(kmc_pool *pool, const int32_t *slots, int32_t n, int32_t stride,

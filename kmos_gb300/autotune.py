@@ -6,8 +6,9 @@ each probe advances them by ``probe_steps`` steps, which the caller counts as wa
 as part of the requested steps.  It picks the launch shape (the balanced one-block-per-SM
 shape, or 2, 4 or 8 warps per block with as many blocks as fit), the step path (gather /
 replay or serial interpreter) and the table placement (the model's hot section in shared
-memory or read from global memory) with the highest measured steps/s, sets them on the
-pool, and returns steps per launch for about ``target_ms`` per launch.
+memory or read from global memory) with the highest measured steps/s and sets them on
+the pool (``tune``); then, for runs of a given length, how many steps each launch takes
+(``tune_steps_per_launch``).
 """
 from __future__ import annotations
 
@@ -16,7 +17,7 @@ from typing import Dict, List, Sequence
 from . import engine as E
 
 
-def tune(pool: E.Pool, slots: Sequence[int], probe_steps: int = 500, target_ms: float = 100.0,
+def tune(pool: E.Pool, slots: Sequence[int], probe_steps: int = 500,
          warps=(0, 2, 4, 8), paths=(True, False)) -> Dict:
     results: List[Dict] = []
     for fast in paths:
@@ -43,8 +44,28 @@ def tune(pool: E.Pool, slots: Sequence[int], probe_steps: int = 500, target_ms: 
         best = trial
     else:
         pool.set_table_placement(True)
-    per_traj_rate = best["steps_per_s"] / len(slots)
-    steps = int(max(1000, min(1_000_000, per_traj_rate * target_ms / 1e3)))
     return {"warps_per_block": best["warps"], "fast_path": best["fast"], "tables": best.get("tables", "shared"),
-            "steps_per_launch": steps,
             "probe_steps_per_trajectory": probe_steps * len(results), "trials": results}
+
+
+def tune_steps_per_launch(pool: E.Pool, slots: Sequence[int], total: int, splits=(1, 2, 4)) -> Dict:
+    """Steps per launch for runs of ``total`` kMC steps per trajectory.  Candidate ``s``
+    runs the ``total`` steps as ``s`` replays of a captured launch of ``total / s`` steps
+    on the real trajectories (which the caller counts as warm-up); the candidate with the
+    least device time (CUDA events around each replay, capture excluded) wins.  A launch
+    ends when its slowest trajectory has done its steps, so fewer, longer launches pay
+    that tail less often; shorter ones hand control back to the host sooner."""
+    trials = []
+    for s in splits:
+        if total % s:
+            continue
+        spl = total // s
+        ms = 0.0
+        for _ in range(s):
+            pool.run_graph(slots, spl, sync=True)
+            ms += pool.last_kernel_ms()
+        trials.append({"launches": s, "steps_per_launch": spl, "ms": ms,
+                       "steps_per_s": len(slots) * total / ms * 1e3})
+    best = max(trials, key=lambda r: r["steps_per_s"])
+    return {"steps_per_launch": best["steps_per_launch"], "launches_per_run": best["launches"],
+            "probe_steps_per_trajectory": total * len(trials), "trials": trials}

@@ -861,7 +861,10 @@ __global__ void kmc_occupation_kernel(const SlotDev *slots, const ModelDev *mode
     if (spc >= 0 && spc < ns && spc < 32) atomicAdd(&hist[spc * 32 + (s % sp)], 1u);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < ns * sp; i += blockDim.x)
+  // a row holds `stride` counters: the host refuses strides below ns * sp, and the copy
+  // stops at the row's end whatever it is given
+  const int nc = min(ns * sp, stride);
+  for (int i = threadIdx.x; i < nc; i += blockDim.x)
     out[(size_t)item * stride + i] = hist[(i / sp) * 32 + (i % sp)];
 }
 
@@ -1382,6 +1385,21 @@ int check_slot(kmc_pool *p, int slot) {
   return KMC_OK;
 }
 
+// Occupation rows of `stride` counters: every listed slot admitted and its model's
+// nspecies * spuck counters fitting in one row (get_occupation's (0:nspecies-1, 1:spuck)
+// matrix, proclist_generic_subroutines.mpy:113-158).
+int check_occupation_list(kmc_pool *p, const int32_t *slots, int n, int stride) {
+  for (int i = 0; i < n; i++) {
+    int rc = check_slot(p, slots[i]);
+    if (rc) return rc;
+    const ModelDev &m = p->models[p->slots[slots[i]].dev.model].dev;
+    if (stride < m.nspecies * m.spuck)
+      return fail(KMC_ERR_ARG, "occupation stride " + std::to_string(stride) + " below nspecies * spuck = " +
+                                   std::to_string(m.nspecies * m.spuck) + " of slot " + std::to_string(slots[i]));
+  }
+  return KMC_OK;
+}
+
 int run_command(kmc_pool *p, int slot, int cmd, int a0, int a1, int a2, int32_t *proc, int32_t *site,
                 const int32_t *d_list) {
   CmdArgs c;
@@ -1819,8 +1837,8 @@ int kmc_pool_get_tables(kmc_pool *p, int32_t slot, int32_t *as1, int32_t *as2) {
 
 int kmc_pool_occupation_counts(kmc_pool *p, const int32_t *slots, int32_t n, int32_t stride, int64_t *out) {
   if (!p || n < 1 || !slots || !out || stride < 1) return fail(KMC_ERR_ARG, "bad arguments");
-  for (int i = 0; i < n; i++) {
-    int rc = check_slot(p, slots[i]);
+  {
+    int rc = check_occupation_list(p, slots, n, stride);
     if (rc) return rc;
   }
   AsyncScratch s_list(p->stream), s_out(p->stream);
@@ -1907,8 +1925,8 @@ int kmc_pool_occupation_counts_static(kmc_pool *p, const int32_t *slots, int32_t
   if (stride < 1 || stride > KMC_STATIC_OCC_MAX_STRIDE)
     return fail(KMC_ERR_ARG, "kmc_pool_occupation_counts_static: stride must be 1.." +
                                  std::to_string(KMC_STATIC_OCC_MAX_STRIDE));
-  for (int i = 0; i < n; i++) {
-    int rc = check_slot(p, slots[i]);
+  {
+    int rc = check_occupation_list(p, slots, n, stride);
     if (rc) return rc;
   }
   if (p->device < 0 || p->device >= kMaxDevices) return fail(KMC_ERR_ARG, "device index beyond the static table");

@@ -329,10 +329,11 @@ def nr_var_names(proc: Process) -> List[str]:
     (io:2800-2830): every (allowed species, flag) pair of the bystanders plus those the
     expression names, sorted by (flag, species) as split on underscores."""
     used = set()
-    for line in (proc.otf_rate or "").split("\n"):
-        for _ty, s, _a in _tokens(line.replace("base_rate", "rates").replace("otf_rate", "gr")):
-            if s.startswith("nr_"):
-                used.add(s)
+    # the whole expression is tokenized at once, as _parse_otf_rate does (io:3066-3085)
+    expr = (proc.otf_rate or "").replace("base_rate", "rates").replace("otf_rate", "gr")
+    for _ty, s, _a in _tokens(expr.replace("beta", "(1/(kboltzmann*T))")):
+        if s.startswith("nr_"):
+            used.add(s)
     nr_vars = list(used)
     specs: Dict[str, List[str]] = {}
     flags = []
@@ -351,18 +352,16 @@ def nr_var_names(proc: Process) -> List[str]:
 def chempot_names(model: Model) -> List[str]:
     """The ``mu_<species>`` chemical potentials any rate_constant or otf_rate names, sorted
     (io:2966-2998): the generated module's ``chempots`` array, set by update_chempot.
-    Here they follow the user parameters in the engine's parameter vector."""
-    params = {p.name for p in model.parameters}
+    Here they follow the user parameters in the engine's parameter vector.  As in the
+    reference, each expression is tokenized whole after the rate aliases (an expression
+    that does not tokenize is an error), and every ``mu_`` name is a chemical potential,
+    also when a user parameter has that name (_parse_otf_rate tests ``mu_`` first,
+    io:3086-3090)."""
     found = set()
     for proc in model.processes:
         for expr in (proc.rate_constant or "", proc.otf_rate or ""):
-            for line in expr.split("\n"):
-                try:
-                    toks = _tokens(line.replace("beta", "(1/(kboltzmann*T))"))
-                except ExprError:
-                    continue
-                found.update(t for ty, t, _a in toks if ty == tokenize.NAME and t.startswith("mu_")
-                             and t not in params)
+            toks = _tokens(expr.replace("beta", "(1/(kboltzmann*T))"))
+            found.update(t for ty, t, _a in toks if ty == tokenize.NAME and t.startswith("mu_"))
     return sorted(found)
 
 

@@ -1,6 +1,6 @@
 """Generates the golden fixtures under tests/golden/ from the reference checkout.
 
-Run in a container that has mhoffman/kmos at KMOS_REFERENCE (default /root/reference);
+Run with KMOS_REFERENCE set to a checkout of mhoffman/kmos;
 the committed outputs are what the tests read, so the tests never need the reference.
 
 Outputs
@@ -31,7 +31,9 @@ from unittest import mock
 
 import numpy as np
 
-REF = os.environ.get("KMOS_REFERENCE", "/root/reference")
+REF = os.environ.get("KMOS_REFERENCE")
+if not REF:
+    raise SystemExit("set KMOS_REFERENCE to a checkout of mhoffman/kmos")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)

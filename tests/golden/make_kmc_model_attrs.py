@@ -3,14 +3,16 @@ proclist objects that kmos.run and the kmos CLI read (every ``base.X``, ``lattic
 ``proclist.X`` and ``self.base.X`` ... in their source), the list the drop-in module
 (kmos_gb300.kmc_model) must provide.
 
-Run in a container that has mhoffman/kmos at KMOS_REFERENCE (default /root/reference):
+Run with KMOS_REFERENCE set to a checkout of mhoffman/kmos:
     python tests/golden/make_kmc_model_attrs.py
 """
 import json
 import os
 import re
 
-REF = os.environ.get("KMOS_REFERENCE", "/root/reference")
+REF = os.environ.get("KMOS_REFERENCE")
+if not REF:
+    raise SystemExit("set KMOS_REFERENCE to a checkout of mhoffman/kmos")
 FILES = ["kmos/run/__init__.py", "kmos/cli.py"]
 HERE = os.path.dirname(os.path.abspath(__file__))
 

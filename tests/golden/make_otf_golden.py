@@ -1,6 +1,6 @@
 """Generates the otf-backend golden fixtures from the reference checkout.
 
-Run in a container that has mhoffman/kmos at KMOS_REFERENCE (default /root/reference);
+Run with KMOS_REFERENCE set to a checkout of mhoffman/kmos;
 the tests read only the committed outputs.
 
 Outputs
@@ -19,7 +19,9 @@ import json
 import os
 import sys
 
-REF = os.environ.get("KMOS_REFERENCE", "/root/reference")
+REF = os.environ.get("KMOS_REFERENCE")
+if not REF:
+    raise SystemExit("set KMOS_REFERENCE to a checkout of mhoffman/kmos")
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, HERE)

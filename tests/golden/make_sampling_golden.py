@@ -8,7 +8,7 @@ KMC_Model.get_std_sampled_data and KMC_Model.get_atoms run unmodified on that st
 The committed JSON pins oracle/sampling.py (the oracle for the engine's on-device
 sampling) to the reference's Python arithmetic.
 
-Run in a container that has mhoffman/kmos at KMOS_REFERENCE (default /root/reference):
+Run with KMOS_REFERENCE set to a checkout of mhoffman/kmos:
     python tests/golden/make_sampling_golden.py
 """
 import json

@@ -192,3 +192,45 @@ def test_chemical_potentials(monkeypatch):
         nco = sum(lat[((x + dx) % 8) + 8 * ((y + dy) % 8)] == co for dx, dy in ((1, 0), (0, 1), (-1, 0), (0, -1)))
         assert base.get_rate(proclist.co_ads, i) == 0.4 * math.exp(-(0.35 * nco))
     lattice.deallocate_system()
+
+
+def test_mu_names_are_chemical_potentials_even_when_a_parameter_has_the_name(monkeypatch):
+    """The reference's _parse_otf_rate (io:3086-3090) tests ``mu_`` before the user
+    parameters, so a parameter named mu_CO never shadows the chemical potential: the
+    rate reads chempots, not the parameter's value."""
+    import math
+    from kmos_gb300 import model as M
+    monkeypatch.setattr(E, "OtfBatch", OracleOtfBatch)
+    m = fixture_model("intZGB_otf")
+    m.parameters.append(M.Parameter(name="mu_CO", value="9.0"))
+    m.processes[0].otf_rate = "base_rate*exp(-mu_CO*nr_CO_1nn)"
+    assert OTF.chempot_names(m) == ["mu_CO"]
+    base, lattice, proclist = kmc_model.configure(m, "otf")
+    pars = kmc_model.proclist_pars
+    proclist.init((8, 8), "IntZGB", lattice.default_layer, 3, True)
+    for p, r in enumerate([0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3], start=1):
+        base.set_rate_const(p, r)
+    pars.update_chempot(pars.mu_co, 0.35)
+    proclist.recalculate_rates_matrix()
+    proclist.do_kmc_steps(300)
+    lat = kmc_model._state.traj.b.state(0)["lattice"]
+    n = base.get_nrofsites(proclist.co_ads)
+    assert n > 0
+    for i in range(1, n + 1):
+        site = base.get_avail_site(proclist.co_ads, i, 1)
+        x, y = (site - 1) % 8, (site - 1) // 8
+        nco = sum(lat[((x + dx) % 8) + 8 * ((y + dy) % 8)] == proclist.co
+                  for dx, dy in ((1, 0), (0, 1), (-1, 0), (0, -1)))
+        assert base.get_rate(proclist.co_ads, i) == 0.4 * math.exp(-(0.35 * nco))
+    lattice.deallocate_system()
+
+
+def test_an_expression_that_does_not_tokenize_is_refused():
+    """As the reference raises on a tokenize error (io:3080-3085), so does the compiler."""
+    import pytest
+    m = fixture_model("intZGB_otf")
+    m.processes[0].otf_rate = "base_rate*exp(-(mu_CO*nr_CO_1nn)"
+    with pytest.raises(OTF.ExprError):
+        OTF.chempot_names(m)
+    with pytest.raises(OTF.ExprError):
+        PG.compile_model(m, "otf")
