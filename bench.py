@@ -50,8 +50,8 @@ UNIT = "steps/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4])
     ap.add_argument("--chunk", type=int, default=0, help="kMC steps per trajectory per bench step")
@@ -223,7 +223,7 @@ def _cpu_worker(args):
 
 
 CPU_STEPS = {1: 2_000_000, 2: 1_000_000, 3: 800_000, 4: 1_000_000}
-AUTOTUNE_PROBE_STEPS = 9 * 500   # steps the default autotune run advances every trajectory
+AUTOTUNE_PROBE_STEPS = 11 * 500   # steps the default autotune run advances every trajectory
 
 
 def cpu_sample(config: int, start: int, steps: int, ntraj=None, sides=None):
@@ -388,7 +388,8 @@ def run_ours(args, dist: Dist):
         # depend on the launch shape)
         from kmos_gb300 import autotune
         tuned = autotune.tune(pool, slots)
-        tuned.pop("trials", None)
+        tuned["trials"] = [{k: r[k] for k in ("fast", "warps", "tables", "tpw", "steps_per_s") if k in r}
+                           for r in tuned["trials"]]
         if args.graph and args.warmup >= 1:
             # the first warm-up bench steps are the steps-per-launch trials: each runs
             # one bench step's chunk as 1, 2 or 4 launches
@@ -494,6 +495,8 @@ def run_ours(args, dist: Dist):
     extras = []
     if line is not None and args.plain:
         extras.append(("plain_dropin", lambda: plain_dropin(wl)))
+        if args.config != 1:
+            extras.append(("plain_dropin_config1", lambda: plain_dropin(configs.build(1), steps=200000)))
     if line is not None and args.serving and dist.world == 1:
         extras.append(("serving", serving_sample))
     if line is not None and args.otf and dist.world == 1:
@@ -508,12 +511,12 @@ def run_ours(args, dist: Dist):
     dist.close()
 
 
-def plain_dropin(wl):
+def plain_dropin(wl, steps: int = 20000):
     """The plain method: one trajectory of the workload (its first) stepped through the
     handle API (kmc_create / kmc_do_steps, what the f2py module calls), after the timed
-    region."""
+    region; wall time of the do_kmc_steps call, as `kmos benchmark` times it
+    (kmos/cli.py:293-312)."""
     from kmos_gb300 import engine as E
-    steps = 20000
     with E.Trajectory(wl.program, wl.sizes[0], seed=wl.seeds[0], rng=E.RNG_PHILOX, traj=wl.trajs[0]) as g:
         g.set_rates(wl.rates[0])
         g.update_accum_rate()

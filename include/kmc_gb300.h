@@ -221,6 +221,25 @@ KMC_API int kmc_pool_occupation_counts_static(kmc_pool *pool, const int32_t *slo
  * blocks per SM (0 = as many as fit), or warps_per_block 0 = balanced: one block per SM,
  * the run's trajectories split evenly over the SMs in the fewest rounds per warp. */
 KMC_API int kmc_pool_set_launch(kmc_pool *pool, int32_t warps_per_block, int32_t blocks_per_sm);
+/* Trajectories per warp of kmc_pool_run: 1 (default, 32 lanes per trajectory) or 2
+ * (16 lanes each, for models of up to 64 processes; larger models keep one).  Two per
+ * warp double the trajectories an SM holds at a given register budget and let one warp
+ * instruction advance both wherever their steps take the same branches.  Results do not
+ * depend on it.  The reference has one trajectory per process (one do_kmc_steps loop,
+ * proclist_generic_subroutines.mpy:1-44); this is a batching knob of this library. */
+KMC_API int kmc_pool_set_trajectories_per_warp(kmc_pool *pool, int32_t n);
+/* 1 (default): when every trajectory of a launch fits, each one's lattice and
+ * avail_sites tables are copied to shared memory when its group takes it, stepped there
+ * and copied back (launches of few, small trajectories: the plain one-trajectory
+ * drop-in); 0: always stepped in device memory.  Results do not depend on it. */
+KMC_API int kmc_pool_set_tables_on_chip(kmc_pool *pool, int32_t enable);
+/* 1 (default): a launch of at most one trajectory per SM whose model has at most 8
+ * processes (the plain one-trajectory drop-in of small models) runs each trajectory on
+ * one warp of its own with the steps on one lane, as the reference's loop runs them
+ * (proclist_generic_subroutines.mpy:1-44), the program, lattice and tables in shared
+ * memory; 0: such launches take the group-parallel step kernel.  Results do not depend
+ * on it. */
+KMC_API int kmc_pool_set_solo(kmc_pool *pool, int32_t enable);
 /* 1 (default): steps whose process has a fast stream run through the gather /
  * replay / scatter path; 0: every step runs the serial interpreter (same results). */
 KMC_API int kmc_pool_set_fast_path(kmc_pool *pool, int32_t enable);

@@ -5,9 +5,10 @@ same whatever warp runs them), so tuning runs short launches on the *real* traje
 each probe advances them by ``probe_steps`` steps, which the caller counts as warm-up or
 as part of the requested steps.  It picks the launch shape (the balanced one-block-per-SM
 shape, or 2, 4 or 8 warps per block with as many blocks as fit), the step path (gather /
-replay or serial interpreter) and the table placement (the model's hot section in shared
-memory or read from global memory) with the highest measured steps/s and sets them on
-the pool (``tune``); then, for runs of a given length, how many steps each launch takes
+replay or serial interpreter), the table placement (the model's hot section in shared
+memory or read from global memory) and the trajectories per warp (one on 32 lanes, or two
+on 16 lanes each) with the highest measured steps/s and sets them on the pool (``tune``,
+11 probes); then, for runs of a given length, how many steps each launch takes
 (``tune_steps_per_launch``).
 """
 from __future__ import annotations
@@ -44,7 +45,25 @@ def tune(pool: E.Pool, slots: Sequence[int], probe_steps: int = 500,
         best = trial
     else:
         pool.set_table_placement(True)
-    return {"warps_per_block": best["warps"], "fast_path": best["fast"], "tables": best.get("tables", "shared"),
+    # trajectories per warp: two half-warp groups per warp, with the best shape and with
+    # the balanced one (or 4 warps per block when the balanced one was the best)
+    best.setdefault("tables", "shared")
+    best["tpw"] = 1
+    for w in (best["warps"], 0 if best["warps"] else 4):
+        pool.set_trajectories_per_warp(2)
+        pool.set_launch(w, 0)
+        pool.timer_start()
+        pool.run(slots, probe_steps, sync=False)
+        ms = pool.timer_stop()
+        trial = {"fast": best["fast"], "warps": w, "tables": best["tables"], "tpw": 2, "ms": ms,
+                 "steps_per_s": len(slots) * probe_steps / ms * 1e3}
+        results.append(trial)
+        if trial["steps_per_s"] > best["steps_per_s"]:
+            best = trial
+    pool.set_trajectories_per_warp(best["tpw"])
+    pool.set_launch(best["warps"], 0)
+    return {"warps_per_block": best["warps"], "fast_path": best["fast"], "tables": best["tables"],
+            "trajectories_per_warp": best["tpw"],
             "probe_steps_per_trajectory": probe_steps * len(results), "trials": results}
 
 

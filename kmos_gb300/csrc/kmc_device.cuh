@@ -389,8 +389,9 @@ __host__ __device__ inline int fast_rec_offset(int nlat, int nchk, int nwr) {
 }
 
 // R rounds of 32 edits: the step kernel comes in R = 3 (streams of up to 96 edits, the
-// common case) and R = 4 (up to 128, large lateral-interaction groups).
-template <int R>
+// common case) and R = 4 (up to 128, large lateral-interaction groups).  G lanes run one
+// trajectory (32: a warp; 16: half a warp), each with its own write log.
+template <int R, int G = 32>
 struct FastSmem {
   int32_t latv[FAST_SLOTS];
   int32_t latsite[FAST_SLOTS];
@@ -399,8 +400,8 @@ struct FastSmem {
   int32_t esite[32 * R];   // target site
   int32_t em[32 * R];      // prefetched avail_sites(p, site, 2) of del edits
   int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS
-  uint4 lkey4[LOG_MAX / 4][32];  // lane-private write logs, four keys per 16 bytes (lane-minor)
-  int32_t lval[LOG_MAX][32];
+  uint4 lkey4[LOG_MAX / 4][G];  // lane-private write logs, four keys per 16 bytes (lane-minor)
+  int32_t lval[LOG_MAX][G];
 };
 
 // The hot section of a model program: fast streams, group records and nli tables with

@@ -2,23 +2,12 @@
 // include/kmc_gb300.h.
 //
 // Kernels
-//   kmc_run_kernel     persistent; one warp owns one trajectory at a time and runs its
-//                      kMC steps (do_kmc_steps, proclist_generic_subroutines.mpy:1-44).
-//                      Warps pull trajectories from a work counter, so thousands of
-//                      uneven trajectories share one launch.  Per step:
-//                        * three FP64 draws (gfortran xoshiro256** or Philox),
-//                        * accum_rates prefix sum in the reference's serial order
-//                          (base.mpy:603-623), recomputed only from the first process
-//                          whose nr_of_sites changed (bit-identical to a full recompute),
-//                        * kmc_time += -log(r)/accum(P) (base.mpy:1123-1161),
-//                        * integ_rates update, one process per lane (base.mpy:626-645),
-//                        * the bisection of interval_search_real (base.mpy:1234-1338)
-//                          as two warp ballots: proc = min(first i with accum(i) > v,
-//                          first i with accum(i) == accum(P)),
-//                        * site = avail_sites(proc, min(n, int(1 + r*n)), 1),
-//                        * run_proc_nr: the op program of that process.
-//                      FP64 adds and multiplies use explicit _rn intrinsics (and the file
-//                      is built with -fmad=false) so nothing is contracted into an FMA.
+//   kmc_run_kernel     persistent do_kmc_steps (proclist_generic_subroutines.mpy:1-44),
+//                      defined in kmc_run.cuh; this file builds its one-warp-per-
+//                      trajectory variants, kmc_run_g16.cu the two-per-warp ones.
+//   kmc_solo_kernel    do_kmc_steps for small launches of models with up to 8
+//                      processes: one warp per trajectory, the steps on one lane
+//                      (kmc_run.cuh).
 //   kmc_init_kernel    device-side initialize_state (proclist_generic_subroutines.mpy:
 //                      236-304): default species, then every touch-up in parallel
 //                      (fresh touch-ups only append at their own site), then a
@@ -44,607 +33,13 @@
 #include "../../include/kmc_gb300.h"
 #include "kmc_device.cuh"
 #include "kmc_host.h"
+#define KMC_DEFINE_SOLO_KERNEL
+#include "kmc_run.cuh"
 
 using namespace kmc;
 using namespace kmc_host;
 
 #define KMC_MAXK 16
-
-// Cycle accounting per step phase (builds with -DKMC_PHASE_TIMING only): lane 0 adds the
-// clock64() time since the previous mark to phase i of its warp.
-#ifdef KMC_PHASE_TIMING
-#define KMC_PHASE(sm, i)                                \
-  do {                                                  \
-    __syncwarp();                                       \
-    if ((threadIdx.x & 31) == 0) {                      \
-      const long long now_ = clock64();                 \
-      (sm).ph[i] += now_ - (sm).tprev;                  \
-      (sm).tprev = now_;                                \
-    }                                                   \
-  } while (0)
-#else
-#define KMC_PHASE(sm, i) \
-  do {                   \
-  } while (0)
-#endif
-constexpr int KMC_NPHASE = 16;
-
-template <int NP, int R>
-struct WarpSmem {
-  double rates[NP * 32];
-  double accum[NP * 32];
-  double term[NP * 32];  // nr_of_sites(i) * rates(i), refreshed when nr_of_sites(i) changes
-  int32_t ns[NP * 32];
-  uint32_t pmask[NP * 32][R];  // edits of each process this step, one bit per edit
-  int32_t ndel[NP * 32];                 // del edits of each process so far this step (0 between steps)
-  long long ph[KMC_NPHASE];  // phase cycle accounting (KMC_PHASE_TIMING builds)
-  long long tprev;
-  FastSmem<R> f;
-};
-
-// Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
-// returns a status.  Clears pmask[p] and ndel[p].  The loads it needs were issued
-// warp-parallel while the edits were evaluated: em[k] = avail_sites(p, site_k, 2) for
-// every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
-// j < min(nd, TAIL_MAX), nd = its del edits.  In a dels-first stream (every del before
-// every add, no (process, site) named by two dels or by two adds) only the moves of
-// the dels are read back, so the cleared position entries and the adds are not logged.
-template <int NP, int R>
-__device__ int replay_process(FastSmem<R> &f, int32_t *ns, uint32_t (*pmask)[R], int32_t *ndel,
-                              const View &v, int p, int rounds, bool dels_first) {
-  const size_t row = (size_t)p * v.stride;
-  int32_t *a1 = v.as1 + row;
-  int32_t *a2 = v.as2 + row;
-  const int n0 = ns[p];
-  if (!KMC_IN(n0, 0, v.stride - 1)) return ST_TABLE;
-  const int lane = threadIdx.x & 31;
-  uint32_t bits[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    bits[r] = r < rounds ? pmask[p][r] : 0u;
-    pmask[p][r] = 0u;
-  }
-  ndel[p] = 0;
-  const bool has_tail = p < TAIL_PROCS;
-  // apply the edits; reads look in the write log, then at the prefetched values.  The
-  // log is append-only (a later entry for a key shadows earlier ones) and is searched
-  // newest first, four keys per shared-memory load; once full, reads go to HBM, which
-  // every write reaches too.
-  int nlog = 0;
-  bool logok = true;
-  auto put = [&](int table, int index, int32_t val) {
-    if (table) a2[index] = val; else a1[index] = val;
-    if (!logok) return;
-    if (nlog < LOG_MAX) {
-      reinterpret_cast<uint32_t *>(&f.lkey4[nlog >> 2][lane])[nlog & 3] = ((uint32_t)table << 31) | (uint32_t)index;
-      f.lval[nlog][lane] = val;
-      nlog++;
-    } else {
-      logok = false;
-    }
-  };
-  auto logged = [&](int table, int index, int32_t &val) -> bool {
-    const uint32_t key = ((uint32_t)table << 31) | (uint32_t)index;
-    for (int g = (nlog - 1) >> 2; g >= 0; g--) {
-      const uint4 k4 = f.lkey4[g][lane];
-      const int b = 4 * g;
-      int i = -1;
-      if (b + 3 < nlog && k4.w == key) i = b + 3;
-      else if (b + 2 < nlog && k4.z == key) i = b + 2;
-      else if (b + 1 < nlog && k4.y == key) i = b + 1;
-      else if (k4.x == key) i = b;
-      if (i >= 0) { val = f.lval[i][lane]; return true; }
-    }
-    return false;
-  };
-  int n = n0;
-#pragma unroll
-  for (int r = 0; r < R; r++) {
-    uint32_t b = bits[r];
-    while (b) {
-      const int k = 32 * r + __ffs(b) - 1;
-      b &= b - 1;
-      const int kind = f.ekind[k], site = f.esite[k];
-      if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
-        if (n + 1 >= v.stride) return ST_TABLE;  // full list: tables out of step with the lattice
-        n += 1;
-        if (dels_first) {  // no del of this process follows, so nothing reads these back
-          a1[n] = site;
-          a2[site] = n;
-          continue;
-        }
-        put(0, n, site);
-        put(1, site, n);
-        continue;
-      }
-      // del_proc (base.mpy:211-265)
-      int m;
-      if (!logok) m = a2[site];
-      else if (nlog == 0 || !logged(1, site, m)) m = f.em[k];
-      if (m == 0) {
-        if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
-        continue;                            // guarded del of an absent entry
-      }
-      if (!KMC_IN(m, 1, n)) return ST_TABLE;
-      if (m < n) {
-        int last;
-        if (!logok) last = a1[n];
-        else if (nlog == 0 || !logged(0, n, last))
-          last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
-        if (!KMC_IN(last, 1, v.stride - 1)) return ST_TABLE;
-        put(0, m, last);
-        a1[n] = 0;  // vacated top entry: read again only after an add (logged) refills it
-        put(1, last, m);
-      } else {
-        a1[m] = 0;  // the same, m being the top
-      }
-      if (dels_first) a2[site] = 0;  // no later del of this process names this site
-      else put(1, site, 0);
-      n -= 1;
-    }
-  }
-  ns[p] = n;
-  return ST_OK;
-}
-
-// One kMC step's run_proc_nr through the gather / evaluate / replay path.  All lanes
-// call it and get the status.
-template <int NP, int R>
-__device__ int fast_step(WarpSmem<NP, R> &sm, const Hot &H, View &v, const int32_t *fs, int bx, int by, int bz,
-                         int lane) {
-  FastSmem<R> &f = sm.f;
-  const int nlat = fs[0], nchk = fs[1], nwr = fs[2];
-  const uint32_t w3 = (uint32_t)fs[3];
-  const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF;
-  const bool dels_first = (w3 >> 20) & 1;
-  const int32_t *coords = fs + 4;
-  const int32_t *chk = coords + nlat;
-  const int32_t *wr = chk + 2 * nchk;
-  // edit k's quads, nedit quads apart: [h, target slot, x, 0], then packed references
-  const int4 *quad = reinterpret_cast<const int4 *>(fs + fast_rec_offset(nlat, nchk, nwr));
-  const unsigned lt = (1u << lane) - 1u;
-  // 1. gather every slot (all lattice loads in flight together); check the old species
-  //    of first replaces
-  int32_t lvv[FAST_SLOTS / 32];
-  bool off_lattice = false;  // (KMC_DEBUG builds)
-#pragma unroll
-  for (int rr = 0; rr < FAST_SLOTS / 32; rr++) {
-    const int i = lane + 32 * rr;
-    lvv[rr] = 0;
-    if (i < nlat) {
-      int site = v.g.site_near(bx, by, bz, coords[i]);
-      if (!KMC_IN(site, 1, v.stride - 1)) { site = 1; off_lattice = true; }
-      f.latsite[i] = site;
-      lvv[rr] = v.lat[site - 1];
-    }
-  }
-#ifdef KMC_DEBUG
-  if (__any_sync(0xffffffffu, off_lattice)) return ST_TABLE;
-#endif
-  KMC_PHASE(sm, 11);
-#pragma unroll
-  for (int rr = 0; rr < FAST_SLOTS / 32; rr++)
-    if (lane + 32 * rr < nlat) f.latv[lane + 32 * rr] = lvv[rr];
-  __syncwarp();
-  bool bad = false;
-  for (int i = lane; i < nchk; i += 32) bad |= !in_mask(f.latv[chk[2 * i]], chk[2 * i + 1]);
-  if (__any_sync(0xffffffffu, bad)) return ST_SPECIES;
-  KMC_PHASE(sm, 4);
-  // 2. evaluate every edit in parallel; compact the ones that happen, in order.  The
-  //    loads the replay needs are issued here and land in shared memory afterwards: a
-  //    del edit's avail_sites(p, site, 2), and the list entry avail_sites(p, n0 - j, 1)
-  //    its swap-remove can move, j = its rank among the process's dels this step.
-  int ne = 0;
-  int32_t emv[R], tv[R];
-  int empos[R], tslot[R];
-#pragma unroll
-  for (int rr = 0; rr < R; rr++) {
-    emv[rr] = 0;
-    empos[rr] = -1;
-    tv[rr] = 0;
-    tslot[rr] = -1;
-    if (32 * rr >= nedit) continue;
-    const int k = 32 * rr + lane;
-    bool on = false;
-    int kind = E_GDEL, p = 0, site = 0, tgt = 0;
-    if (k < nedit) {
-      // all of the edit's quads in flight together; the table index is the base plus
-      // code(slot) * mul over every packed reference (unused ones are 0: slot 0 times 0)
-      const int4 q0 = quad[k];
-      int4 q1 = make_int4(0, 0, 0, 0), q2 = q1, q3 = q1;
-      if (nq >= 1) q1 = quad[nedit + k];
-      if (nq >= 2) q2 = quad[2 * nedit + k];
-      if (nq >= 3) q3 = quad[3 * nedit + k];
-      const uint32_t h = (uint32_t)q0.x;
-      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-      tgt = q0.y;
-      if (op >= 6) {
-        const int ns = H.nspecies;
-        auto tref = [&](int32_t w) { return species_code(f.latv[w & 0xFF], ns) * (w >> 8); };
-        int idx = q0.z + ((tref(q1.x) + tref(q1.y)) + (tref(q1.z) + tref(q1.w)));
-        if (nq >= 2) idx += (tref(q2.x) + tref(q2.y)) + (tref(q2.z) + tref(q2.w));
-        if (nq >= 3) idx += (tref(q3.x) + tref(q3.y)) + (tref(q3.z) + tref(q3.w));
-        p = H.h[idx];
-        on = p != 0;
-        kind = op == 6 ? E_DEL : E_ADD;
-      } else if (op == 2) {
-        on = true; p = arg;
-      } else if (op == 3) {
-        if (cnt <= 1) {  // the condition is in the quad: [h, target, slot, mask]
-          on = cnt == 0 || in_mask(f.latv[q0.z], q0.w);
-        } else {
-          const int32_t *e = fs + q0.z;  // [h, target, ref * cnt, mask * cnt]
-          on = true;
-          for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], f.latv), e[2 + cnt + c]);
-        }
-        p = arg; kind = E_ADD;
-      } else {
-        const int32_t *e = fs + q0.z;  // [h, target, 0, record offset, ref * cnt]
-        p = nli_refs(H, cnt, e[2], e[3], e + 4, f.latv);
-        on = p != 0;
-        kind = op == 4 ? E_DEL : E_ADD;
-      }
-    }
-    KMC_PHASE(sm, 12);
-    if (on) {
-      site = f.latsite[tgt];
-      if (kind != E_ADD) emv[rr] = v.as2[(size_t)(p - 1) * v.stride + site];
-    }
-    KMC_PHASE(sm, 13);
-    // a del's rank among its process's dels picks which list entry it loads; the ranks
-    // only have to be distinct, so a shared-memory counter gives them in any order
-    if (on && kind != E_ADD) {
-      const int q = p - 1;
-      const int rank = atomicAdd(&sm.ndel[q], 1);
-      if (rank < TAIL_MAX && q < TAIL_PROCS) {
-        const int n0 = sm.ns[q];
-        tslot[rr] = q * TAIL_MAX + rank;
-        if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)q * v.stride + n0 - rank];
-      }
-    }
-    KMC_PHASE(sm, 14);
-    const unsigned b = __ballot_sync(0xffffffffu, on);
-    if (on) {
-      const int pos = ne + __popc(b & lt);
-      f.ekind[pos] = (int8_t)kind;
-      f.ep[pos] = (int16_t)(p - 1);
-      f.esite[pos] = site;
-      atomicOr(&sm.pmask[p - 1][pos >> 5], 1u << (pos & 31));  // the process's edit mask
-      if (kind != E_ADD) empos[rr] = pos;
-    }
-    ne += __popc(b);
-    KMC_PHASE(sm, 15);
-  }
-  const int rounds = (ne + 31) >> 5;
-  KMC_PHASE(sm, 5);
-  // the loads issued during evaluation land now
-#pragma unroll
-  for (int rr = 0; rr < R; rr++) {
-    if (empos[rr] >= 0) f.em[empos[rr]] = emv[rr];
-    if (tslot[rr] >= 0) (&f.tail[0][0])[tslot[rr]] = tv[rr];
-  }
-  __syncwarp();
-  KMC_PHASE(sm, 6);
-  // 3. every process with edits replays them on its own lane (process j on lane j % 32)
-  int err = ST_OK;
-  for (int j = lane; j < v.P; j += 32) {
-    uint32_t any = 0;
-#pragma unroll
-    for (int r = 0; r < R; r++) any |= r < rounds ? sm.pmask[j][r] : 0u;
-    if (any) {
-      const int e = replay_process<NP, R>(f, sm.ns, sm.pmask, sm.ndel, v, j, rounds, dels_first);
-      if (e) err = e;
-    }
-  }
-  KMC_PHASE(sm, 7);
-  // 4. the final species of every replaced slot
-  if (!__any_sync(0xffffffffu, err != ST_OK))
-    for (int i = lane; i < nwr; i += 32) v.lat[f.latsite[wr[2 * i]] - 1] = (int8_t)wr[2 * i + 1];
-  const int e0 = __reduce_max_sync(0xffffffffu, (unsigned)err);
-  __syncwarp();
-  KMC_PHASE(sm, 8);
-  return e0;
-}
-
-// --------------------------------------------------------------------- run kernel
-struct RunArgs {
-  SlotDev *slots;
-  const ModelDev *models;
-  const int32_t *list;
-  const int64_t *steps;
-  int32_t n;
-  int32_t *counter;
-  int32_t *trace;                 // (proc, site) per step of a single-slot run, or null
-  const volatile int32_t *cancel; // host-mapped cancel flag, or null
-  int32_t fast;                   // 1: use the gather / replay path where it applies
-  int32_t model;                  // every listed slot runs this model
-  int32_t stage_words;            // hot-section words copied to shared memory (0 = read it from global)
-  unsigned long long *phase;      // KMC_NPHASE cycle sums (KMC_PHASE_TIMING builds)
-};
-
-template <int NP, int R>
-__global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const ModelDev M = a.models[a.model];
-  const int P = M.P;
-  // stage the model's hot section (fast streams, group records, nli tables)
-  int32_t *hot_s = reinterpret_cast<int32_t *>(smem_raw);
-  const int stage = a.stage_words;
-  for (int i = threadIdx.x; i < stage; i += blockDim.x) hot_s[i] = M.prog[M.off_hot + i];
-  Hot H;
-  H.h = stage ? hot_s : M.prog + M.off_hot;
-  H.grp = M.hot_grp;
-  H.tab = M.hot_tab;
-  H.nspecies = M.nspecies;
-  const size_t hot_bytes = ((size_t)stage * 4 + 15) / 16 * 16;
-  WarpSmem<NP, R> &sm = reinterpret_cast<WarpSmem<NP, R> *>(smem_raw + hot_bytes)[wib];
-  for (int i = lane; i < NP * 32 * R; i += 32) (&sm.pmask[0][0])[i] = 0u;
-  for (int i = lane; i < NP * 32; i += 32) sm.ndel[i] = 0;
-  for (int i = lane; i < KMC_NPHASE; i += 32) sm.ph[i] = 0;
-  __syncthreads();
-
-  // Work: every warp first takes item (warp in block) * gridDim.x + block -- the list
-  // is sorted by cost, so each block gets an even share of long and short trajectories
-  // -- then pulls further items from the counter.
-  const int nstatic = gridDim.x * (blockDim.x >> 5);
-  for (int round = 0;; round++) {
-    int item = wib * gridDim.x + blockIdx.x;
-    if (round > 0) {
-      if (lane == 0) item = nstatic + atomicAdd(a.counter, 1);
-      item = __shfl_sync(0xffffffffu, item, 0);
-    }
-    if (item >= a.n) break;
-    const int slot = a.list[item];
-    const int64_t nsteps = a.steps[item];
-    SlotDev &S = a.slots[slot];
-    if (S.status != ST_OK || S.model != a.model) continue;
-    const int stride = S.V + 1;
-
-    View v;
-    v.lat = S.lat;
-    v.as1 = S.as1;
-    v.as2 = S.as2;
-    v.ns = sm.ns;
-    v.prog = M.prog;
-    v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
-    FastDiv div_spuck, div_x, div_y;  // calculate_nr2lattice without hardware division
-    div_spuck.init(M.spuck);
-    div_x.init(S.X);
-    div_y.init(S.Y);
-    v.stride = stride;
-    v.backend = M.backend;
-    v.P = P;
-    v.off_groups = M.off_groups;
-    v.collect = false;
-
-    const bool fast_ok = a.fast && M.off_hot != 0 && S.V <= FAST_MAXV && P <= 256 &&
-                         (M.reach_x == 0 || S.X > 2 * M.reach_x) && (M.reach_y == 0 || S.Y > 2 * M.reach_y) &&
-                         (M.reach_z == 0 || S.Z > 2 * M.reach_z);
-    double ig[NP];
-    int64_t ps[NP];
-    int32_t n0[NP];
-#pragma unroll
-    for (int j = 0; j < NP; j++) {
-      const int i = lane + 32 * j;
-      if (i < P) {
-        const double r = S.rates[i];
-        const int n = S.nsites[i];
-        sm.rates[i] = r;
-        sm.accum[i] = S.accum[i];
-        sm.ns[i] = n;
-        sm.term[i] = __dmul_rn((double)n, r);
-        n0[j] = n;
-        ig[j] = S.integ[i];
-        ps[j] = S.procstat[i];
-      } else {
-        n0[j] = 0;
-        ig[j] = 0.0;
-        ps[j] = 0;
-      }
-    }
-    // with every rate >= +0 every term n*r is >= +0, so is every partial sum, and adding
-    // a +0 term leaves a sum >= +0 unchanged bit for bit: the chain skips those adds
-    bool neg_rate = false;
-#pragma unroll
-    for (int j = 0; j < NP; j++) {
-      const int i = lane + 32 * j;
-      neg_rate |= i < P && (__double_as_longlong(sm.rates[i]) < 0);
-    }
-    const bool skip_zero = !__any_sync(0xffffffffu, neg_rate);
-    double t = S.kmc_time, dt = S.kmc_time_step;
-    int64_t kstep = S.kmc_step;
-    // random numbers: every 32 steps, lane j draws step k + j's (ran_time, ran_proc,
-    // ran_site) and -log(ran_time); steps take them with shuffles
-    uint64_t rbase[4] = {S.rng[0], S.rng[1], S.rng[2], S.rng[3]};
-    const int rng_kind = S.rng_kind;
-    const uint32_t seed = S.seed, traj = S.traj;
-    double my_nl = 0.0, my_rp = 0.0, my_rs = 0.0;
-    int bidx = 32;
-    int from = S.accum_from;
-    int status = ST_OK;
-    int64_t k = 0;
-    __syncwarp();
-    if (lane == 0) sm.tprev = clock64();
-
-    for (; k < nsteps; k++) {
-      if (a.cancel && (k & 1023) == 0 && *a.cancel) { status = ST_CANCELLED; break; }
-      if (bidx == 32) {
-        if (k > 0) {  // advance the base state past the batch just used
-          if (rng_kind == RNG_GFORTRAN) {
-            for (int d = 0; d < 96; d++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
-          } else {
-            rbase[0] += 32;
-          }
-        }
-        uint64_t st[4] = {rbase[0], rbase[1], rbase[2], rbase[3]};
-        double rt;
-        if (rng_kind == RNG_GFORTRAN) {
-          for (int d = 0; d < 3 * lane; d++) xoshiro_next(st[0], st[1], st[2], st[3]);
-        } else {
-          st[0] += lane;
-        }
-        draw3(rng_kind, st, seed, traj, rt, my_rp, my_rs);
-        my_nl = -log(rt);
-        bidx = 0;
-      }
-      const double nl = __shfl_sync(0xffffffffu, my_nl, bidx);
-      const double ran_proc = __shfl_sync(0xffffffffu, my_rp, bidx);
-      const double ran_site = __shfl_sync(0xffffffffu, my_rs, bidx);
-      bidx++;
-      KMC_PHASE(sm, 0);
-
-      // update_accum_rate from the first stale entry: entries before it are the same
-      // sums of the same terms, so the result equals a full recompute bit for bit
-      if (lane == 0 && from < P) {
-        double acc = from > 0 ? sm.accum[from - 1] : 0.0;
-        int i = from;
-        if (i == 0) { acc = sm.term[0]; sm.accum[0] = acc; i = 1; }
-        for (; i < P; i += 8) {
-          double t8[8];  // load a chunk of terms before the dependent adds
-#pragma unroll
-          for (int j = 0; j < 8; j++) t8[j] = (i + j < P) ? sm.term[i + j] : 0.0;
-#pragma unroll
-          for (int j = 0; j < 8; j++)
-            if (i + j < P) {
-              if (!(skip_zero && __double_as_longlong(t8[j]) == 0)) acc = __dadd_rn(acc, t8[j]);
-              sm.accum[i + j] = acc;
-            }
-        }
-      }
-      from = P;
-      __syncwarp();
-      KMC_PHASE(sm, 1);
-      const double total = sm.accum[P - 1];
-      const long long tbits = __double_as_longlong(total);
-      if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
-
-      // determine_procsite: for non-negative doubles the order of the bit patterns is
-      // the order of the values
-      const long long vbits = __double_as_longlong(__dmul_rn(ran_proc, total));
-      int proc = -1;
-#pragma unroll
-      for (int j = 0; j < NP; j++) {
-        const int i = lane + 32 * j;
-        const long long ab = i < P ? __double_as_longlong(sm.accum[i]) : 0;
-        const bool pred = (i < P) && (ab > vbits || ab == tbits);
-        const unsigned b = __ballot_sync(0xffffffffu, pred);
-        if (proc < 0 && b) proc = 32 * j + __ffs(b) - 1;
-      }
-      const int n = sm.ns[proc];
-      if (n <= 0) { status = ST_DEADLOCK; break; }
-      // idx = int(1 + ran_site * n): the int -> double and the truncation by bit
-      // manipulation (exact for 1 <= n < 2^31 and 1 <= q < 2^32), the product and the sum
-      // in FP64 as the reference rounds them
-      const long long qb = __double_as_longlong(__dadd_rn(1.0, __dmul_rn(ran_site, int_to_double(n))));
-      const int qe = (int)(qb >> 52) - 1023;
-      int idx = (int)((((unsigned long long)qb & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - qe));
-      if (idx > n) idx = n;
-      if (!KMC_IN(n, 1, S.V)) { status = ST_TABLE; break; }
-
-#pragma unroll
-      for (int j = 0; j < NP; j++)
-        if (proc == lane + 32 * j) ps[j] += 1;  // increment_procstat
-
-      KMC_PHASE(sm, 2);
-      int err = ST_OK;
-      const int fs_off = fast_ok ? H.h[proc] : 0;
-      int site = 0;
-      if (lane == 0) site = v.as1[(size_t)proc * stride + idx];
-
-      // while the site load is in flight: update_clocks, kmc_time += -log(r)/accum(P)
-      // with the quotient as -log(r) times the reciprocal of accum(P) (within 2 ulp),
-      // and update_integ_rate, integ(i) = integ(i) + n(i)*r(i)*dt
-      dt = __dmul_rn(nl, __drcp_rn(total));
-      t = __dadd_rn(t, dt);
-      kstep += 1;
-#pragma unroll
-      for (int j = 0; j < NP; j++) {
-        const int i = lane + 32 * j;
-        if (i < P) ig[j] = __dadd_rn(ig[j], __dmul_rn(sm.term[i], dt));
-      }
-
-      if (lane == 0 && a.trace) { a.trace[2 * k] = proc + 1; a.trace[2 * k + 1] = site; }
-      site = __shfl_sync(0xffffffffu, site, 0);
-      if (site < 1 || site > S.V) { status = ST_TABLE; break; }  // list entry outside the lattice
-      int bx, by, bz, bn;
-      {  // calculate_nr2lattice (lattice.mpy:177-210)
-        const unsigned c = div_spuck.div((unsigned)(site - 1));
-        bn = site - M.spuck * (int)c;
-        const unsigned r = div_x.div(c);
-        bx = (int)(c - (unsigned)S.X * r);
-        const unsigned zq = div_y.div(r);
-        by = (int)(r - (unsigned)S.Y * zq);
-        bz = (int)zq;
-      }
-      KMC_PHASE(sm, 3);
-      if (fs_off) {
-        err = fast_step<NP, R>(sm, H, v, H.h + fs_off, bx, by, bz, lane);
-      } else {
-        if (lane == 0) {
-          v.minp = P;
-          v.err = ST_OK;
-          run_stream(v, M.prog[M.off_proc + proc], bx, by, bz);
-          err = v.err;
-        }
-        err = __shfl_sync(0xffffffffu, err, 0);
-        __syncwarp();
-        KMC_PHASE(sm, 9);
-      }
-      if (err) { status = err; break; }
-      // refresh the terms of processes whose nr_of_sites changed; accum restarts at
-      // the first of them
-      int first = P;
-#pragma unroll
-      for (int j = 0; j < NP; j++) {
-        const int i = lane + 32 * j;
-        const int nn = i < P ? sm.ns[i] : 0;
-        const bool ch = i < P && nn != n0[j];
-        if (ch) { sm.term[i] = __dmul_rn(int_to_double(nn), sm.rates[i]); n0[j] = nn; }
-        const unsigned b = __ballot_sync(0xffffffffu, ch);
-        if (first == P && b) first = 32 * j + __ffs(b) - 1;
-      }
-      from = first;
-      __syncwarp();
-      KMC_PHASE(sm, 10);
-    }
-    // random state after the draws actually used: bidx draws of the current batch
-    // (a step that found no process has drawn its numbers, as in the reference)
-    if (bidx < 32 || k > 0) {
-      const int used = bidx;
-      if (rng_kind == RNG_GFORTRAN) {
-        for (int d = 0; d < 3 * used; d++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
-      } else {
-        rbase[0] += used;
-      }
-    }
-
-#pragma unroll
-    for (int j = 0; j < NP; j++) {
-      const int i = lane + 32 * j;
-      if (i < P) {
-        S.integ[i] = ig[j];
-        S.procstat[i] = ps[j];
-        S.nsites[i] = sm.ns[i];
-        S.accum[i] = sm.accum[i];
-      }
-    }
-    if (lane == 0) {
-      S.kmc_time = t;
-      S.kmc_time_step = dt;
-      S.kmc_step = kstep;
-      S.rng[0] = rbase[0]; S.rng[1] = rbase[1]; S.rng[2] = rbase[2]; S.rng[3] = rbase[3];
-      S.accum_from = from;
-      S.status = status;
-    }
-    __syncwarp();
-  }
-#ifdef KMC_PHASE_TIMING
-  if (lane == 0 && a.phase)
-    for (int i = 0; i < KMC_NPHASE; i++) atomicAdd(&a.phase[i], (unsigned long long)sm.ph[i]);
-#endif
-}
 
 // -------------------------------------------------------------------- init kernel
 struct InitArgs {
@@ -1157,58 +552,163 @@ constexpr int STAGE_MAX_WORDS = 16384;  // hot sections up to 64 KB go to shared
 
 // One launch of the run kernel: every listed slot runs `model`.
 struct LaunchPlan {
-  int model, first, count, blocks, threads, np, rounds;
+  int model, first, count, blocks, threads, np, rounds, g;
+  const void *fn;  // host stub of the kernel variant
   size_t smem;
   RunArgs a;
 };
 
-template <int NP, int R>
-int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes) {
-  L.np = NP;
-  L.rounds = R;
+// Shared memory of one trajectory group of the (np, r, g) variant.
+template <int NP, int R, int G>
+constexpr size_t wsz() { return sizeof(WarpSmem<NP, R, G>); }
+size_t warp_smem_bytes(int np, int r, int g) {
+  switch (g * 1000 + np * 10 + r) {
+    case 32013: return wsz<1, 3, 32>();
+    case 32014: return wsz<1, 4, 32>();
+    case 32023: return wsz<2, 3, 32>();
+    case 32024: return wsz<2, 4, 32>();
+    case 32043: return wsz<4, 3, 32>();
+    case 32083: return wsz<8, 3, 32>();
+    case 16013: return wsz<1, 3, 16>();
+    case 16014: return wsz<1, 4, 16>();
+    case 16023: return wsz<2, 3, 16>();
+    case 16024: return wsz<2, 4, 16>();
+    case 16043: return wsz<4, 3, 16>();
+    case 16044: return wsz<4, 4, 16>();
+    default: return 0;
+  }
+}
+
+const void *run_kernel_g32(int np, int r) {
+  switch (np * 10 + r) {
+    case 13: return (const void *)kmc_run_kernel<1, 3, 32>;
+    case 14: return (const void *)kmc_run_kernel<1, 4, 32>;
+    case 23: return (const void *)kmc_run_kernel<2, 3, 32>;
+    case 24: return (const void *)kmc_run_kernel<2, 4, 32>;
+    case 43: return (const void *)kmc_run_kernel<4, 3, 32>;
+    case 83: return (const void *)kmc_run_kernel<8, 3, 32>;
+    default: return nullptr;
+  }
+}
+
+// Launch shape of one model's launch with kernel variant (np, r, g).  ts_max: the
+// largest ts_need of its trajectories; their lattice and tables go to shared memory when
+// the pool allows it and every trajectory of the launch then still runs in one round.
+int plan_kernel(kmc_pool *p, LaunchPlan &L, size_t hot_bytes, int np, int r, int g, size_t ts_max) {
+  L.np = np;
+  L.rounds = r;
+  L.g = g;
+  L.fn = g == 16 ? run_kernel_g16(np, r) : run_kernel_g32(np, r);
+  const size_t wsm = warp_smem_bytes(np, r, g);
+  if (!L.fn || !wsm) return fail(KMC_ERR_ARG, "no step kernel for this model and launch mode");
   // The attribute is a per-function cap shared by every plan (and pool) on the device:
   // raise it to the device's limit once rather than to this plan's size, which would
   // lower it under a plan made before this one.
   cudaFuncAttributes fa;
-  CK(cudaFuncGetAttributes(&fa, kmc_run_kernel<NP, R>));
+  CK(cudaFuncGetAttributes(&fa, L.fn));
   int optin = 0;
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
-  const int cap = optin - (int)fa.sharedSizeBytes;
+  const int64_t cap = optin - (int64_t)fa.sharedSizeBytes;
   if (fa.maxDynamicSharedSizeBytes < cap)
-    CK(cudaFuncSetAttribute(kmc_run_kernel<NP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    CK(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+  const int gpw = 32 / g;  // trajectory groups per warp
+  const size_t ts = p->tables_on_chip ? align_up(ts_max, 16) : 0;
+  auto smem_for = [&](int warps, bool on_chip) {
+    return hot_bytes + (wsm + (on_chip ? ts : 0)) * (size_t)warps * gpw;
+  };
+  auto occupancy = [&](int warps, bool on_chip, int *nb) -> int {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(nb, L.fn, 32 * warps, smem_for(warps, on_chip)));
+    return KMC_OK;
+  };
   if (p->warps_per_block > 0) {
     const int wpb = p->warps_per_block;
+    const int gpb = wpb * gpw;
     L.threads = 32 * wpb;
-    L.smem = hot_bytes + sizeof(WarpSmem<NP, R>) * wpb;
-    if ((int64_t)L.smem > cap) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
-    int bps = p->blocks_per_sm;
-    if (bps <= 0) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kmc_run_kernel<NP, R>, L.threads, L.smem));
+    bool on_chip = false;
+    int bps = 0;
+    if (ts > 0 && (int64_t)smem_for(wpb, true) <= cap) {
+      if (int rc_ = occupancy(wpb, true, &bps)) return rc_;
+      if (p->blocks_per_sm > 0) bps = std::min(bps, p->blocks_per_sm);
+      on_chip = bps >= 1 && (int64_t)L.count <= (int64_t)p->num_sms * bps * gpb;
+    }
+    if (!on_chip) {
+      if ((int64_t)smem_for(wpb, false) > cap)
+        return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
+      bps = p->blocks_per_sm;
+      if (bps <= 0) { if (int rc_ = occupancy(wpb, false, &bps)) return rc_; }
+    }
     if (bps <= 0) return fail(KMC_ERR_CUDA, "run kernel does not fit on an SM with this launch shape");
-    L.blocks = std::max(1, std::min((L.count + wpb - 1) / wpb, p->num_sms * bps));
+    L.smem = smem_for(wpb, on_chip);
+    L.a.groups = gpb;
+    L.a.ts_bytes = on_chip ? (int32_t)ts : 0;
+    L.blocks = std::max(1, std::min((L.count + gpb - 1) / gpb, p->num_sms * bps));
     return KMC_OK;
   }
   // balanced: one block per SM, as many warps per block as fit (registers: 16 at 128
-  // per thread; shared memory), and the fewest rounds of items per warp with the warps
-  // split evenly over the SMs
+  // per thread; shared memory), and the fewest rounds of items per group with the
+  // groups split evenly over the SMs
   const int regs = std::max(1, fa.numRegs);
-  int maxw = std::min(16, 65536 / (regs * 32));
-  maxw = std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / (int64_t)sizeof(WarpSmem<NP, R>));
-  // the occupancy calculator has the last word (register allocation granularity)
-  while (maxw >= 1) {
-    int nb = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kmc_run_kernel<NP, R>, 32 * maxw,
-                                                     hot_bytes + sizeof(WarpSmem<NP, R>) * maxw));
-    if (nb >= 1) break;
-    maxw--;
+  auto fit_warps = [&](bool on_chip, int *out) -> int {
+    int maxw = std::min(16, 65536 / (regs * 32));
+    const int64_t per_warp = (int64_t)(wsm + (on_chip ? ts : 0)) * gpw;
+    maxw = (int)std::min<int64_t>(maxw, (cap - (int64_t)hot_bytes) / per_warp);
+    // the occupancy calculator has the last word (register allocation granularity)
+    while (maxw >= 1) {
+      int nb = 0;
+      if (int rc_ = occupancy(maxw, on_chip, &nb)) return rc_;
+      if (nb >= 1) break;
+      maxw--;
+    }
+    *out = maxw;
+    return KMC_OK;
+  };
+  const int blocks = std::max(1, std::min(p->num_sms, (L.count + gpw - 1) / gpw));
+  int maxw = 0;
+  bool on_chip = false;
+  if (ts > 0) {
+    if (int rc_ = fit_warps(true, &maxw)) return rc_;
+    on_chip = maxw >= 1 && (int64_t)L.count <= (int64_t)blocks * maxw * gpw;
   }
+  if (!on_chip) { if (int rc_ = fit_warps(false, &maxw)) return rc_; }
   if (maxw < 1) return fail(KMC_ERR_ARG, "model's shared-memory section too large for one block");
-  const int blocks = std::max(1, std::min(p->num_sms, L.count));
-  const int rounds = (L.count + blocks * maxw - 1) / (blocks * maxw);
-  const int warps = (L.count + rounds - 1) / rounds;
+  const int rounds = (L.count + blocks * maxw * gpw - 1) / (blocks * maxw * gpw);
+  const int groups = (L.count + rounds - 1) / rounds;
+  const int warps = (groups + gpw - 1) / gpw;
   const int wpb = std::min(maxw, (warps + blocks - 1) / blocks);
   L.threads = 32 * wpb;
-  L.smem = hot_bytes + sizeof(WarpSmem<NP, R>) * wpb;
+  L.smem = smem_for(wpb, on_chip);
   L.blocks = blocks;
+  L.a.groups = wpb * gpw;
+  L.a.ts_bytes = on_chip ? (int32_t)ts : 0;
+  return KMC_OK;
+}
+
+// The solo kernel: one block of one warp per trajectory, the program and (when they fit)
+// the lattice and tables in shared memory.
+int plan_solo(kmc_pool *p, LaunchPlan &L, size_t ts_max) {
+  L.np = 1;
+  L.rounds = 0;
+  L.g = 32;
+  L.fn = (const void *)kmc_solo_kernel;
+  cudaFuncAttributes fa;
+  CK(cudaFuncGetAttributes(&fa, L.fn));
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
+  const int64_t cap = optin - (int64_t)fa.sharedSizeBytes;
+  if (fa.maxDynamicSharedSizeBytes < cap)
+    CK(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+  const ModelHost &mh = p->models[L.model];
+  const size_t prog_b = align_up((size_t)mh.dev.len * 4, 16);
+  const size_t ts = p->tables_on_chip ? align_up(ts_max, 16) : 0;
+  size_t smem = sizeof(SoloSmem);
+  L.a.prog_words = 0;
+  L.a.ts_bytes = 0;
+  if ((int64_t)(smem + prog_b) <= cap) { smem += prog_b; L.a.prog_words = mh.dev.len; }
+  if (ts > 0 && (int64_t)(smem + ts) <= cap) { smem += ts; L.a.ts_bytes = (int32_t)ts; }
+  L.a.groups = 1;
+  L.threads = 32;
+  L.blocks = L.count;
+  L.smem = smem;
   return KMC_OK;
 }
 
@@ -1250,17 +750,25 @@ int plan_run(kmc_pool *p, const int32_t *slots, const int64_t *steps, int n, std
     a.fast = p->fast_path;
     a.model = model;
     a.stage_words = (p->stage_hot && md.off_hot && md.hot_len <= STAGE_MAX_WORDS) ? md.hot_len : 0;
+    a.prog_words = 0;
     a.phase = p->d_phase;
     const size_t hot_bytes = ((size_t)a.stage_words * 4 + 15) / 16 * 16;
     // fast streams of more than 96 edits run in the 4-round kernel (built for up to 64
     // processes); a larger model with such streams takes the serial interpreter
     const bool big = md.max_nedit > 96;
     if (big && md.P > 64) a.fast = 0;
-    int rc;
-    if (md.P <= 32) rc = big ? plan_kernel<1, 4>(p, L, hot_bytes) : plan_kernel<1, 3>(p, L, hot_bytes);
-    else if (md.P <= 64) rc = big ? plan_kernel<2, 4>(p, L, hot_bytes) : plan_kernel<2, 3>(p, L, hot_bytes);
-    else if (md.P <= 128) rc = plan_kernel<4, 3>(p, L, hot_bytes);
-    else rc = plan_kernel<8, 3>(p, L, hot_bytes);
+    // two trajectories per warp (16 lanes each) for models of up to 64 processes
+    const int g = (p->traj_per_warp == 2 && md.P <= 64) ? 16 : 32;
+    int np = 1;
+    while (np * g < md.P) np *= 2;
+    const int r = (big && md.P <= 64) ? 4 : 3;
+    size_t ts_max = 0;
+    for (int k = i; k < j; k++) {
+      const SlotDev &d = p->slots[ls[k]].dev;
+      ts_max = std::max(ts_max, ts_need(md.P, d.V));
+    }
+    int rc = (p->solo && md.P <= SOLO_PMAX && L.count <= p->num_sms) ? plan_solo(p, L, ts_max)
+                                                                       : plan_kernel(p, L, hot_bytes, np, r, g, ts_max);
     if (rc) return rc;
     plans.push_back(L);
     i = j;
@@ -1299,14 +807,8 @@ int issue_run(kmc_pool *p, std::vector<LaunchPlan> &plans, const int32_t *d_list
       st = p->aux[i];
       CK(cudaStreamWaitEvent(st, p->fork_ev, 0));
     }
-    switch (L.np * 10 + L.rounds) {
-      case 13: kmc_run_kernel<1, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 14: kmc_run_kernel<1, 4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 23: kmc_run_kernel<2, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 24: kmc_run_kernel<2, 4><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      case 43: kmc_run_kernel<4, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-      default: kmc_run_kernel<8, 3><<<L.blocks, L.threads, L.smem, st>>>(L.a); break;
-    }
+    void *args[] = {&L.a};
+    CK(cudaLaunchKernel(L.fn, dim3(L.blocks), dim3(L.threads), args, L.smem, st));
     CK(cudaGetLastError());
     p->launches++;
     if (fork) CK(cudaEventRecord(p->aux_ev[i], st));
@@ -1745,6 +1247,27 @@ int kmc_pool_set_launch(kmc_pool *p, int32_t warps_per_block, int32_t blocks_per
   if (!p || warps_per_block < 0 || warps_per_block > 16 || blocks_per_sm < 0) return fail(KMC_ERR_ARG, "bad launch shape");
   p->warps_per_block = warps_per_block;
   p->blocks_per_sm = blocks_per_sm;
+  clear_graphs(p);
+  return KMC_OK;
+}
+
+int kmc_pool_set_trajectories_per_warp(kmc_pool *p, int32_t n) {
+  if (!p || (n != 1 && n != 2)) return fail(KMC_ERR_ARG, "trajectories per warp must be 1 or 2");
+  p->traj_per_warp = n;
+  clear_graphs(p);
+  return KMC_OK;
+}
+
+int kmc_pool_set_solo(kmc_pool *p, int32_t enable) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  p->solo = enable ? 1 : 0;
+  clear_graphs(p);
+  return KMC_OK;
+}
+
+int kmc_pool_set_tables_on_chip(kmc_pool *p, int32_t enable) {
+  if (!p) return fail(KMC_ERR_ARG, "bad pool");
+  p->tables_on_chip = enable ? 1 : 0;
   clear_graphs(p);
   return KMC_OK;
 }

@@ -132,6 +132,10 @@ struct kmc_pool {
   int fast_path = 1;
   int stage_hot = 1;  // 1: a model's hot section goes to shared memory when it fits
   int blocks_per_sm = 0;  // 0 = occupancy maximum
+  int traj_per_warp = 1;  // 2: two trajectories per warp, 16 lanes each (models of up to 64 processes)
+  int tables_on_chip = 1; // 1: a launch's lattices and tables go to shared memory when they all fit
+  int solo = 1;           // 1: launches of at most one trajectory per SM of models with up to 8
+                          //    processes run the solo kernel (steps on one lane)
   std::unordered_map<kmc_host::GraphKey, kmc_host::GraphEntry, kmc_host::GraphKeyHash> graphs;
   std::mutex mu;
   unsigned long long *d_phase = nullptr;  // KMC_NPHASE cycle sums

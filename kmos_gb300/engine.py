@@ -89,6 +89,9 @@ SIGNATURES = {
     "kmc_pool_set_rates": (_i32, [_vp, _i32, _pd]),
     "kmc_pool_occupation_counts": (_i32, [_vp, _p32, _i32, _i32, _p64]),
     "kmc_pool_occupation_counts_static": (_i32, [_vp, _p32, _i32, _i32, _p64]),
+    "kmc_pool_set_trajectories_per_warp": (_i32, [_vp, _i32]),
+    "kmc_pool_set_tables_on_chip": (_i32, [_vp, _i32]),
+    "kmc_pool_set_solo": (_i32, [_vp, _i32]),
     "kmc_pool_get_results": (_i32, [_vp, _p32, _i32, _i32, _p64, _pd, _pd, _p64, _p32]),
     "kmc_pool_set_launch": (_i32, [_vp, _i32, _i32]),
     "kmc_pool_set_fast_path": (_i32, [_vp, _i32]),
@@ -477,6 +480,18 @@ class Pool:
 
     def set_fast_path(self, enable: bool):
         _check(load().kmc_pool_set_fast_path(self.h, 1 if enable else 0))
+
+    def set_trajectories_per_warp(self, n: int):
+        """1: 32 lanes per trajectory; 2: two trajectories per warp, 16 lanes each."""
+        _check(load().kmc_pool_set_trajectories_per_warp(self.h, int(n)))
+
+    def set_solo(self, enable: bool):
+        """Small launches of models with up to 8 processes: steps on one lane per trajectory."""
+        _check(load().kmc_pool_set_solo(self.h, 1 if enable else 0))
+
+    def set_tables_on_chip(self, enable: bool):
+        """Lattice and avail_sites tables in shared memory for launches where they fit."""
+        _check(load().kmc_pool_set_tables_on_chip(self.h, 1 if enable else 0))
 
     def set_table_placement(self, shared: bool):
         """Hot section (fast streams, nli tables) in shared memory (True) or read from
