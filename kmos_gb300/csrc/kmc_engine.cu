@@ -689,7 +689,17 @@ int plan_solo(kmc_pool *p, LaunchPlan &L, size_t ts_max) {
   L.np = 1;
   L.rounds = 0;
   L.g = 32;
-  L.fn = (const void *)kmc_solo_kernel;
+  switch (p->models[L.model].dev.P) {
+    case 1: L.fn = (const void *)kmc_solo_kernel<1>; break;
+    case 2: L.fn = (const void *)kmc_solo_kernel<2>; break;
+    case 3: L.fn = (const void *)kmc_solo_kernel<3>; break;
+    case 4: L.fn = (const void *)kmc_solo_kernel<4>; break;
+    case 5: L.fn = (const void *)kmc_solo_kernel<5>; break;
+    case 6: L.fn = (const void *)kmc_solo_kernel<6>; break;
+    case 7: L.fn = (const void *)kmc_solo_kernel<7>; break;
+    case 8: L.fn = (const void *)kmc_solo_kernel<8>; break;
+    default: return fail(KMC_ERR_ARG, "solo kernel: more processes than it is built for");
+  }
   cudaFuncAttributes fa;
   CK(cudaFuncGetAttributes(&fa, L.fn));
   int optin = 0;

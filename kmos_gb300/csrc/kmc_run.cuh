@@ -716,38 +716,136 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
 
 // --------------------------------------------------------------- solo kernel
 // One trajectory per block of one warp, for models of at most SOLO_PMAX processes (the
-// plain one-trajectory drop-in and other small launches).  The steps themselves run on
-// lane 0 alone, as the reference's loop runs them: no warp collective per step.  The
-// other lanes draw the random numbers of the next 32 steps at once (the same streams as
-// kmc_run_kernel: lane j takes step k + j) and copy the state on and off chip.  The op
+// plain one-trajectory drop-in and other small launches).  The steps run on lane 0
+// alone, as the reference's loop runs them: no warp collective per step, the process
+// vectors (rates, accum, terms, integ, procstat) in lane 0's registers.  The other lanes
+// draw the random numbers of the next 32 steps at once (the same streams as
+// kmc_run_kernel: lane j takes step k + j) and copy the state on and off chip.  The
 // program, the lattice and the avail_sites tables sit in shared memory when they fit
-// (RunArgs::prog_words, RunArgs::ts_bytes); run_proc_nr is the serial interpreter
-// (run_stream).  Arithmetic and order are kmc_run_kernel's, so results are the same bit
-// for bit.
+// (RunArgs::prog_words, RunArgs::ts_bytes).  run_proc_nr evaluates the process's resolved
+// fast stream serially (every condition on the values before the step, then the table
+// edits in program order, then the lattice writes: the serial interpreter's result) and
+// falls back to the interpreter where the fast form does not apply.  Arithmetic and
+// order are kmc_run_kernel's, so results are the same bit for bit.
 constexpr int SOLO_PMAX = 8;
 
 struct SoloSmem {
   double nl[32], rp[32], rs[32];  // -log(ran_time), ran_proc, ran_site of the batch's steps
-  double rates[SOLO_PMAX], accum[SOLO_PMAX], term[SOLO_PMAX], integ[SOLO_PMAX];
-  long long procstat[SOLO_PMAX];
-  int32_t ns[SOLO_PMAX], n0[SOLO_PMAX];
+  int32_t latv[FAST_SLOTS];       // slot species before the step
+  int32_t latsite[FAST_SLOTS];    // slot sites
+  int32_t ns[SOLO_PMAX];          // nr_of_sites
   int32_t status, used, from, pad;
 };
 
+// run_proc_nr of one step through the process's resolved fast stream, serially: the
+// slots' species, the old-species checks, every edit's condition on the values before the
+// step and its table operation in program order (add_proc / del_proc / guarded del_proc,
+// base.mpy:211-302, written out here so that the view stays in registers), then the
+// replaced slots' final species.
+__device__ __forceinline__ int solo_fast_stream(View &v, const Hot &H, const int32_t *fs, int bx, int by, int bz,
+                                                int32_t *latv, int32_t *latsite) {
+  const int nlat = fs[0], nchk = fs[1], nwr = fs[2];
+  const uint32_t w3 = (uint32_t)fs[3];
+  const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF;
+  const int32_t *coords = fs + 4;
+  const int32_t *chk = coords + nlat;
+  const int32_t *wr = chk + 2 * nchk;
+  const int4 *quad = reinterpret_cast<const int4 *>(fs + fast_rec_offset(nlat, nchk, nwr));
+  for (int i = 0; i < nlat; i++) {
+    const int site = v.g.site_near(bx, by, bz, coords[i]);
+    if (!KMC_IN(site, 1, v.stride - 1)) return ST_TABLE;
+    latsite[i] = site;
+    latv[i] = v.lat[site - 1];
+  }
+  for (int i = 0; i < nchk; i++)
+    if (!in_mask(latv[chk[2 * i]], chk[2 * i + 1])) return ST_SPECIES;
+  for (int k = 0; k < nedit; k++) {
+    const int4 q0 = quad[k];
+    const uint32_t h = (uint32_t)q0.x;
+    const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
+    int p, kind;
+    if (op >= 6) {
+      const int ns = H.nspecies;
+      auto tref = [&](int32_t w) { return species_code(latv[w & 0xFF], ns) * (w >> 8); };
+      int idx = q0.z;
+      if (nq >= 1) { const int4 q = quad[nedit + k]; idx += (tref(q.x) + tref(q.y)) + (tref(q.z) + tref(q.w)); }
+      if (nq >= 2) { const int4 q = quad[2 * nedit + k]; idx += (tref(q.x) + tref(q.y)) + (tref(q.z) + tref(q.w)); }
+      if (nq >= 3) { const int4 q = quad[3 * nedit + k]; idx += (tref(q.x) + tref(q.y)) + (tref(q.z) + tref(q.w)); }
+      p = H.h[idx];
+      kind = op == 6 ? E_DEL : E_ADD;
+    } else if (op == 2) {
+      p = arg;
+      kind = E_GDEL;
+    } else if (op == 3) {
+      bool on;
+      if (cnt <= 1) {
+        on = cnt == 0 || in_mask(latv[q0.z], q0.w);
+      } else {
+        const int32_t *e = fs + q0.z;
+        on = true;
+        for (int c = 0; c < cnt && on; c++) on = in_mask(ref_value(e[2 + c], latv), e[2 + cnt + c]);
+      }
+      p = on ? arg : 0;
+      kind = E_ADD;
+    } else {
+      const int32_t *e = fs + q0.z;
+      p = nli_refs(H, cnt, e[2], e[3], e + 4, latv);
+      kind = op == 4 ? E_DEL : E_ADD;
+    }
+    if (p == 0) continue;
+    const int site = latsite[q0.y];
+    int32_t *a1 = v.as1 + (size_t)(p - 1) * v.stride;
+    int32_t *a2 = v.as2 + (size_t)(p - 1) * v.stride;
+    if (kind == E_ADD) {  // add_proc (base.mpy:268-302)
+      const int n = v.ns[p - 1] + 1;
+      if (n >= v.stride) return ST_TABLE;  // a full list: tables out of step with the lattice
+      v.ns[p - 1] = n;
+      a1[n] = site;
+      a2[site] = n;
+    } else {  // del_proc (base.mpy:211-265), guarded or not
+      const int m = a2[site];
+      if (m == 0) {
+        if (kind == E_DEL) return ST_TABLE;  // nli names a process that is not there
+        continue;
+      }
+      const int n = v.ns[p - 1];
+      if (!KMC_IN(m, 1, n)) return ST_TABLE;
+      if (m < n) {
+        const int last = a1[n];
+        if (!KMC_IN(last, 1, v.stride - 1)) return ST_TABLE;
+        a1[m] = last;
+        a1[n] = 0;
+        a2[last] = m;
+      } else {
+        a1[m] = 0;
+      }
+      a2[site] = 0;
+      v.ns[p - 1] = n - 1;
+    }
+    if (p - 1 < v.minp) v.minp = p - 1;
+  }
+  for (int i = 0; i < nwr; i++) v.lat[latsite[wr[2 * i]] - 1] = (int8_t)wr[2 * i + 1];
+  return ST_OK;
+}
+
 // Defined in the one translation unit that defines KMC_DEFINE_SOLO_KERNEL (kmc_engine.cu).
+// PP = the model's process count exactly, so every loop over processes unrolls to its
+// true length and the vectors stay in registers; __maxnreg__ gives the one warp of the
+// block the registers that takes without spills.
 #ifdef KMC_DEFINE_SOLO_KERNEL
-__global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
+template <int PP>
+__global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Group<32> grp;
   const int lane = grp.gl;
   const int item = blockIdx.x;
   if (item >= a.n) return;
   const ModelDev M = a.models[a.model];
-  const int P = M.P;
+  constexpr int P = PP;
   const int slot = a.list[item];
   const int64_t nsteps = a.steps[item];
   SlotDev &S = a.slots[slot];
-  if (S.status != ST_OK || S.model != a.model || P > SOLO_PMAX) return;
+  if (S.status != ST_OK || S.model != a.model || M.P != PP) return;
   SoloSmem &sm = *reinterpret_cast<SoloSmem *>(smem_raw);
   const size_t prog_b = ((size_t)a.prog_words * 4 + 15) / 16 * 16;
   int32_t *prog_s = reinterpret_cast<int32_t *>(smem_raw + sizeof(SoloSmem));
@@ -768,27 +866,44 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
     group_copy(v.as1, S.as1, tab_b, grp);
     group_copy(v.as2, S.as2, tab_b, grp);
   }
+  const int32_t *prog = a.prog_words ? prog_s : M.prog;
   v.ns = sm.ns;
-  v.prog = a.prog_words ? prog_s : M.prog;
+  v.prog = prog;
   v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
   v.stride = stride;
   v.backend = M.backend;
   v.P = P;
   v.off_groups = M.off_groups;
   v.collect = false;
-  if (lane < P) {
-    const double r = S.rates[lane];
-    const int n = S.nsites[lane];
-    sm.rates[lane] = r;
-    sm.accum[lane] = S.accum[lane];
-    sm.ns[lane] = n;
-    sm.n0[lane] = n;
-    sm.term[lane] = __dmul_rn((double)n, r);
-    sm.integ[lane] = S.integ[lane];
-    sm.procstat[lane] = S.procstat[lane];
+  v.minp = P;
+  v.err = ST_OK;
+  Hot H;
+  H.h = prog + M.off_hot;
+  H.grp = M.hot_grp;
+  H.tab = M.hot_tab;
+  H.nspecies = M.nspecies;
+  const bool fast_ok = a.fast && M.off_hot != 0 && S.V <= FAST_MAXV &&
+                       (M.reach_x == 0 || S.X > 2 * M.reach_x) && (M.reach_y == 0 || S.Y > 2 * M.reach_y) &&
+                       (M.reach_z == 0 || S.Z > 2 * M.reach_z);
+  // the process vectors in registers (every index a compile-time constant)
+  double rates_r[PP], accum_r[PP], term_r[PP], integ_r[PP];
+  long long ps_r[PP];
+  int32_t n0_r[PP];
+  bool neg_rate = false;
+#pragma unroll
+  for (int i = 0; i < PP; i++) {
+    rates_r[i] = S.rates[i];
+    accum_r[i] = S.accum[i];
+    n0_r[i] = S.nsites[i];
+    term_r[i] = __dmul_rn((double)n0_r[i], rates_r[i]);
+    integ_r[i] = S.integ[i];
+    ps_r[i] = S.procstat[i];
+    neg_rate |= __double_as_longlong(rates_r[i]) < 0;
   }
-  bool neg_rate = lane < P && (__double_as_longlong(S.rates[lane]) < 0);
-  const bool skip_zero = !grp.any(neg_rate);
+  // with every rate >= +0 every term n*r is >= +0, so is every partial sum, and adding
+  // a +0 term leaves a sum >= +0 unchanged bit for bit: the chain skips those adds
+  const bool skip_zero = !neg_rate;
+  if (lane < P) sm.ns[lane] = S.nsites[lane];
   if (lane == 0) {
     sm.status = ST_OK;
     sm.used = 0;
@@ -807,6 +922,23 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
   int64_t k = 0;
   int status = ST_OK;
   int used = 0;  // draws of the current batch taken
+#ifdef KMC_PHASE_TIMING
+  // lane 0's cycles per phase of the step (builds with KMC_PHASE_TIMING only): 0 draws,
+  // 1 accum, 2 bisection and site, 3 clock and integ, 4 site coordinates, 5 run_proc_nr,
+  // 6 term refresh
+  long long ph[7] = {0, 0, 0, 0, 0, 0, 0};
+  long long tp = clock64();
+#define SOLO_PHASE(i)                 \
+  do {                                \
+    const long long now_ = clock64(); \
+    ph[i] += now_ - tp;               \
+    tp = now_;                        \
+  } while (0)
+#else
+#define SOLO_PHASE(i) \
+  do {                \
+  } while (0)
+#endif
   while (k < nsteps && status == ST_OK) {
     if (a.cancel && grp.any(*a.cancel != 0)) { status = ST_CANCELLED; break; }  // one decision for the warp
     // every lane draws one step of the next batch
@@ -834,32 +966,40 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
     const int nb = (int)min((int64_t)32, nsteps - k);
     if (lane == 0) {
       int from = sm.from, b = 0;
+      SOLO_PHASE(0);
       for (; b < nb; b++) {
         const double nl = sm.nl[b], ran_proc = sm.rp[b], ran_site = sm.rs[b];
         used = b + 1;
         // update_accum_rate from the first stale entry (base.mpy:603-623)
         if (from < P) {
-          double acc = from > 0 ? sm.accum[from - 1] : 0.0;
-          int i = from;
-          if (i == 0) { acc = sm.term[0]; sm.accum[0] = acc; i = 1; }
-          for (; i < P; i++) {
-            const double tm = sm.term[i];
-            if (!(skip_zero && __double_as_longlong(tm) == 0)) acc = __dadd_rn(acc, tm);
-            sm.accum[i] = acc;
+          double acc = 0.0;
+#pragma unroll
+          for (int i = 0; i < PP; i++) {
+            if (i >= from) {
+              if (i == 0) {
+                acc = term_r[0];
+              } else {
+                if (i == from) acc = accum_r[i - 1];
+                if (!(skip_zero && __double_as_longlong(term_r[i]) == 0)) acc = __dadd_rn(acc, term_r[i]);
+              }
+              accum_r[i] = acc;
+            }
           }
         }
         from = P;
-        const double total = sm.accum[P - 1];
+        const double total = accum_r[PP - 1];
         const long long tbits = __double_as_longlong(total);
         if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
+        const double rcp = __drcp_rn(total);  // issued early: used by the clock below
+        SOLO_PHASE(1);
         // determine_procsite (base.mpy:1075-1120, 1234-1338): the first process whose
         // accumulated rate exceeds ran_proc * total, or reaches total
         const long long vbits = __double_as_longlong(__dmul_rn(ran_proc, total));
-        int proc = 0;
-        while (proc < P - 1) {
-          const long long ab = __double_as_longlong(sm.accum[proc]);
-          if (ab > vbits || ab == tbits) break;
-          proc++;
+        int proc = P - 1;
+#pragma unroll
+        for (int i = PP - 1; i >= 0; i--) {
+          const long long ab = __double_as_longlong(accum_r[i]);
+          if (ab > vbits || ab == tbits) proc = i;
         }
         const int n = sm.ns[proc];
         if (n <= 0) { status = ST_DEADLOCK; break; }
@@ -869,14 +1009,20 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
         if (idx > n) idx = n;
         if (!KMC_IN(n, 1, S.V)) { status = ST_TABLE; break; }
         const int site = v.as1[(size_t)proc * stride + idx];
-        sm.procstat[proc] += 1;
+        const int fs_off = fast_ok ? H.h[proc] : 0;
+#pragma unroll
+        for (int i = 0; i < PP; i++)
+          if (i == proc) ps_r[i] += 1;  // increment_procstat
+        SOLO_PHASE(2);
         // update_clocks and update_integ_rate, as kmc_run_kernel computes them
-        dt = __dmul_rn(nl, __drcp_rn(total));
+        dt = __dmul_rn(nl, rcp);
         t = __dadd_rn(t, dt);
         kstep += 1;
-        for (int i = 0; i < P; i++) sm.integ[i] = __dadd_rn(sm.integ[i], __dmul_rn(sm.term[i], dt));
+#pragma unroll
+        for (int i = 0; i < PP; i++) integ_r[i] = __dadd_rn(integ_r[i], __dmul_rn(term_r[i], dt));
         if (a.trace) { a.trace[2 * (k + b)] = proc + 1; a.trace[2 * (k + b) + 1] = site; }
         if (site < 1 || site > S.V) { status = ST_TABLE; break; }
+        SOLO_PHASE(3);
         int bx, by, bz;
         {  // calculate_nr2lattice (lattice.mpy:177-210)
           const unsigned c = div_spuck.div((unsigned)(site - 1));
@@ -886,20 +1032,38 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
           by = (int)(r - (unsigned)S.Y * zq);
           bz = (int)zq;
         }
-        v.minp = P;
-        v.err = ST_OK;
-        run_stream(v, v.prog[M.off_proc + proc], bx, by, bz);
-        if (v.err) { status = v.err; break; }
+        SOLO_PHASE(4);
+        int err;
+        int minp;
+        if (fs_off) {
+          v.minp = P;
+          v.err = ST_OK;
+          err = solo_fast_stream(v, H, H.h + fs_off, bx, by, bz, sm.latv, sm.latsite);
+          minp = v.minp;
+        } else {
+          View vv = v;  // the interpreter takes its view by reference: a copy keeps v in registers
+          vv.minp = P;
+          vv.err = ST_OK;
+          run_stream(vv, prog[M.off_proc + proc], bx, by, bz);
+          err = vv.err;
+          minp = vv.minp;
+        }
+        if (err) { status = err; break; }
+        SOLO_PHASE(5);
         int first = P;
-        for (int i = v.minp; i < P; i++) {
-          const int nn = sm.ns[i];
-          if (nn != sm.n0[i]) {
-            sm.term[i] = __dmul_rn(int_to_double(nn), sm.rates[i]);
-            sm.n0[i] = nn;
-            if (first == P) first = i;
+#pragma unroll
+        for (int i = 0; i < PP; i++) {
+          if (i >= minp) {
+            const int nn = sm.ns[i];
+            if (nn != n0_r[i]) {
+              term_r[i] = __dmul_rn(int_to_double(nn), rates_r[i]);
+              n0_r[i] = nn;
+              if (first == P) first = i;
+            }
           }
         }
         from = first;
+        SOLO_PHASE(6);
       }
       sm.from = from;
       sm.status = status;
@@ -918,19 +1082,26 @@ __global__ void __launch_bounds__(32) kmc_solo_kernel(RunArgs a) {
       rbase[0] += used;
     }
   }
-  if (lane < P) {
-    S.integ[lane] = sm.integ[lane];
-    S.procstat[lane] = sm.procstat[lane];
-    S.nsites[lane] = sm.ns[lane];
-    S.accum[lane] = sm.accum[lane];
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < PP; i++) {
+      S.integ[i] = integ_r[i];
+      S.procstat[i] = ps_r[i];
+      S.nsites[i] = sm.ns[i];
+      S.accum[i] = accum_r[i];
+    }
   }
   if (on_chip) {
     group_copy(S.lat, v.lat, S.V, grp);
     group_copy(S.as1, v.as1, tab_b, grp);
     group_copy(S.as2, v.as2, tab_b, grp);
   }
+#ifdef KMC_PHASE_TIMING
+  if (lane == 0 && a.phase)
+    for (int i = 0; i < 7; i++) atomicAdd(&a.phase[i], (unsigned long long)ph[i]);
+#endif
+#undef SOLO_PHASE
   if (lane == 0) {
-    // steps taken: the batches before the last, plus the last batch's completed steps
     S.kmc_time = t;
     S.kmc_time_step = dt;
     S.kmc_step = kstep;
