@@ -7,7 +7,7 @@
 //                      trajectory variants, kmc_run_g16.cu the two-per-warp ones.
 //   kmc_solo_kernel    do_kmc_steps for small launches of models with up to 8
 //                      processes: one warp per trajectory, the steps on one lane
-//                      (kmc_run.cuh).
+//                      (kmc_run.cuh, built in kmc_solo.cu).
 //   kmc_init_kernel    device-side initialize_state (proclist_generic_subroutines.mpy:
 //                      236-304): default species, then every touch-up in parallel
 //                      (fresh touch-ups only append at their own site), then a
@@ -33,7 +33,6 @@
 #include "../../include/kmc_gb300.h"
 #include "kmc_device.cuh"
 #include "kmc_host.h"
-#define KMC_DEFINE_SOLO_KERNEL
 #include "kmc_run.cuh"
 
 using namespace kmc;
@@ -689,24 +688,13 @@ int plan_solo(kmc_pool *p, LaunchPlan &L, size_t ts_max) {
   L.np = 1;
   L.rounds = 0;
   L.g = 32;
-  switch (p->models[L.model].dev.P) {
-    case 1: L.fn = (const void *)kmc_solo_kernel<1>; break;
-    case 2: L.fn = (const void *)kmc_solo_kernel<2>; break;
-    case 3: L.fn = (const void *)kmc_solo_kernel<3>; break;
-    case 4: L.fn = (const void *)kmc_solo_kernel<4>; break;
-    case 5: L.fn = (const void *)kmc_solo_kernel<5>; break;
-    case 6: L.fn = (const void *)kmc_solo_kernel<6>; break;
-    case 7: L.fn = (const void *)kmc_solo_kernel<7>; break;
-    case 8: L.fn = (const void *)kmc_solo_kernel<8>; break;
-    default: return fail(KMC_ERR_ARG, "solo kernel: more processes than it is built for");
-  }
+  // the variant is chosen below, once the placement is known; none has static shared
+  // memory, so any of them gives the dynamic limit
   cudaFuncAttributes fa;
-  CK(cudaFuncGetAttributes(&fa, L.fn));
+  CK(cudaFuncGetAttributes(&fa, solo_kernel(1, false)));
   int optin = 0;
   CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device));
   const int64_t cap = optin - (int64_t)fa.sharedSizeBytes;
-  if (fa.maxDynamicSharedSizeBytes < cap)
-    CK(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   const ModelHost &mh = p->models[L.model];
   const size_t prog_b = align_up((size_t)mh.dev.len * 4, 16);
   const size_t ts = p->tables_on_chip ? align_up(ts_max, 16) : 0;
@@ -715,6 +703,14 @@ int plan_solo(kmc_pool *p, LaunchPlan &L, size_t ts_max) {
   L.a.ts_bytes = 0;
   if ((int64_t)(smem + prog_b) <= cap) { smem += prog_b; L.a.prog_words = mh.dev.len; }
   if (ts > 0 && (int64_t)(smem + ts) <= cap) { smem += ts; L.a.ts_bytes = (int32_t)ts; }
+  // on chip: the program and every trajectory's lattice and tables (ts covers the largest)
+  const bool onchip = L.a.prog_words > 0 && L.a.ts_bytes > 0;
+  L.fn = solo_kernel(mh.dev.P, onchip);
+  if (!L.fn) return fail(KMC_ERR_ARG, "solo kernel: more processes than it is built for");
+  // raise the chosen variant's dynamic shared-memory limit to the device's
+  CK(cudaFuncGetAttributes(&fa, L.fn));
+  if (fa.maxDynamicSharedSizeBytes < cap)
+    CK(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   L.a.groups = 1;
   L.threads = 32;
   L.blocks = L.count;

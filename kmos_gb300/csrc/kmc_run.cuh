@@ -731,10 +731,12 @@ constexpr int SOLO_PMAX = 8;
 
 struct SoloSmem {
   double nl[32], rp[32], rs[32];  // -log(ran_time), ran_proc, ran_site of the batch's steps
+  double tot[32], dtb[32];        // each step's total rate and kmc_time_step
+  double thist[32][SOLO_PMAX];    // each step's terms nr_of_sites * rate (before its edits)
   int32_t latv[FAST_SLOTS];       // slot species before the step
   int32_t latsite[FAST_SLOTS];    // slot sites
   int32_t ns[SOLO_PMAX];          // nr_of_sites
-  int32_t status, used, from, pad;
+  int32_t status, used, from, nclk;
 };
 
 // run_proc_nr of one step through the process's resolved fast stream, serially: the
@@ -828,12 +830,14 @@ __device__ __forceinline__ int solo_fast_stream(View &v, const Hot &H, const int
   return ST_OK;
 }
 
-// Defined in the one translation unit that defines KMC_DEFINE_SOLO_KERNEL (kmc_engine.cu).
+// Defined in the one translation unit that defines KMC_DEFINE_SOLO_KERNEL (kmc_solo.cu).
 // PP = the model's process count exactly, so every loop over processes unrolls to its
 // true length and the vectors stay in registers; __maxnreg__ gives the one warp of the
-// block the registers that takes without spills.
+// block the registers that takes without spills.  ONCHIP: the launch staged the program
+// and every trajectory's lattice and tables in shared memory, so every table pointer is
+// a shared-memory one and its accesses compile to shared-memory loads and stores.
 #ifdef KMC_DEFINE_SOLO_KERNEL
-template <int PP>
+template <int PP, bool ONCHIP>
 __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Group<32> grp;
@@ -856,7 +860,8 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   v.lat = S.lat;
   v.as1 = S.as1;
   v.as2 = S.as2;
-  const bool on_chip = a.ts_bytes > 0 && ts_need(P, S.V) <= (size_t)a.ts_bytes;
+  // the host plans ONCHIP only when the program and every listed trajectory fit
+  constexpr bool on_chip = ONCHIP;
   const size_t lat_b = ((size_t)S.V + 15) / 16 * 16, tab_b = (size_t)P * stride * 4;
   if (on_chip) {
     v.lat = reinterpret_cast<int8_t *>(ts);
@@ -866,7 +871,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
     group_copy(v.as1, S.as1, tab_b, grp);
     group_copy(v.as2, S.as2, tab_b, grp);
   }
-  const int32_t *prog = a.prog_words ? prog_s : M.prog;
+  const int32_t *prog = ONCHIP ? prog_s : (a.prog_words ? prog_s : M.prog);
   v.ns = sm.ns;
   v.prog = prog;
   v.g.X = S.X; v.g.Y = S.Y; v.g.Z = S.Z; v.g.spuck = M.spuck;
@@ -886,7 +891,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
                        (M.reach_x == 0 || S.X > 2 * M.reach_x) && (M.reach_y == 0 || S.Y > 2 * M.reach_y) &&
                        (M.reach_z == 0 || S.Z > 2 * M.reach_z);
   // the process vectors in registers (every index a compile-time constant)
-  double rates_r[PP], accum_r[PP], term_r[PP], integ_r[PP];
+  double rates_r[PP], accum_r[PP], term_r[PP];
   long long ps_r[PP];
   int32_t n0_r[PP];
   bool neg_rate = false;
@@ -896,10 +901,12 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
     accum_r[i] = S.accum[i];
     n0_r[i] = S.nsites[i];
     term_r[i] = __dmul_rn((double)n0_r[i], rates_r[i]);
-    integ_r[i] = S.integ[i];
     ps_r[i] = S.procstat[i];
     neg_rate |= __double_as_longlong(rates_r[i]) < 0;
   }
+  // the running sums of the clock and integ_rates: lane 0 kmc_time, lane 1 + i process
+  // i's integ_rates, advanced once per batch of steps (kmc_time is read by no step)
+  double run_sum = lane == 0 ? S.kmc_time : (lane <= P ? S.integ[lane - 1] : 0.0);
   // with every rate >= +0 every term n*r is >= +0, so is every partial sum, and adding
   // a +0 term leaves a sum >= +0 unchanged bit for bit: the chain skips those adds
   const bool skip_zero = !neg_rate;
@@ -913,7 +920,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   div_spuck.init(M.spuck);
   div_x.init(S.X);
   div_y.init(S.Y);
-  double t = S.kmc_time, dt = S.kmc_time_step;
+  double dt = S.kmc_time_step;
   int64_t kstep = S.kmc_step;
   uint64_t rbase[4] = {S.rng[0], S.rng[1], S.rng[2], S.rng[3]};
   const int rng_kind = S.rng_kind;
@@ -923,9 +930,9 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   int status = ST_OK;
   int used = 0;  // draws of the current batch taken
 #ifdef KMC_PHASE_TIMING
-  // lane 0's cycles per phase of the step (builds with KMC_PHASE_TIMING only): 0 draws,
-  // 1 accum, 2 bisection and site, 3 clock and integ, 4 site coordinates, 5 run_proc_nr,
-  // 6 term refresh
+  // lane 0's cycles per phase of the step (builds with KMC_PHASE_TIMING only): 0 draws
+  // and the previous batch's clock and integ, 1 accum, 2 bisection and site, 3 trace,
+  // 4 site coordinates, 5 run_proc_nr, 6 term refresh
   long long ph[7] = {0, 0, 0, 0, 0, 0, 0};
   long long tp = clock64();
 #define SOLO_PHASE(i)                 \
@@ -965,7 +972,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
     grp.sync();
     const int nb = (int)min((int64_t)32, nsteps - k);
     if (lane == 0) {
-      int from = sm.from, b = 0;
+      int from = sm.from, b = 0, nclk = 0;
       SOLO_PHASE(0);
       for (; b < nb; b++) {
         const double nl = sm.nl[b], ran_proc = sm.rp[b], ran_site = sm.rs[b];
@@ -990,7 +997,6 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
         const double total = accum_r[PP - 1];
         const long long tbits = __double_as_longlong(total);
         if (!(tbits > 0 && tbits < 0x7FF0000000000000LL)) { status = ST_DEADLOCK; break; }
-        const double rcp = __drcp_rn(total);  // issued early: used by the clock below
         SOLO_PHASE(1);
         // determine_procsite (base.mpy:1075-1120, 1234-1338): the first process whose
         // accumulated rate exceeds ran_proc * total, or reaches total
@@ -1014,14 +1020,17 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
         for (int i = 0; i < PP; i++)
           if (i == proc) ps_r[i] += 1;  // increment_procstat
         SOLO_PHASE(2);
-        // update_clocks and update_integ_rate, as kmc_run_kernel computes them
-        dt = __dmul_rn(nl, rcp);
-        t = __dadd_rn(t, dt);
-        kstep += 1;
+        // update_clocks and update_integ_rate: this step's total rate and terms are kept,
+        // and the sums are advanced for the whole batch after it (below), in step order
+        auto clock_integ = [&]() {
+          sm.tot[b] = total;
 #pragma unroll
-        for (int i = 0; i < PP; i++) integ_r[i] = __dadd_rn(integ_r[i], __dmul_rn(term_r[i], dt));
+          for (int i = 0; i < PP; i++) sm.thist[b][i] = term_r[i];
+          kstep += 1;
+          nclk = b + 1;
+        };
         if (a.trace) { a.trace[2 * (k + b)] = proc + 1; a.trace[2 * (k + b) + 1] = site; }
-        if (site < 1 || site > S.V) { status = ST_TABLE; break; }
+        if (site < 1 || site > S.V) { clock_integ(); status = ST_TABLE; break; }
         SOLO_PHASE(3);
         int bx, by, bz;
         {  // calculate_nr2lattice (lattice.mpy:177-210)
@@ -1048,8 +1057,9 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
           err = vv.err;
           minp = vv.minp;
         }
-        if (err) { status = err; break; }
         SOLO_PHASE(5);
+        clock_integ();
+        if (err) { status = err; break; }
         int first = P;
 #pragma unroll
         for (int i = 0; i < PP; i++) {
@@ -1068,10 +1078,29 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
       sm.from = from;
       sm.status = status;
       sm.used = used;
+      sm.nclk = nclk;
     }
     grp.sync();
     status = sm.status;
     used = sm.used;
+    {
+      // the batch's clock and integ_rates (base.mpy:626-645, 1123-1161), as
+      // kmc_run_kernel computes them: kmc_time_step = -log(r) times the reciprocal of the
+      // total rate, one step per lane; then, step by step, kmc_time += kmc_time_step on
+      // lane 0 (its term is 1, and 1 * x is x exactly) and integ(i) += term(i) *
+      // kmc_time_step on lane 1 + i, one instruction stream for both
+      const int nclk = sm.nclk;
+      if (lane < nclk) sm.dtb[lane] = __dmul_rn(sm.nl[lane], __drcp_rn(sm.tot[lane]));
+      grp.sync();
+      const int ti = lane >= 1 && lane <= P ? lane - 1 : 0;
+      for (int j = 0; j < nclk; j++) {
+        const double d = sm.dtb[j];
+        const double term = lane == 0 ? 1.0 : sm.thist[j][ti];
+        run_sum = __dadd_rn(run_sum, __dmul_rn(term, d));
+      }
+      if (nclk > 0) dt = sm.dtb[nclk - 1];
+      grp.sync();
+    }
     k += nb;
   }
   // random state after the draws actually used: `used` draws of the last batch
@@ -1085,12 +1114,12 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < PP; i++) {
-      S.integ[i] = integ_r[i];
       S.procstat[i] = ps_r[i];
       S.nsites[i] = sm.ns[i];
       S.accum[i] = accum_r[i];
     }
   }
+  if (lane >= 1 && lane <= P) S.integ[lane - 1] = run_sum;
   if (on_chip) {
     group_copy(S.lat, v.lat, S.V, grp);
     group_copy(S.as1, v.as1, tab_b, grp);
@@ -1102,7 +1131,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
 #endif
 #undef SOLO_PHASE
   if (lane == 0) {
-    S.kmc_time = t;
+    S.kmc_time = run_sum;
     S.kmc_time_step = dt;
     S.kmc_step = kstep;
     S.rng[0] = rbase[0]; S.rng[1] = rbase[1]; S.rng[2] = rbase[2]; S.rng[3] = rbase[3];
@@ -1119,4 +1148,6 @@ namespace kmc_host {
 // lanes per trajectory; null for a variant that is not built.
 const void *run_kernel_g32(int np, int r);
 const void *run_kernel_g16(int np, int r);
+// Host stub of the solo kernel for a model of P processes (null beyond SOLO_PMAX).
+const void *solo_kernel(int P, bool onchip);
 }  // namespace kmc_host
