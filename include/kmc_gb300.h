@@ -374,6 +374,11 @@ KMC_API int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_
 /* Device time of the last launch (CUDA events on the handle's stream) and launch count. */
 KMC_API int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms);
 KMC_API int kmc_otf_launch_count(kmc_otf *h, int64_t *n);
+/* Cycles the otf step loop spent per phase, summed over trajectories (8 entries: draws,
+ * running sums and accum_rates, clock and integ, pick, event op list, event evaluation,
+ * event replay, unused), in builds compiled with KMC_PHASE_TIMING; KMC_ERR_ARG
+ * otherwise.  reset != 0 clears them. */
+KMC_API int kmc_otf_phase_cycles(kmc_otf *h, uint64_t *out, int32_t reset);
 
 #ifdef __cplusplus
 }

@@ -70,7 +70,32 @@ struct Dev {
   int64_t *procstat;
   const double *rates, *userpar;
   Traj *traj;
+  unsigned long long *phase;  // OTF_NPHASE cycle sums (KMC_PHASE_TIMING builds)
 };
+
+// Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
+// the clock64() time since its previous mark to phase i: 0 draws, 1 running sums and
+// accum_rates, 2 clock and integ, 3 process and entry pick, 4 event: replaces and op list,
+// 5 event: conditions and rates evaluated in parallel, 6 event: table replay.
+constexpr int OTF_NPHASE = 8;
+#ifdef KMC_PHASE_TIMING
+#define OTF_MARK(i)                     \
+  do {                                  \
+    if ((threadIdx.x & 31) == 0) {      \
+      const long long now_ = clock64(); \
+      oph[i] += now_ - otp;             \
+      otp = now_;                       \
+    }                                   \
+  } while (0)
+#define OTF_PH_PARAMS , long long *oph, long long &otp
+#define OTF_PH_ARGS , oph, otp
+#else
+#define OTF_MARK(i) \
+  do {              \
+  } while (0)
+#define OTF_PH_PARAMS
+#define OTF_PH_ARGS
+#endif
 
 // One trajectory's view.
 struct View {
@@ -341,7 +366,7 @@ struct EventSmem {
 // table.  Updates come before adds in every stream, so an update whose entry was absent
 // before the event is absent at its turn too and needs no rate.  Ops past the first
 // OTF_RATE_OPS are done by lane 0 alone.
-__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane) {
+__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane OTF_PH_PARAMS) {
   const int32_t *w = v.d->prog;
   int nops = 0;
   if (lane == 0) {
@@ -366,6 +391,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
   nops = __shfl_sync(0xFFFFFFFFu, nops, 0);
   const int err0 = __shfl_sync(0xFFFFFFFFu, v.err, 0);
   __syncwarp();
+  OTF_MARK(4);
   if (err0) return;
   for (int k = lane; k < nops; k += 32) {
     const int p = es.off[k];
@@ -387,6 +413,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     es.ok[k] = ok ? 1 : 0;
   }
   __syncwarp();
+  OTF_MARK(5);
   if (lane != 0) return;
   uint64_t moved = 0;  // processes (0-based, < 64) an op of this event deleted or added
   int k = 0;
@@ -601,10 +628,16 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     return;
   }
   // cmd 0: do_kmc_steps (proclist_generic_subroutines.mpy:1-44)
+#ifdef KMC_PHASE_TIMING
+  long long oph[OTF_NPHASE] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long otp = clock64();
+#endif
   for (int64_t step = 0; step < n; step++) {
     double r0, r1, r2;
     draw3(tr.rng_kind, tr.rng, tr.seed, tr.traj, r0, r1, r2);
+    OTF_MARK(0);
     accum_step(v, sacc, stot, lane);
+    OTF_MARK(1);
     const double total = sacc[P];
     if (!(total > 0.0)) { tr.status = ST_DEADLOCK; break; }
     // update_clocks (base_otf.f90:1280-1320), update_integ_rate (719-738)
@@ -613,6 +646,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     tr.kmc_step += 1;
     for (int p0 = lane; p0 < P; p0 += 32)
       v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(stot[p0], tr.kmc_time_step));
+    OTF_MARK(2);
     int err = 0, proc = 0, site = 0;
     if (lane == 0) {
       proc = interval_search(sacc, P, __dmul_rn(r1, total));
@@ -635,15 +669,21 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     if (err) { tr.status = err; break; }
     proc = __shfl_sync(0xFFFFFFFFu, proc, 0);
     site = __shfl_sync(0xFFFFFFFFu, site, 0);
+    OTF_MARK(3);
     {
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_event(v, sm.ev[warp], d.prog[d.off_proc + proc - 1], x, y, z, lane);
+      run_event(v, sm.ev[warp], d.prog[d.off_proc + proc - 1], x, y, z, lane OTF_PH_ARGS);
     }
     err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
+    OTF_MARK(6);
     if (err) { tr.status = err; break; }
   }
+#ifdef KMC_PHASE_TIMING
+  if (lane == 0 && d.phase)
+    for (int i = 0; i < OTF_NPHASE; i++) atomicAdd(&d.phase[i], (unsigned long long)oph[i]);
+#endif
   for (int p0 = lane; p0 < P; p0 += 32) v.accum[p0] = sacc[p0 + 1];
   if (lane == 0) d.traj[t] = tr;
 }
@@ -846,9 +886,10 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   const size_t PV = (size_t)P * (V + 1), TP = (size_t)T * P;
   const size_t sizes[] = {(size_t)len * 4, (size_t)T * V, T * PV * 4, T * PV * 4, T * PV * 8, T * PV * 8,
                           TP * 4, TP * 4, TP * 8, TP * 8, TP * 8, TP * 8, (size_t)T * sizeof(Traj),
-                          (size_t)P * 8, (size_t)(d.nuser > 0 ? d.nuser : 1) * 8};
-  size_t offs[15], total = 0;
-  for (int i = 0; i < 15; i++) { offs[i] = total; total = align_up(total + sizes[i], 256); }
+                          (size_t)P * 8, (size_t)(d.nuser > 0 ? d.nuser : 1) * 8,
+                          (size_t)otfdev::OTF_NPHASE * 8};
+  size_t offs[16], total = 0;
+  for (int i = 0; i < 16; i++) { offs[i] = total; total = align_up(total + sizes[i], 256); }
   auto cleanup = [&](int code) { if (h->mem) cudaFree(h->mem); if (h->stream) cudaStreamDestroy(h->stream);
                                  if (h->ev0) cudaEventDestroy(h->ev0); if (h->ev1) cudaEventDestroy(h->ev1);
                                  delete h; return code; };
@@ -869,6 +910,7 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   d.traj = (Traj *)(base + offs[12]);
   h->d_rates = (double *)(base + offs[13]); h->d_userpar = (double *)(base + offs[14]);
   d.rates = h->d_rates; d.userpar = h->d_userpar;
+  d.phase = (unsigned long long *)(base + offs[15]);
   h->rates.assign(P, 0.0);
   h->userpar.assign(d.nuser, 0.0);
   std::vector<Traj> tr(T);
@@ -1027,6 +1069,19 @@ int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms) {
   if (!h || !ms) return fail(KMC_ERR_ARG, "bad arguments");
   *ms = h->last_ms;
   return KMC_OK;
+}
+
+int kmc_otf_phase_cycles(kmc_otf *h, uint64_t *out, int32_t reset) {
+  if (!h || !out) return fail(KMC_ERR_ARG, "bad arguments");
+#ifdef KMC_PHASE_TIMING
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(out, h->d.phase, sizeof(unsigned long long) * otfdev::OTF_NPHASE, cudaMemcpyDeviceToHost));
+  if (reset) CK(cudaMemset(h->d.phase, 0, sizeof(unsigned long long) * otfdev::OTF_NPHASE));
+  return KMC_OK;
+#else
+  (void)reset;
+  return fail(KMC_ERR_ARG, "library built without KMC_PHASE_TIMING");
+#endif
 }
 
 int kmc_otf_launch_count(kmc_otf *h, int64_t *n) {

@@ -975,7 +975,7 @@ __global__ void __maxnreg__(224) kmc_solo_kernel(RunArgs a) {
       int from = sm.from, b = 0, nclk = 0;
       SOLO_PHASE(0);
       for (; b < nb; b++) {
-        const double nl = sm.nl[b], ran_proc = sm.rp[b], ran_site = sm.rs[b];
+        const double ran_proc = sm.rp[b], ran_site = sm.rs[b];
         used = b + 1;
         // update_accum_rate from the first stale entry (base.mpy:603-623)
         if (from < P) {

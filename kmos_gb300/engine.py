@@ -128,6 +128,7 @@ SIGNATURES = {
     "kmc_otf_get_state": (_i32, [_vp, _i32, _p32, _p32, _p32, _p32, _p64, _pd, _pd, _pd, _pd, _pd, _p64]),
     "kmc_otf_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_otf_launch_count": (_i32, [_vp, _p64]),
+    "kmc_otf_phase_cycles": (_i32, [_vp, ctypes.POINTER(ctypes.c_uint64), _i32]),
 }
 
 _lib = None
@@ -783,3 +784,10 @@ class OtfBatch:
         n = _i64()
         _check(load().kmc_otf_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+    def phase_cycles(self, reset: bool = True) -> np.ndarray:
+        """Per-phase cycle sums of the otf step loop (library built with KMC_PHASE_TIMING)."""
+        out = np.zeros(8, np.uint64)
+        _check(load().kmc_otf_phase_cycles(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                           1 if reset else 0))
+        return out
