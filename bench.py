@@ -142,12 +142,19 @@ class Clocks:
         except OSError:
             self.proc = None
             return
+        self.first = threading.Event()
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        # the first query of a fresh nvidia-smi can hold the driver for seconds, and a
+        # launch made meanwhile waits for it: the timed region starts after the first
+        # sample has arrived
+        self.first.wait(timeout=30.0)
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+            self.first.set()
+        self.first.set()
 
     def stop(self):
         if not self.proc:
