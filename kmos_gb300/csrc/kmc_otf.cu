@@ -18,14 +18,15 @@
 // left-to-right sums bit for bit, and pm is at once the accum_rates_proc array
 // determine_procsite (base_otf.f90:1213-1277) searches.
 //
-// One warp per trajectory.  A step: lanes re-sum the stale lists (one process per lane,
-// a serial chain each), lane 0 chains the process totals into accum_rates, every lane
-// advances the clock and integ_rates of its processes, lane 0 picks the process and the
-// entry (interval_search_real on accum_rates and on the chosen list's running sums), and
-// the event runs (run_event): lane 0 writes the lattice, the lanes load the table
-// positions and evaluate the add conditions and the rate programs (gr_<name>,
-// io:2800-2965) in parallel, lane 0 replays guarded dels, rate updates and adds in
-// program order.
+// One warp per trajectory, four per block; each block first copies the program to its
+// shared memory.  A step: lanes re-sum the stale lists (one process per lane, a serial
+// chain each), lane 0 chains the process totals into accum_rates, every lane advances
+// the clock and integ_rates of its processes, lane 0 picks the process and the entry
+// (interval_search_real on accum_rates and on the chosen list's running sums), and the
+// event runs (run_event): lane 0 writes the lattice, the lanes load the table positions
+// and evaluate the add conditions and the rate programs (gr_<name>, io:2800-2965) in
+// parallel, then every lane replays the guarded dels, rate updates and adds of its own
+// processes in program order (ops of different processes touch different rows).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -71,6 +72,8 @@ struct Dev {
   const double *rates, *userpar;
   Traj *traj;
   unsigned long long *phase;  // OTF_NPHASE cycle sums (KMC_PHASE_TIMING builds)
+  int32_t prog_len;           // program words
+  int32_t prog_staged;        // 1: each block copies the program to shared memory
 };
 
 // Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
@@ -100,6 +103,7 @@ constexpr int OTF_NPHASE = 8;
 // One trajectory's view.
 struct View {
   const Dev *d;
+  const int32_t *prog;  // the program: the block's shared-memory copy when staged
   int8_t *lat;
   int32_t *as1, *as2, *dirty, *ns;
   double *rm, *pm, *integ, *accum, *tot;
@@ -112,6 +116,7 @@ struct View {
 __device__ inline View view_of(const Dev &d, int t) {
   View v;
   v.d = &d;
+  v.prog = d.prog;
   const size_t PV = (size_t)d.P * (d.V + 1);
   v.lat = d.lat + (size_t)t * d.V;
   v.as1 = d.as1 + (size_t)t * PV;
@@ -155,7 +160,7 @@ __device__ inline double powi_kind(double xd, int32_t m, int kind) {
 // gr_<p>(cell): bystander counts, then the rate program with base_rate = rates(p).
 __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
   const Dev &d = *v.d;
-  const int32_t *r = d.prog + d.prog[d.off_rate + p - 1];
+  const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
   const int nb = r[0], nv = r[1];
   int32_t nr[OTF_NRMAX];
   for (int k = 0; k < nv; k++) nr[k] = 0;
@@ -285,7 +290,7 @@ __device__ inline bool can_do(const View &v, int p, int site) { return v.as2[v.r
 
 // One op stream (run_proc_<name> or touchup_cell) at cell (bx, by, bz), serially.
 __device__ void run_stream(View &v, int pos, int bx, int by, int bz) {
-  const int32_t *w = v.d->prog;
+  const int32_t *w = v.prog;
   for (;;) {
     if (v.err) return;
     const uint32_t h = (uint32_t)w[pos];
@@ -349,8 +354,10 @@ constexpr int OTF_RATE_OPS = 128;  // rate evaluations of one event done warp-pa
 
 struct EventSmem {
   double rate[OTF_RATE_OPS];
-  int32_t off[OTF_RATE_OPS];
+  int32_t off[OTF_RATE_OPS];  // program offsets of the stream's table ops
   int32_t m0[OTF_RATE_OPS];   // avail_sites(p, site, 2) before the event
+  int32_t site[OTF_RATE_OPS]; // the op's site
+  int16_t p0[OTF_RATE_OPS];   // the op's process, 0-based
   int8_t ok[OTF_RATE_OPS];
 };
 
@@ -360,15 +367,20 @@ struct EventSmem {
 // do not read the lattice), so: (1) lane 0 applies the replaces and lists the table
 // ops; (2) lanes load each op's avail_sites(p, site, 2) as it stands before the event
 // and evaluate the add conditions and the rates in parallel, from the final lattice;
-// (3) lane 0 replays the table operations in program order with those values.  A
-// position loaded in (2) is used while no earlier op of the event has deleted or added
-// an entry of that process (updates move no entry); after that the replay reads the
-// table.  Updates come before adds in every stream, so an update whose entry was absent
-// before the event is absent at its turn too and needs no rate.  Ops past the first
-// OTF_RATE_OPS are done by lane 0 alone.
+// (3) the table operations are replayed with those values: every op touches only its
+// own process's rows, running total, list length and stale mark, so ops of different
+// processes commute, and lane j replays the ops of processes j, j + 32, ... in program
+// order.  A position loaded in (2) is used while no earlier op of the event has deleted
+// or added an entry of that process (updates move no entry); after that the replay
+// reads the table.  Updates come before adds in every stream, so an update whose entry
+// was absent before the event is absent at its turn too and needs no rate.  A stream of
+// more than OTF_RATE_OPS ops is replayed by lane 0 alone, in program order, the ops past
+// the listed ones evaluated there.
 __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane OTF_PH_PARAMS) {
-  const int32_t *w = v.d->prog;
+  const int32_t *w = v.prog;
+  int32_t *offs = es.off;
   int nops = 0;
+  bool over = false;
   if (lane == 0) {
     for (int p = pos;;) {
       const uint32_t h = (uint32_t)w[p];
@@ -380,7 +392,8 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
         v.lat[site - 1] = (int8_t)w[p + 3];
         p += 4;
       } else if (op == OP_ADD || op == OP_UPDATE || op == OP_GDEL) {
-        if (nops < OTF_RATE_OPS) es.off[nops++] = p;
+        if (nops < OTF_RATE_OPS) offs[nops++] = p;
+        else over = true;
         p += op == OP_ADD ? 2 + 2 * cnt : 2;
       } else {
         v.err = ST_PROGRAM;
@@ -389,15 +402,17 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     }
   }
   nops = __shfl_sync(0xFFFFFFFFu, nops, 0);
+  over = __shfl_sync(0xFFFFFFFFu, over, 0);
   const int err0 = __shfl_sync(0xFFFFFFFFu, v.err, 0);
   __syncwarp();
   OTF_MARK(4);
   if (err0) return;
   for (int k = lane; k < nops; k += 32) {
-    const int p = es.off[k];
+    const int p = offs[k];
     const uint32_t h = (uint32_t)w[p];
     const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-    const int m0 = v.as2[v.row(arg - 1) + v.g.site(bx, by, bz, w[p + 1])];
+    const int site = v.g.site(bx, by, bz, w[p + 1]);
+    const int m0 = v.as2[v.row(arg - 1) + site];
     bool ok = op == OP_ADD || (op == OP_UPDATE && m0 != 0);
     if (op == OP_ADD)
       for (int c = 0; c < cnt && ok; c++)
@@ -411,9 +426,48 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     es.m0[k] = m0;
     es.rate[k] = rate;
     es.ok[k] = ok ? 1 : 0;
+    es.site[k] = site;
+    es.p0[k] = (int16_t)(arg - 1);
   }
   __syncwarp();
   OTF_MARK(5);
+  if (!over) {
+    // one process per lane: its ops in program order (base_otf.f90:221-364)
+    uint32_t moved = 0;  // bit (p0 >> 5): an op of this event deleted or added an entry of p0
+    for (int k = 0; k < nops && !v.err; k++) {
+      const int p0 = es.p0[k];
+      if ((p0 & 31) != lane) continue;
+      const int p = offs[k];
+      const int op = (uint32_t)w[p] & 0xFF;
+      const int site = es.site[k];
+      const uint32_t bit = 1u << (p0 >> 5);
+      const int m = (moved & bit) ? v.as2[v.row(p0) + site] : es.m0[k];
+      if (op == OP_GDEL) {
+        if (m != 0) {
+          del_at(v, p0 + 1, site, m);
+          moved |= bit;
+        }
+      } else if (op == OP_ADD) {
+        if (es.ok[k]) {
+          add_at(v, p0 + 1, site, es.rate[k], m);
+          moved |= bit;
+        }
+      } else if (m != 0) {  // OP_UPDATE (base_otf.f90:333-364)
+        double rate = es.rate[k];
+        if (!es.ok[k]) {  // absent before the event, present now
+          int cx, cy, cz;
+          v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
+          rate = rate_of(v, p0 + 1, cx, cy, cz);
+        }
+        double *r = v.rm + v.row(p0);
+        v.tot[p0] = __dsub_rn(__dadd_rn(v.tot[p0], rate), r[m]);
+        r[m] = rate;
+        mark(v, p0, m);
+      }
+    }
+    v.err = (int)__reduce_max_sync(0xFFFFFFFFu, (unsigned)v.err);
+    return;
+  }
   if (lane != 0) return;
   uint64_t moved = 0;  // processes (0-based, < 64) an op of this event deleted or added
   int k = 0;
@@ -549,26 +603,33 @@ struct Smem {
 // trace); 1 = update_accum_rate; 2 = update_integ_rate; 3 = get_next_kmc_step of `only`
 // (out[0..1]); 4 = run_proc_nr(out[0], out[1]) on `only`; 5 = initialize_state(layer = n);
 // 6 = recalculate_rates_matrix.
-__global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
+__global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
   __shared__ Smem sm;
+  extern __shared__ __align__(16) int32_t prog_s[];  // the program, when staged
+  // the block copies the program to shared memory first (every thread is still here)
+  if (d.prog_staged) {
+    for (int i = threadIdx.x; i < d.prog_len; i += blockDim.x) prog_s[i] = d.prog[i];
+    __syncthreads();
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t = blockIdx.x * OTF_WARPS + warp;
   if (t >= d.T || (only >= 0 && t != only)) return;
   View v = view_of(d, t);
+  if (d.prog_staged) v.prog = prog_s;
   Traj tr = d.traj[t];
   if (tr.status && cmd != 5) return;
   double *sacc = sm.acc[warp], *stot = sm.tot[warp];
   const int P = d.P;
   if (cmd == 5) {  // initialize_state (proclist_generic_subroutines.mpy:236-304), the cell touch-up
     if (lane == 0) {
-      const int32_t *site_layer = d.prog + d.off_site_layer, *site_def = d.prog + d.off_site_default;
+      const int32_t *site_layer = v.prog + d.off_site_layer, *site_def = v.prog + d.off_site_default;
       for (int s = 1; s <= d.V; s++) {
         const int nr = (s - 1) % d.spuck + 1;
         v.lat[s - 1] = (int8_t)(site_layer[nr - 1] == (int)n ? site_def[nr - 1] : d.null_species);
       }
       for (int k = 0; k < d.Z && !v.err; k++)
         for (int j = 0; j < d.Y && !v.err; j++)
-          for (int i = 0; i < d.X && !v.err; i++) run_stream(v, d.prog[d.off_touch], i, j, k);
+          for (int i = 0; i < d.X && !v.err; i++) run_stream(v, v.prog[d.off_touch], i, j, k);
       tr.status = v.err;
       d.traj[t] = tr;
     }
@@ -621,7 +682,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
       v.procstat[proc - 1] += 1;
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_stream(v, d.prog[d.off_proc + proc - 1], x, y, z);
+      run_stream(v, v.prog[d.off_proc + proc - 1], x, y, z);
       tr.status = v.err;
       d.traj[t] = tr;
     }
@@ -673,7 +734,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
     {
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_event(v, sm.ev[warp], d.prog[d.off_proc + proc - 1], x, y, z, lane OTF_PH_ARGS);
+      run_event(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane OTF_PH_ARGS);
     }
     err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
@@ -684,6 +745,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS) otf_kernel(Dev d, int cmd, int
   if (lane == 0 && d.phase)
     for (int i = 0; i < OTF_NPHASE; i++) atomicAdd(&d.phase[i], (unsigned long long)oph[i]);
 #endif
+
   for (int p0 = lane; p0 < P; p0 += 32) v.accum[p0] = sacc[p0 + 1];
   if (lane == 0) d.traj[t] = tr;
 }
@@ -830,8 +892,23 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     d.accum += (size_t)only * d.P; d.tot += (size_t)only * d.P; d.procstat += (size_t)only * d.P;
     d.traj += only; d.T = 1;
   }
+  // the program goes to every block's shared memory when it fits beside the static part
+  size_t dyn = 0;
+  {
+    cudaFuncAttributes fa;
+    CK(cudaFuncGetAttributes(&fa, otfdev::otf_kernel));
+    int optin = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int64_t cap = optin - (int64_t)fa.sharedSizeBytes;
+    const size_t want = align_up((size_t)d.prog_len * 4, 16);
+    d.prog_staged = (int64_t)want <= cap ? 1 : 0;
+    if (d.prog_staged) dyn = want;
+    if (dyn > 0 && fa.maxDynamicSharedSizeBytes < (int)dyn)
+      CK(cudaFuncSetAttribute(otfdev::otf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+  }
   CK(cudaEventRecord(h->ev0, h->stream));
-  otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, 0, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
+  otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, dyn, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
   CK(cudaGetLastError());
   CK(cudaEventRecord(h->ev1, h->stream));
   h->launches++;
@@ -901,6 +978,8 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   char *base = (char *)h->mem;
   int32_t *dprog = (int32_t *)(base + offs[0]);
   d.prog = dprog;
+  d.prog_len = len;
+  d.prog_staged = 0;
   d.lat = (int8_t *)(base + offs[1]);
   d.as1 = (int32_t *)(base + offs[2]); d.as2 = (int32_t *)(base + offs[3]);
   d.rm = (double *)(base + offs[4]); d.pm = (double *)(base + offs[5]);
