@@ -351,6 +351,7 @@ __device__ void run_stream(View &v, int pos, int bx, int by, int bz) {
 }
 
 constexpr int OTF_RATE_OPS = 128;  // rate evaluations of one event done warp-parallel
+constexpr int OTF_PMASK_PROCS = 64; // models of up to 64 processes replay through per-process masks
 
 struct EventSmem {
   double rate[OTF_RATE_OPS];
@@ -359,6 +360,7 @@ struct EventSmem {
   int32_t site[OTF_RATE_OPS]; // the op's site
   int16_t p0[OTF_RATE_OPS];   // the op's process, 0-based
   int8_t ok[OTF_RATE_OPS];
+  uint32_t pmask[OTF_PMASK_PROCS][OTF_RATE_OPS / 32];  // each process's ops, one bit per op
 };
 
 // run_proc_<name> of a step with the whole warp.  Every rate and every add condition
@@ -428,16 +430,16 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     es.ok[k] = ok ? 1 : 0;
     es.site[k] = site;
     es.p0[k] = (int16_t)(arg - 1);
+    if (arg - 1 < OTF_PMASK_PROCS) atomicOr(&es.pmask[arg - 1][k >> 5], 1u << (k & 31));
   }
   __syncwarp();
   OTF_MARK(5);
   if (!over) {
     // one process per lane: its ops in program order (base_otf.f90:221-364)
     uint32_t moved = 0;  // bit (p0 >> 5): an op of this event deleted or added an entry of p0
-    for (int k = 0; k < nops && !v.err; k++) {
+    auto apply = [&](int k) {
       const int p0 = es.p0[k];
-      if ((p0 & 31) != lane) continue;
-      const int p = offs[k];
+      const int p = es.off[k];
       const int op = (uint32_t)w[p] & 0xFF;
       const int site = es.site[k];
       const uint32_t bit = 1u << (p0 >> 5);
@@ -464,10 +466,31 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
         r[m] = rate;
         mark(v, p0, m);
       }
+    };
+    if (v.d->P <= OTF_PMASK_PROCS) {
+      // each lane walks only its own processes' ops (bits of their masks, cleared as
+      // read), so the lanes' replays run side by side
+      for (int q = lane; q < v.d->P; q += 32)
+        for (int wd = 0; wd < OTF_RATE_OPS / 32; wd++) {
+          uint32_t b = es.pmask[q][wd];
+          es.pmask[q][wd] = 0u;
+          while (b && !v.err) {
+            const int k = 32 * wd + __ffs(b) - 1;
+            b &= b - 1;
+            apply(k);
+          }
+        }
+    } else {
+      for (int k = 0; k < nops && !v.err; k++)
+        if ((es.p0[k] & 31) == lane) apply(k);
     }
     v.err = (int)__reduce_max_sync(0xFFFFFFFFu, (unsigned)v.err);
     return;
   }
+  // more ops than listed: lane 0 replays the stream alone; the masks are emptied first
+  for (int q = lane; q < v.d->P && q < OTF_PMASK_PROCS; q += 32)
+    for (int wd = 0; wd < OTF_RATE_OPS / 32; wd++) es.pmask[q][wd] = 0u;
+  __syncwarp();
   if (lane != 0) return;
   uint64_t moved = 0;  // processes (0-based, < 64) an op of this event deleted or added
   int k = 0;
@@ -688,7 +711,10 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
     }
     return;
   }
-  // cmd 0: do_kmc_steps (proclist_generic_subroutines.mpy:1-44)
+  // cmd 0: do_kmc_steps (proclist_generic_subroutines.mpy:1-44); the event masks start
+  // empty and every event's replay leaves them empty
+  for (int i = lane; i < OTF_PMASK_PROCS * (OTF_RATE_OPS / 32); i += 32) (&sm.ev[warp].pmask[0][0])[i] = 0u;
+  __syncwarp();
 #ifdef KMC_PHASE_TIMING
   long long oph[OTF_NPHASE] = {0, 0, 0, 0, 0, 0, 0, 0};
   long long otp = clock64();
