@@ -719,16 +719,43 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
   long long oph[OTF_NPHASE] = {0, 0, 0, 0, 0, 0, 0, 0};
   long long otp = clock64();
 #endif
-  for (int64_t step = 0; step < n; step++) {
-    double r0, r1, r2;
-    draw3(tr.rng_kind, tr.rng, tr.seed, tr.traj, r0, r1, r2);
+  // random numbers: every 32 steps lane j draws step k + j's (ran_time, ran_proc,
+  // ran_site) and -log(ran_time); steps take them with shuffles
+  uint64_t rbase[4] = {tr.rng[0], tr.rng[1], tr.rng[2], tr.rng[3]};
+  double my_nl = 0.0, my_r1 = 0.0, my_r2 = 0.0;
+  int bidx = 32;
+  int64_t step = 0;
+  for (; step < n; step++) {
+    if (bidx == 32) {
+      if (step > 0) {  // past the batch just used
+        if (tr.rng_kind == RNG_GFORTRAN) {
+          for (int dd = 0; dd < 96; dd++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
+        } else {
+          rbase[0] += 32;
+        }
+      }
+      uint64_t st[4] = {rbase[0], rbase[1], rbase[2], rbase[3]};
+      if (tr.rng_kind == RNG_GFORTRAN) {
+        for (int dd = 0; dd < 3 * lane; dd++) xoshiro_next(st[0], st[1], st[2], st[3]);
+      } else {
+        st[0] += lane;
+      }
+      double q0;
+      draw3(tr.rng_kind, st, tr.seed, tr.traj, q0, my_r1, my_r2);
+      my_nl = -log(q0);
+      bidx = 0;
+    }
+    const double nl = __shfl_sync(0xFFFFFFFFu, my_nl, bidx);
+    const double r1 = __shfl_sync(0xFFFFFFFFu, my_r1, bidx);
+    const double r2 = __shfl_sync(0xFFFFFFFFu, my_r2, bidx);
+    bidx++;
     OTF_MARK(0);
     accum_step(v, sacc, stot, lane);
     OTF_MARK(1);
     const double total = sacc[P];
     if (!(total > 0.0)) { tr.status = ST_DEADLOCK; break; }
     // update_clocks (base_otf.f90:1280-1320), update_integ_rate (719-738)
-    tr.kmc_time_step = __ddiv_rn(-log(r0), total);
+    tr.kmc_time_step = __ddiv_rn(nl, total);
     tr.kmc_time = __dadd_rn(tr.kmc_time, tr.kmc_time_step);
     tr.kmc_step += 1;
     for (int p0 = lane; p0 < P; p0 += 32)
@@ -771,6 +798,16 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
   if (lane == 0 && d.phase)
     for (int i = 0; i < OTF_NPHASE; i++) atomicAdd(&d.phase[i], (unsigned long long)oph[i]);
 #endif
+  // the random state after the draws actually used: bidx draws of the current batch (a
+  // step that found no process has drawn its numbers, as in the reference)
+  if (bidx < 32 || step > 0) {
+    if (tr.rng_kind == RNG_GFORTRAN) {
+      for (int dd = 0; dd < 3 * bidx; dd++) xoshiro_next(rbase[0], rbase[1], rbase[2], rbase[3]);
+    } else {
+      rbase[0] += bidx;
+    }
+  }
+  tr.rng[0] = rbase[0]; tr.rng[1] = rbase[1]; tr.rng[2] = rbase[2]; tr.rng[3] = rbase[3];
 
   for (int p0 = lane; p0 < P; p0 += 32) v.accum[p0] = sacc[p0 + 1];
   if (lane == 0) d.traj[t] = tr;

@@ -37,7 +37,11 @@ def main(argv=None):
     from . import configs, engine as E
     sides = [int(x) for x in a.sides.split(",")] if a.sides else None
     wl = configs.build(a.config, n=a.ntraj, steps=0, sides=sides)
-    pool = E.Pool(arena_bytes=1 << 30, max_slots=max(4, wl.n))
+    probe = E.Pool(arena_bytes=1 << 20, max_slots=1)
+    pmid = probe.add_model(wl.program)
+    need = sum(probe.slot_bytes(pmid, sz) for sz in wl.sizes)
+    probe.close()
+    pool = E.Pool(arena_bytes=need + (64 << 20), max_slots=max(4, wl.n))
     pool.set_solo(bool(a.solo))
     pool.set_fast_path(bool(a.fast))
     mid = pool.add_model(wl.program)
