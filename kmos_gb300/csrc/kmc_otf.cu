@@ -74,7 +74,6 @@ struct Dev {
   unsigned long long *phase;  // OTF_NPHASE cycle sums (KMC_PHASE_TIMING builds)
   int32_t prog_len;           // program words
   int32_t prog_staged;        // 1: each block copies the program to shared memory
-  int32_t rate_small;         // 1: every rate program fits rate_of_small's registers
 };
 
 // Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
@@ -158,90 +157,9 @@ __device__ inline double powi_kind(double xd, int32_t m, int kind) {
   return (double)y;
 }
 
-// One binary instruction of a typed rate program on (a, b): integers as gfortran's
-// wrapping int32 arithmetic with truncating division, default reals in IEEE single,
-// real(8) in double, integer powers by binary powering.
-__device__ inline double rate_binary(int op, int kind, double a, double b2) {
-  if (op == I_POWI) return powi_kind(a, (int32_t)b2, kind);
-  if (op == I_POW) return kind == K_F32 ? (double)powf((float)a, (float)b2) : pow(a, b2);
-  if (kind == K_INT) {
-    const int32_t ia = (int32_t)a, ib = (int32_t)b2;
-    return op == I_ADD ? (double)(int32_t)((uint32_t)ia + (uint32_t)ib)
-         : op == I_SUB ? (double)(int32_t)((uint32_t)ia - (uint32_t)ib)
-         : op == I_MUL ? (double)(int32_t)((uint32_t)ia * (uint32_t)ib)
-         : (ib == 0 ? 0.0 : (ib == -1 ? (double)(int32_t)(0u - (uint32_t)ia) : (double)(ia / ib)));
-  }
-  if (kind == K_F32) {
-    const float fa = (float)a, fb = (float)b2;
-    return op == I_ADD ? __fadd_rn(fa, fb) : op == I_SUB ? __fsub_rn(fa, fb)
-         : op == I_MUL ? __fmul_rn(fa, fb) : __fdiv_rn(fa, fb);
-  }
-  return op == I_ADD ? __dadd_rn(a, b2) : op == I_SUB ? __dsub_rn(a, b2)
-       : op == I_MUL ? __dmul_rn(a, b2) : __ddiv_rn(a, b2);
-}
-
-// One unary instruction of a typed rate program.
-__device__ inline double rate_unary(int op, int kind, int arg, double x) {
-  switch (op) {
-    case I_NEG: return kind == K_INT ? (double)(int32_t)(0u - (uint32_t)(int32_t)x) : -x;
-    case I_EXP: return kind == K_F32 ? (double)expf((float)x) : exp(x);
-    case I_LOG: return kind == K_F32 ? (double)logf((float)x) : log(x);
-    case I_SQRT: return kind == K_F32 ? (double)__fsqrt_rn((float)x) : __dsqrt_rn(x);
-    case I_ABS: return fabs(x);
-    default:  // I_CVT
-      return (kind == K_INT && arg == K_F32) ? (double)(float)(int32_t)x : x;
-  }
-}
-
-// gr_<p>(cell) for models whose every rate program keeps at most 4 values on its stack,
-// counts at most 8 bystander variables over at most 255 sites and uses no auxiliary
-// variables (Dev::rate_small): the counts packed 8 bits per variable and the stack in
-// four registers (s0 the top), so nothing goes to local memory.
-__device__ double rate_of_small(View &v, int p, int cx, int cy, int cz) {
-  const Dev &d = *v.d;
-  const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
-  const int nb = r[0];
-  uint64_t nrp = 0;
-  const int32_t *b = r + 4;
-  for (int k = 0; k < nb; k++) {
-    const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
-    const int npairs = b[1];
-    for (int j = 0; j < npairs; j++)
-      if (sp == b[2 + 2 * j]) nrp += 1ull << (8 * b[3 + 2 * j]);
-    b += 2 + 2 * npairs;
-  }
-  const int32_t *code = b;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, result = 0.0;
-  for (int pc = 0;;) {
-    const uint32_t w = (uint32_t)code[pc++];
-    const int op = w & 0xFF, kind = (w >> 8) & 0xFF, arg = (int)(w >> 16);
-    double x;
-    switch (op) {
-      case I_END: return result;
-      case I_PUSH_BASE: x = d.rates[p - 1]; break;
-      case I_PUSH_PAR: x = d.userpar[arg]; break;
-      case I_PUSH_NR: x = (double)(int)((nrp >> (8 * arg)) & 0xFFu); break;
-      case I_PUSH_INT: x = (double)code[pc++]; break;
-      case I_PUSH_CONST: x = __hiloint2double(code[pc + 1], code[pc]); pc += 2; break;
-      case I_STORE_RESULT:
-        result = s0; s0 = s1; s1 = s2; s2 = s3;
-        continue;
-      case I_ADD: case I_SUB: case I_MUL: case I_DIV: case I_POWI: case I_POW:
-        s0 = rate_binary(op, kind, s1, s0); s1 = s2; s2 = s3;
-        continue;
-      case I_NEG: case I_EXP: case I_LOG: case I_SQRT: case I_ABS: case I_CVT:
-        s0 = rate_unary(op, kind, arg, s0);
-        continue;
-      default: v.err = ST_PROGRAM; return 0.0;
-    }
-    s3 = s2; s2 = s1; s1 = s0; s0 = x;  // a push
-  }
-}
-
 // gr_<p>(cell): bystander counts, then the rate program with base_rate = rates(p).
 __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
   const Dev &d = *v.d;
-  if (d.rate_small) return rate_of_small(v, p, cx, cy, cz);
   const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
   const int nb = r[0], nv = r[1];
   int32_t nr[OTF_NRMAX];
@@ -274,13 +192,41 @@ __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
       case I_LOAD_AUX: st[sp++] = aux[arg]; break;
       case I_STORE_AUX: aux[arg] = st[--sp]; break;
       case I_STORE_RESULT: result = st[--sp]; break;
-      case I_ADD: case I_SUB: case I_MUL: case I_DIV: case I_POWI: case I_POW: {
+      case I_ADD: case I_SUB: case I_MUL: case I_DIV: {
         const double b2 = st[--sp], a = st[sp - 1];
-        st[sp - 1] = rate_binary(op, kind, a, b2);
+        double r2;
+        if (kind == K_INT) {
+          const int32_t ia = (int32_t)a, ib = (int32_t)b2;
+          r2 = op == I_ADD ? (double)(int32_t)((uint32_t)ia + (uint32_t)ib)
+             : op == I_SUB ? (double)(int32_t)((uint32_t)ia - (uint32_t)ib)
+             : op == I_MUL ? (double)(int32_t)((uint32_t)ia * (uint32_t)ib)
+             : (ib == 0 ? 0.0 : (ib == -1 ? (double)(int32_t)(0u - (uint32_t)ia) : (double)(ia / ib)));
+        } else if (kind == K_F32) {
+          const float fa = (float)a, fb = (float)b2;
+          r2 = op == I_ADD ? __fadd_rn(fa, fb) : op == I_SUB ? __fsub_rn(fa, fb)
+             : op == I_MUL ? __fmul_rn(fa, fb) : __fdiv_rn(fa, fb);
+        } else {
+          r2 = op == I_ADD ? __dadd_rn(a, b2) : op == I_SUB ? __dsub_rn(a, b2)
+             : op == I_MUL ? __dmul_rn(a, b2) : __ddiv_rn(a, b2);
+        }
+        st[sp - 1] = r2;
         break;
       }
-      case I_NEG: case I_EXP: case I_LOG: case I_SQRT: case I_ABS: case I_CVT:
-        st[sp - 1] = rate_unary(op, kind, arg, st[sp - 1]);
+      case I_NEG:
+        st[sp - 1] = kind == K_INT ? (double)(int32_t)(0u - (uint32_t)(int32_t)st[sp - 1]) : -st[sp - 1];
+        break;
+      case I_POWI: { const double m = st[--sp]; st[sp - 1] = powi_kind(st[sp - 1], (int32_t)m, kind); break; }
+      case I_POW: {
+        const double b2 = st[--sp], a = st[sp - 1];
+        st[sp - 1] = kind == K_F32 ? (double)powf((float)a, (float)b2) : pow(a, b2);
+        break;
+      }
+      case I_EXP: st[sp - 1] = kind == K_F32 ? (double)expf((float)st[sp - 1]) : exp(st[sp - 1]); break;
+      case I_LOG: st[sp - 1] = kind == K_F32 ? (double)logf((float)st[sp - 1]) : log(st[sp - 1]); break;
+      case I_SQRT: st[sp - 1] = kind == K_F32 ? (double)__fsqrt_rn((float)st[sp - 1]) : __dsqrt_rn(st[sp - 1]); break;
+      case I_ABS: st[sp - 1] = fabs(st[sp - 1]); break;
+      case I_CVT:
+        if (kind == K_INT && arg == K_F32) st[sp - 1] = (double)(float)(int32_t)st[sp - 1];
         break;
       default: v.err = ST_PROGRAM; return 0.0;
     }
@@ -894,38 +840,6 @@ namespace {
 
 bool span_ok(int64_t off, int64_t len, int64_t total) { return off >= 0 && len >= 0 && off + len <= total; }
 
-// Whether every rate program of a (validated) otf program fits rate_of_small: stack depth
-// at most 4, at most 8 bystander variables over at most 255 sites, no auxiliary variables.
-int rates_fit_registers(const int32_t *w, int32_t len, int P, int off_rate) {
-  for (int p = 0; p < P; p++) {
-    const int pos = w[off_rate + p];
-    if (pos < 0 || pos + 4 > len) return 0;
-    const int nb = w[pos], nv = w[pos + 1], nc = w[pos + 2];
-    if (nb > 255 || nv > 8) return 0;
-    int q = pos + 4;
-    for (int k = 0; k < nb && q + 2 <= len; k++) q += 2 + 2 * w[q + 1];
-    if (q + nc > len) return 0;
-    int depth = 0;
-    for (int pc = q; pc < q + nc;) {
-      const uint32_t h = (uint32_t)w[pc++];
-      const int op = h & 0xFF;
-      switch (op) {
-        case otfdev::I_END: pc = q + nc; break;
-        case otfdev::I_PUSH_BASE: case otfdev::I_PUSH_PAR: case otfdev::I_PUSH_NR: depth++; break;
-        case otfdev::I_PUSH_INT: pc += 1; depth++; break;
-        case otfdev::I_PUSH_CONST: pc += 2; depth++; break;
-        case otfdev::I_LOAD_AUX: case otfdev::I_STORE_AUX: return 0;
-        case otfdev::I_STORE_RESULT: depth--; break;
-        case otfdev::I_ADD: case otfdev::I_SUB: case otfdev::I_MUL: case otfdev::I_DIV:
-        case otfdev::I_POWI: case otfdev::I_POW: depth--; break;
-        default: break;  // unary
-      }
-      if (depth > 4) return 0;
-    }
-  }
-  return 1;
-}
-
 // Simulates a rate program's stack on the host: every instruction known, every index in
 // range, depth within the device stack, exactly one final END.
 int check_code(const int32_t *c, int64_t len, int nvars, int nuser) {
@@ -1129,7 +1043,6 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   d.prog = dprog;
   d.prog_len = len;
   d.prog_staged = 0;
-  d.rate_small = rates_fit_registers(program, len, P, d.off_rate);
   d.lat = (int8_t *)(base + offs[1]);
   d.as1 = (int32_t *)(base + offs[2]); d.as2 = (int32_t *)(base + offs[3]);
   d.rm = (double *)(base + offs[4]); d.pm = (double *)(base + offs[5]);
