@@ -371,6 +371,14 @@ KMC_API int kmc_otf_run_proc_nr(kmc_otf *h, int32_t traj, int32_t proc, int32_t 
 KMC_API int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, int32_t *as2,
                               int32_t *nr_of_sites, int64_t *procstat, double *integ_rates, double *accum_rates,
                               double *rates_matrix, double *totals, double clock[2], int64_t *kmc_step);
+/* Rate tables (no reference counterpart; results are the same either way): a process's
+ * rate depends only on its bystander counts, so for models whose counts take at most
+ * 4096 combinations in all, each combination's rate is computed once by the process's
+ * rate program after the rates or user parameters change, and steps look it up.  on = 0
+ * evaluates every rate (gr_<name>, io:2800-2965) instead.  entries: the table size (0:
+ * the model has none). */
+KMC_API int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on);
+KMC_API int kmc_otf_rate_table_entries(kmc_otf *h, int32_t *entries);
 /* Device time of the last launch (CUDA events on the handle's stream) and launch count. */
 KMC_API int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms);
 KMC_API int kmc_otf_launch_count(kmc_otf *h, int64_t *n);

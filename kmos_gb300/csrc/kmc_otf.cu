@@ -72,8 +72,12 @@ struct Dev {
   const double *rates, *userpar;
   Traj *traj;
   unsigned long long *phase;  // OTF_NPHASE cycle sums (KMC_PHASE_TIMING builds)
-  int32_t prog_len;           // program words
-  int32_t prog_staged;        // 1: each block copies the program to shared memory
+  int32_t prog_len;           // words of the image: the program, then the rate tables
+  int32_t prog_staged;        // 1: each block copies the image to shared memory
+  int32_t tab_index;          // image word of the P table-record offsets (-1: no table)
+  int32_t tab_values;         // image word of the table values (doubles, 16-byte aligned)
+  int32_t tab_entries;        // table values
+  int32_t tab_on;             // 1: rate_of reads the tables
 };
 
 // Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
@@ -157,22 +161,9 @@ __device__ inline double powi_kind(double xd, int32_t m, int kind) {
   return (double)y;
 }
 
-// gr_<p>(cell): bystander counts, then the rate program with base_rate = rates(p).
-__device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
-  const Dev &d = *v.d;
-  const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
-  const int nb = r[0], nv = r[1];
-  int32_t nr[OTF_NRMAX];
-  for (int k = 0; k < nv; k++) nr[k] = 0;
-  const int32_t *b = r + 4;
-  for (int k = 0; k < nb; k++) {
-    const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
-    const int npairs = b[1];
-    for (int j = 0; j < npairs; j++)
-      if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
-    b += 2 + 2 * npairs;
-  }
-  const int32_t *code = b;
+// The rate program of process p (code) with base_rate = rates(p) and the bystander
+// counts nr: the body of gr_<p> (io:2800-2965) after its counting loop.
+__device__ double rate_program(const Dev &d, const int32_t *code, int p, const int32_t *nr, int &err) {
   double st[OTF_STACK], aux[OTF_AUX], result = 0.0;
   for (int k = 0; k < OTF_AUX; k++) aux[k] = 0.0;
   int sp = 0;
@@ -228,8 +219,84 @@ __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
       case I_CVT:
         if (kind == K_INT && arg == K_F32) st[sp - 1] = (double)(float)(int32_t)st[sp - 1];
         break;
-      default: v.err = ST_PROGRAM; return 0.0;
+      default: err = ST_PROGRAM; return 0.0;
     }
+  }
+}
+
+// The first word of process p's rate program (past its bystander list).
+__device__ inline const int32_t *rate_code(const int32_t *prog, const Dev &d, int p) {
+  const int32_t *r = prog + prog[d.off_rate + p - 1];
+  const int nb = r[0];
+  const int32_t *b = r + 4;
+  for (int k = 0; k < nb; k++) b += 2 + 2 * b[1];
+  return b;
+}
+
+// gr_<p>(cell).  With rate tables: a process's rate depends only on its bystander counts
+// (rates and user parameters are fixed between launches), so the counts select an entry
+// of the process's table, which otf_table_kernel filled with rate_program's value for
+// those counts -- the same double the program gives here.  The table index is the counts
+// in mixed radix: each bystander matching a pair adds the stride of that pair's
+// variable.  Otherwise the counts are taken and the program run.
+__device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
+  const Dev &d = *v.d;
+  if (d.tab_on) {
+    const int rec = v.prog[d.tab_index + p - 1];
+    if (rec >= 0) {
+      const int32_t *m = v.prog + rec;
+      const int nv = m[1];
+      const int nb = m[2 + nv];
+      const int32_t *b = m + 3 + nv;
+      int idx = m[0];
+      for (int k = 0; k < nb; k++) {
+        const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
+        const int npairs = b[1];
+        for (int j = 0; j < npairs; j++)
+          if (sp == b[2 + 2 * j]) idx += b[3 + 2 * j];
+        b += 2 + 2 * npairs;
+      }
+      return reinterpret_cast<const double *>(v.prog + d.tab_values)[idx];
+    }
+  }
+  const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
+  const int nb = r[0], nv = r[1];
+  int32_t nr[OTF_NRMAX];
+  for (int k = 0; k < nv; k++) nr[k] = 0;
+  const int32_t *b = r + 4;
+  for (int k = 0; k < nb; k++) {
+    const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
+    const int npairs = b[1];
+    for (int j = 0; j < npairs; j++)
+      if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
+    b += 2 + 2 * npairs;
+  }
+  return rate_program(d, b, p, nr, v.err);
+}
+
+// Fills the rate tables: thread e computes entry e -- the process whose table holds it,
+// the counts its index encodes (mixed radix, first variable fastest), the program's rate.
+__global__ void otf_table_kernel(Dev d, int32_t *img) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.tab_entries) return;
+  for (int p0 = 0; p0 < d.P; p0++) {
+    const int rec = img[d.tab_index + p0];
+    if (rec < 0) continue;
+    const int32_t *m = img + rec;
+    const int nv = m[1];
+    int size = 1;
+    for (int k = 0; k < nv; k++) size *= m[2 + k];
+    if (e < m[0] || e >= m[0] + size) continue;
+    int32_t nr[OTF_NRMAX];
+    int rem = e - m[0];
+    for (int k = 0; k < nv; k++) {
+      nr[k] = rem % m[2 + k];
+      rem /= m[2 + k];
+    }
+    int err = 0;
+    const double r = rate_program(d, rate_code(img, d, p0 + 1), p0 + 1, nr, err);
+    reinterpret_cast<double *>(img + d.tab_values)[e] = r;
+    return;
   }
 }
 
@@ -824,7 +891,8 @@ using otfdev::Traj;
 
 struct kmc_otf {
   cudaStream_t stream = nullptr;
-  std::vector<int32_t> prog;
+  std::vector<int32_t> prog;  // the image: the program, then the rate-table records
+  bool tab_stale = true;      // rates or user parameters changed since the tables were filled
   Dev d{};
   std::vector<double> rates, userpar;
   double *d_rates = nullptr, *d_userpar = nullptr;
@@ -944,6 +1012,65 @@ int validate_otf(const int32_t *w, int32_t len) {
   return KMC_OK;
 }
 
+constexpr int64_t OTF_TABLE_MAX = 4096;  // table entries of one model (32 KB of doubles)
+
+// Appends the rate-table records to a checked program: for each process whose counts
+// take at most OTF_TABLE_MAX combinations in all, the record [first entry, nv,
+// radix(nv), nb, then per bystander: coordinate, npairs, (species, stride of the
+// variable) x npairs], where radix(k) = 1 + the pairs counting into variable k (the
+// most it can reach) and stride(k) = radix(0) ... radix(k - 1).  The index array of the
+// P record offsets (-1: no table) follows the program; the values follow the records.
+void build_image(const int32_t *w, int32_t len, std::vector<int32_t> &img, Dev &d) {
+  const int P = w[3];
+  const int64_t off_rate = w[22];
+  img.assign(w, w + len);
+  img.resize(align_up((size_t)len, 2), 0);
+  d.tab_index = (int32_t)img.size();
+  img.resize(img.size() + P, -1);
+  int64_t entries = 0;
+  for (int p = 0; p < P; p++) {
+    const int64_t r = w[off_rate + p];
+    const int nb = w[r], nv = w[r + 1];
+    std::vector<int64_t> radix(nv, 1);
+    int64_t pos = r + 4;
+    for (int k = 0; k < nb; k++) {
+      const int np = w[pos + 1];
+      for (int j = 0; j < np; j++) radix[w[pos + 3 + 2 * j]] += 1;
+      pos += 2 + 2 * (int64_t)np;
+    }
+    int64_t size = 1;
+    std::vector<int64_t> stride(nv);
+    for (int k = 0; k < nv && size <= OTF_TABLE_MAX; k++) {
+      stride[k] = size;
+      size *= radix[k];
+    }
+    if (size > OTF_TABLE_MAX || entries + size > OTF_TABLE_MAX) continue;
+    img[d.tab_index + p] = (int32_t)img.size();
+    img.push_back((int32_t)entries);
+    img.push_back(nv);
+    for (int k = 0; k < nv; k++) img.push_back((int32_t)radix[k]);
+    img.push_back(nb);
+    pos = r + 4;
+    for (int k = 0; k < nb; k++) {
+      const int np = w[pos + 1];
+      img.push_back(w[pos]);
+      img.push_back(np);
+      for (int j = 0; j < np; j++) {
+        img.push_back(w[pos + 2 + 2 * j]);
+        img.push_back((int32_t)stride[w[pos + 3 + 2 * j]]);
+      }
+      pos += 2 + 2 * (int64_t)np;
+    }
+    entries += size;
+  }
+  d.tab_entries = (int32_t)entries;
+  img.resize(align_up(img.size(), 4), 0);
+  d.tab_values = (int32_t)img.size();
+  img.resize(img.size() + 2 * (size_t)entries, 0);
+  d.tab_on = entries > 0 ? 1 : 0;
+  if (!entries) d.tab_index = -1;
+}
+
 int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
   const int blocks = only >= 0 ? 1 : (h->d.T + otfdev::OTF_WARPS - 1) / otfdev::OTF_WARPS;
   Dev d = h->d;
@@ -969,6 +1096,11 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     if (d.prog_staged) dyn = want;
     if (dyn > 0 && fa.maxDynamicSharedSizeBytes < (int)dyn)
       CK(cudaFuncSetAttribute(otfdev::otf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+  }
+  if (h->d.tab_entries > 0 && h->tab_stale) {
+    otfdev::otf_table_kernel<<<(h->d.tab_entries + 127) / 128, 128, 0, h->stream>>>(h->d, const_cast<int32_t *>(h->d.prog));
+    CK(cudaGetLastError());
+    h->tab_stale = false;
   }
   CK(cudaEventRecord(h->ev0, h->stream));
   otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, dyn, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
@@ -1016,15 +1148,16 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(KMC_ERR_NODEVICE, "no CUDA device");
   kmc_otf *h = new kmc_otf();
-  h->prog.assign(program, program + len);
   const int P = program[3], T = ntraj;
   Dev &d = h->d;
+  build_image(program, len, h->prog, d);
+  const int32_t img_len = (int32_t)h->prog.size();
   d.P = P; d.nspecies = program[4]; d.null_species = program[5]; d.spuck = program[6];
   d.nuser = program[23]; d.off_proc = program[10]; d.off_touch = program[11]; d.off_rate = program[22];
   d.off_site_layer = program[13]; d.off_site_default = program[14];
   d.X = dims[0]; d.Y = dims[1]; d.Z = dims[2]; d.V = (int)V; d.T = T;
   const size_t PV = (size_t)P * (V + 1), TP = (size_t)T * P;
-  const size_t sizes[] = {(size_t)len * 4, (size_t)T * V, T * PV * 4, T * PV * 4, T * PV * 8, T * PV * 8,
+  const size_t sizes[] = {(size_t)img_len * 4, (size_t)T * V, T * PV * 4, T * PV * 4, T * PV * 8, T * PV * 8,
                           TP * 4, TP * 4, TP * 8, TP * 8, TP * 8, TP * 8, (size_t)T * sizeof(Traj),
                           (size_t)P * 8, (size_t)(d.nuser > 0 ? d.nuser : 1) * 8,
                           (size_t)otfdev::OTF_NPHASE * 8};
@@ -1041,7 +1174,7 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   char *base = (char *)h->mem;
   int32_t *dprog = (int32_t *)(base + offs[0]);
   d.prog = dprog;
-  d.prog_len = len;
+  d.prog_len = img_len;
   d.prog_staged = 0;
   d.lat = (int8_t *)(base + offs[1]);
   d.as1 = (int32_t *)(base + offs[2]); d.as2 = (int32_t *)(base + offs[3]);
@@ -1061,7 +1194,7 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
     tr[t].seed = (uint32_t)seed; tr[t].traj = traj0 + (uint32_t)t; tr[t].rng_kind = rng_kind;
     if (rng_kind == RNG_GFORTRAN) gfortran_seed(tr[t].rng, seed);
   }
-  if (cudaMemcpyAsync(dprog, program, (size_t)len * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+  if (cudaMemcpyAsync(dprog, h->prog.data(), (size_t)img_len * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
       cudaMemcpyAsync(d.traj, tr.data(), (size_t)T * sizeof(Traj), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
     return cleanup(fail(KMC_ERR_CUDA, "upload"));
   std::vector<int32_t> dirty(TP, 0x7FFFFFFF);
@@ -1093,6 +1226,7 @@ int kmc_otf_destroy(kmc_otf *h) {
 int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate) {
   if (!h || proc < 1 || proc > h->d.P) return fail(KMC_ERR_ARG, "bad process");
   h->rates[proc - 1] = rate;
+  h->tab_stale = true;
   CK(cudaMemcpyAsync(h->d_rates, h->rates.data(), h->rates.size() * 8, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return KMC_OK;
@@ -1101,6 +1235,7 @@ int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate) {
 int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value) {
   if (!h || k < 1 || k > h->d.nuser) return fail(KMC_ERR_ARG, "bad user parameter");
   h->userpar[k - 1] = value;
+  h->tab_stale = true;
   CK(cudaMemcpyAsync(h->d_userpar, h->userpar.data(), h->userpar.size() * 8, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return KMC_OK;
@@ -1204,6 +1339,18 @@ int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, 
     if (clock) { clock[0] = tr.kmc_time; clock[1] = tr.kmc_time_step; }
     if (kmc_step) *kmc_step = tr.kmc_step;
   }
+  return KMC_OK;
+}
+
+int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on) {
+  if (!h) return fail(KMC_ERR_ARG, "bad handle");
+  h->d.tab_on = on && h->d.tab_entries > 0 ? 1 : 0;
+  return KMC_OK;
+}
+
+int kmc_otf_rate_table_entries(kmc_otf *h, int32_t *entries) {
+  if (!h || !entries) return fail(KMC_ERR_ARG, "bad arguments");
+  *entries = h->d.tab_entries;
   return KMC_OK;
 }
 

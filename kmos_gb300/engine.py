@@ -129,6 +129,8 @@ SIGNATURES = {
     "kmc_otf_last_kernel_ms": (_i32, [_vp, _P(ctypes.c_float)]),
     "kmc_otf_launch_count": (_i32, [_vp, _p64]),
     "kmc_otf_phase_cycles": (_i32, [_vp, ctypes.POINTER(ctypes.c_uint64), _i32]),
+    "kmc_otf_set_rate_tables": (_i32, [_vp, _i32]),
+    "kmc_otf_rate_table_entries": (_i32, [_vp, _p32]),
 }
 
 _lib = None
@@ -783,6 +785,16 @@ class OtfBatch:
     def launch_count(self) -> int:
         n = _i64()
         _check(load().kmc_otf_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def set_rate_tables(self, on: bool) -> None:
+        """Rates looked up in per-process tables of every bystander-count combination
+        (the default where the model has them) or evaluated by the rate programs."""
+        _check(load().kmc_otf_set_rate_tables(self.h, 1 if on else 0))
+
+    def rate_table_entries(self) -> int:
+        n = ctypes.c_int32()
+        _check(load().kmc_otf_rate_table_entries(self.h, ctypes.byref(n)))
         return n.value
 
     def phase_cycles(self, reset: bool = True) -> np.ndarray:

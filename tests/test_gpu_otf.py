@@ -164,3 +164,43 @@ def test_dropin_module_otf_build():
         assert base.get_rate(p) == tot[p - 1]
     np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
     lattice.deallocate_system()
+
+
+def _states_equal(a, b, t):
+    ga, gb = a.state(t), b.state(t)
+    for k in ga:
+        np.testing.assert_array_equal(np.asarray(ga[k]), np.asarray(gb[k]), err_msg=k)
+
+
+def test_rate_tables_give_the_programs_rates():
+    """Rates looked up in the per-process tables equal the rate programs' own values bit for
+    bit: two batches, tables on and off, same trajectories, including a rate-constant and a
+    user-parameter change between launches (the tables are refilled) and exp / sqrt / aux
+    rate expressions."""
+    m = fixture_model("intZGB_otf")
+    m.processes[0].otf_rate = "e = J_O_CO*nr_O_1nn + 0.5*J_CO_CO*nr_CO_1nn\notf_rate = base_rate*exp(-e)"
+    m.processes[8].otf_rate = "base_rate*sqrt(1.0d0 + nr_O_1nn)/(1 + nr_CO_1nn)"
+    prog = PG.compile_model(m, "otf")
+    batches = []
+    for on in (True, False):
+        b = E.OtfBatch(prog, (14, 12), ntraj=5, seed=3, traj0=2)
+        b.set_rate_tables(on)
+        b.set_rates(INTZGB_RATES)
+        b.set_user_parameters(INTZGB_PARAMS)
+        b.recalculate_rates_matrix()
+        b.update_accum_rate()
+        b.update_integ_rate()
+        batches.append(b)
+    on, off = batches
+    assert on.rate_table_entries() == 25 + 1 + 4 * 256 + 2 + 2 * 49
+    for block, change in ((500, None), (700, "rate"), (900, "param")):
+        for b in batches:
+            if change == "rate":
+                b.set_rates([r * 1.7 for r in INTZGB_RATES])
+                b.recalculate_rates_matrix()
+            elif change == "param":
+                b.set_user_parameters([p * 0.9 for p in INTZGB_PARAMS])
+                b.recalculate_rates_matrix()
+            b.do_kmc_steps(block)
+        for t in range(5):
+            _states_equal(on, off, t)
