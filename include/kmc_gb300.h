@@ -378,6 +378,14 @@ KMC_API int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_
  * evaluates every rate (gr_<name>, io:2800-2965) instead.  entries: the table size (0:
  * the model has none). */
 KMC_API int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on);
+/* Constant-rate running sums (no reference counterpart; results are the same either
+ * way): every entry of a process whose rate program reads no bystander count holds the
+ * same rate c once recalculate_rates_matrix has run, so the running sums of its list
+ * (update_accum_rate, base_otf.f90:687-716) are fl(pm(i-1) + c) from 0 -- one table per
+ * process, filled after the rates or user parameters change, replaces re-summing the
+ * list.  Used between recalculate_rates_matrix and the next rate or parameter change,
+ * for lattices of up to 65536 sites; on = 0 always sums the lists. */
+KMC_API int kmc_otf_set_constant_rate_sums(kmc_otf *h, int32_t on);
 KMC_API int kmc_otf_rate_table_entries(kmc_otf *h, int32_t *entries);
 /* Device time of the last launch (CUDA events on the handle's stream) and launch count. */
 KMC_API int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms);

@@ -78,6 +78,9 @@ struct Dev {
   int32_t tab_values;         // image word of the table values (doubles, 16-byte aligned)
   int32_t tab_entries;        // table values
   int32_t tab_on;             // 1: rate_of reads the tables
+  int32_t uni_index;          // image word of the P constant-rate row numbers (-1: none)
+  int32_t uni_on;             // 1: constant-rate processes' running sums come from usum
+  double *usum;               // per constant-rate process: its running sums of 0..V entries
 };
 
 // Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
@@ -297,6 +300,28 @@ __global__ void otf_table_kernel(Dev d, int32_t *img) {
     const double r = rate_program(d, rate_code(img, d, p0 + 1), p0 + 1, nr, err);
     reinterpret_cast<double *>(img + d.tab_values)[e] = r;
     return;
+  }
+}
+
+// A process whose rate program reads no bystander count gives every list entry the same
+// rate c, so while every entry holds the current c its running sums are
+// pm(i) = fl(pm(i-1) + c) from pm(0) = 0: the same numbers for every trajectory and step.
+// Row r of usum holds them for i = 0..V, filled here (one thread per such process) when
+// the rates or user parameters change.
+__global__ void otf_uniform_kernel(Dev d, const int32_t *img) {
+  const int p0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p0 >= d.P || d.uni_index < 0) return;
+  const int row = img[d.uni_index + p0];
+  if (row < 0) return;
+  const int32_t none[1] = {0};
+  int err = 0;
+  const double c = rate_program(d, rate_code(img, d, p0 + 1), p0 + 1, none, err);
+  double *u = d.usum + (size_t)row * (d.V + 1);
+  double s = 0.0;
+  u[0] = 0.0;
+  for (int i = 1; i <= d.V; i++) {
+    s = __dadd_rn(s, c);
+    u[i] = s;
   }
 }
 
@@ -638,14 +663,34 @@ __device__ inline int interval_search(const double *arr, int size, double value)
   return mid;
 }
 
+// The running sums of process p0's list (1-based): its usum row while the constant-rate
+// sums hold (see otf_uniform_kernel), else the list's own pm row.
+__device__ inline const double *sums_of(const View &v, int p0) {
+  const Dev &d = *v.d;
+  if (d.uni_on) {
+    const int row = v.prog[d.uni_index + p0];
+    if (row >= 0) return d.usum + (size_t)row * (d.V + 1);
+  }
+  return v.pm + v.row(p0);
+}
+
 // update_accum_rate: stale running sums re-summed (lanes: processes), then the totals
-// chained into accum_rates on lane 0.  sacc is the warp's accum_rates (1-based).
+// chained into accum_rates on lane 0.  sacc is the warp's accum_rates (1-based).  A
+// constant-rate process's total is read from its usum row; its pm row is left stale,
+// with dirty still marking the first entry changed since it was last summed.
 __device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
   const int P = v.d->P;
   for (int p0 = lane; p0 < P; p0 += 32) {
     const int n = v.ns[p0];
-    const int lo = v.dirty[p0];
+    const double *us = sums_of(v, p0);
     double *pm = v.pm + v.row(p0);
+    if (us != pm) {
+      const double t = n > 0 ? us[n] : 0.0;
+      stot[p0] = t;
+      v.tot[p0] = t;
+      continue;
+    }
+    const int lo = v.dirty[p0];
     if (lo <= n) {
       // the chain is serial; its loads are not: 16 entries are fetched before their adds
       const double *rm = v.rm + v.row(p0);
@@ -751,7 +796,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
       int site = 0;
       if (proc) {
         const int nn = v.ns[proc - 1];
-        const double *pm = v.pm + v.row(proc - 1);
+        const double *pm = sums_of(v, proc - 1);
         const int k = nn > 0 ? interval_search(pm, nn, __dmul_rn(r0, pm[nn])) : 0;
         site = k ? v.as1[v.row(proc - 1) + k] : 0;
       }
@@ -835,7 +880,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
       if (!proc || nn <= 0) {
         err = ST_DEADLOCK;
       } else {
-        const double *pm = v.pm + v.row(proc - 1);
+        const double *pm = sums_of(v, proc - 1);
         const int k = interval_search(pm, nn, __dmul_rn(r2, pm[nn]));
         if (!k) {
           err = ST_DEADLOCK;
@@ -893,6 +938,9 @@ struct kmc_otf {
   cudaStream_t stream = nullptr;
   std::vector<int32_t> prog;  // the image: the program, then the rate-table records
   bool tab_stale = true;      // rates or user parameters changed since the tables were filled
+  bool uni_ok = true;         // every entry of a constant-rate process holds the current rate
+  bool uni_enabled = true;    // kmc_otf_set_constant_rate_sums
+  int uni_rows = 0;           // constant-rate processes
   Dev d{};
   std::vector<double> rates, userpar;
   double *d_rates = nullptr, *d_userpar = nullptr;
@@ -1019,8 +1067,9 @@ constexpr int64_t OTF_TABLE_MAX = 4096;  // table entries of one model (32 KB of
 // radix(nv), nb, then per bystander: coordinate, npairs, (species, stride of the
 // variable) x npairs], where radix(k) = 1 + the pairs counting into variable k (the
 // most it can reach) and stride(k) = radix(0) ... radix(k - 1).  The index array of the
-// P record offsets (-1: no table) follows the program; the values follow the records.
-void build_image(const int32_t *w, int32_t len, std::vector<int32_t> &img, Dev &d) {
+// P record offsets (-1: no table) follows the program; then the records, the P usum row
+// numbers of the constant-rate processes (-1: not one), and the values.
+void build_image(const int32_t *w, int32_t len, std::vector<int32_t> &img, Dev &d, int &uni_rows) {
   const int P = w[3];
   const int64_t off_rate = w[22];
   img.assign(w, w + len);
@@ -1064,6 +1113,14 @@ void build_image(const int32_t *w, int32_t len, std::vector<int32_t> &img, Dev &
     entries += size;
   }
   d.tab_entries = (int32_t)entries;
+  // the constant-rate processes (rate programs reading no count): their usum rows
+  d.uni_index = (int32_t)img.size();
+  img.resize(img.size() + P, -1);
+  int rows = 0;
+  for (int p = 0; p < P; p++)
+    if (w[w[off_rate + p] + 1] == 0) img[d.uni_index + p] = rows++;
+  if (!rows) d.uni_index = -1;
+  uni_rows = rows;
   img.resize(align_up(img.size(), 4), 0);
   d.tab_values = (int32_t)img.size();
   img.resize(img.size() + 2 * (size_t)entries, 0);
@@ -1097,11 +1154,20 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     if (dyn > 0 && fa.maxDynamicSharedSizeBytes < (int)dyn)
       CK(cudaFuncSetAttribute(otfdev::otf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   }
-  if (h->d.tab_entries > 0 && h->tab_stale) {
-    otfdev::otf_table_kernel<<<(h->d.tab_entries + 127) / 128, 128, 0, h->stream>>>(h->d, const_cast<int32_t *>(h->d.prog));
-    CK(cudaGetLastError());
+  if (h->tab_stale) {
+    if (h->d.tab_entries > 0) {
+      otfdev::otf_table_kernel<<<(h->d.tab_entries + 127) / 128, 128, 0, h->stream>>>(h->d, const_cast<int32_t *>(h->d.prog));
+      CK(cudaGetLastError());
+    }
+    if (h->d.uni_index >= 0) {
+      otfdev::otf_uniform_kernel<<<(h->d.P + 31) / 32, 32, 0, h->stream>>>(h->d, h->d.prog);
+      CK(cudaGetLastError());
+    }
     h->tab_stale = false;
   }
+  // recalculate_rates_matrix gives every entry the current rate before it sums
+  if (cmd == 6) h->uni_ok = true;
+  d.uni_on = h->uni_enabled && h->uni_ok && d.uni_index >= 0 ? 1 : 0;
   CK(cudaEventRecord(h->ev0, h->stream));
   otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, dyn, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
   CK(cudaGetLastError());
@@ -1150,19 +1216,23 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   kmc_otf *h = new kmc_otf();
   const int P = program[3], T = ntraj;
   Dev &d = h->d;
-  build_image(program, len, h->prog, d);
+  build_image(program, len, h->prog, d, h->uni_rows);
   const int32_t img_len = (int32_t)h->prog.size();
   d.P = P; d.nspecies = program[4]; d.null_species = program[5]; d.spuck = program[6];
   d.nuser = program[23]; d.off_proc = program[10]; d.off_touch = program[11]; d.off_rate = program[22];
   d.off_site_layer = program[13]; d.off_site_default = program[14];
   d.X = dims[0]; d.Y = dims[1]; d.Z = dims[2]; d.V = (int)V; d.T = T;
   const size_t PV = (size_t)P * (V + 1), TP = (size_t)T * P;
+  // constant-rate running sums for lattices of up to 65536 sites (512 KB per process)
+  const bool use_usum = h->uni_rows > 0 && V <= 65536;
+  if (!use_usum) d.uni_index = -1;
   const size_t sizes[] = {(size_t)img_len * 4, (size_t)T * V, T * PV * 4, T * PV * 4, T * PV * 8, T * PV * 8,
                           TP * 4, TP * 4, TP * 8, TP * 8, TP * 8, TP * 8, (size_t)T * sizeof(Traj),
                           (size_t)P * 8, (size_t)(d.nuser > 0 ? d.nuser : 1) * 8,
-                          (size_t)otfdev::OTF_NPHASE * 8};
-  size_t offs[16], total = 0;
-  for (int i = 0; i < 16; i++) { offs[i] = total; total = align_up(total + sizes[i], 256); }
+                          (size_t)otfdev::OTF_NPHASE * 8,
+                          use_usum ? (size_t)h->uni_rows * (V + 1) * 8 : 0};
+  size_t offs[17], total = 0;
+  for (int i = 0; i < 17; i++) { offs[i] = total; total = align_up(total + sizes[i], 256); }
   auto cleanup = [&](int code) { if (h->mem) cudaFree(h->mem); if (h->stream) cudaStreamDestroy(h->stream);
                                  if (h->ev0) cudaEventDestroy(h->ev0); if (h->ev1) cudaEventDestroy(h->ev1);
                                  delete h; return code; };
@@ -1186,6 +1256,8 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   h->d_rates = (double *)(base + offs[13]); h->d_userpar = (double *)(base + offs[14]);
   d.rates = h->d_rates; d.userpar = h->d_userpar;
   d.phase = (unsigned long long *)(base + offs[15]);
+  d.usum = use_usum ? (double *)(base + offs[16]) : nullptr;
+  d.uni_on = 0;
   h->rates.assign(P, 0.0);
   h->userpar.assign(d.nuser, 0.0);
   std::vector<Traj> tr(T);
@@ -1227,6 +1299,7 @@ int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate) {
   if (!h || proc < 1 || proc > h->d.P) return fail(KMC_ERR_ARG, "bad process");
   h->rates[proc - 1] = rate;
   h->tab_stale = true;
+  h->uni_ok = false;
   CK(cudaMemcpyAsync(h->d_rates, h->rates.data(), h->rates.size() * 8, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return KMC_OK;
@@ -1236,6 +1309,7 @@ int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value) {
   if (!h || k < 1 || k > h->d.nuser) return fail(KMC_ERR_ARG, "bad user parameter");
   h->userpar[k - 1] = value;
   h->tab_stale = true;
+  h->uni_ok = false;
   CK(cudaMemcpyAsync(h->d_userpar, h->userpar.data(), h->userpar.size() * 8, cudaMemcpyHostToDevice, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return KMC_OK;
@@ -1345,6 +1419,12 @@ int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, 
 int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on) {
   if (!h) return fail(KMC_ERR_ARG, "bad handle");
   h->d.tab_on = on && h->d.tab_entries > 0 ? 1 : 0;
+  return KMC_OK;
+}
+
+int kmc_otf_set_constant_rate_sums(kmc_otf *h, int32_t on) {
+  if (!h) return fail(KMC_ERR_ARG, "bad handle");
+  h->uni_enabled = on != 0;
   return KMC_OK;
 }
 

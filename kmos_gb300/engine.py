@@ -130,6 +130,7 @@ SIGNATURES = {
     "kmc_otf_launch_count": (_i32, [_vp, _p64]),
     "kmc_otf_phase_cycles": (_i32, [_vp, ctypes.POINTER(ctypes.c_uint64), _i32]),
     "kmc_otf_set_rate_tables": (_i32, [_vp, _i32]),
+    "kmc_otf_set_constant_rate_sums": (_i32, [_vp, _i32]),
     "kmc_otf_rate_table_entries": (_i32, [_vp, _p32]),
 }
 
@@ -791,6 +792,11 @@ class OtfBatch:
         """Rates looked up in per-process tables of every bystander-count combination
         (the default where the model has them) or evaluated by the rate programs."""
         _check(load().kmc_otf_set_rate_tables(self.h, 1 if on else 0))
+
+    def set_constant_rate_sums(self, on: bool) -> None:
+        """Running sums of constant-rate processes' lists from per-process tables (the
+        default) or always re-summed."""
+        _check(load().kmc_otf_set_constant_rate_sums(self.h, 1 if on else 0))
 
     def rate_table_entries(self) -> int:
         n = ctypes.c_int32()

@@ -204,3 +204,40 @@ def test_rate_tables_give_the_programs_rates():
             b.do_kmc_steps(block)
         for t in range(5):
             _states_equal(on, off, t)
+
+
+def test_constant_rate_sums_equal_summed_lists():
+    """Constant-rate processes' running sums read from their tables equal the re-summed
+    lists bit for bit (every state field, and so every later pick): two batches with the
+    tables on and off; between launches a rate change without recalculate_rates_matrix
+    (old and new rates mixed in one list, so the lists are summed from their first
+    change), then recalculate_rates_matrix (tables again), a user-parameter change, and
+    the picks of get_next_kmc_step and a trace."""
+    m = fixture_model("intZGB_otf")
+    prog = PG.compile_model(m, "otf")
+    batches = []
+    for on in (True, False):
+        b = E.OtfBatch(prog, (20, 18), ntraj=4, seed=9, traj0=1)
+        b.set_constant_rate_sums(on)
+        b.set_rates(INTZGB_RATES)
+        b.set_user_parameters(INTZGB_PARAMS)
+        b.recalculate_rates_matrix()
+        b.update_accum_rate()
+        b.update_integ_rate()
+        batches.append(b)
+    on, off = batches
+    steps = [(400, None), (300, "rate"), (300, "recalc"), (500, "param"), (200, "recalc")]
+    for block, change in steps:
+        for b in batches:
+            if change == "rate":
+                b.set_rates([r * (1.3 if p in (1, 6, 7) else 1.0) for p, r in enumerate(INTZGB_RATES)])
+            elif change == "param":
+                b.set_user_parameters([p * 1.1 for p in INTZGB_PARAMS])
+            elif change == "recalc":
+                b.recalculate_rates_matrix()
+            b.do_kmc_steps(block)
+        for t in range(4):
+            _states_equal(on, off, t)
+    assert on.get_next_kmc_step(2) == off.get_next_kmc_step(2)
+    np.testing.assert_array_equal(on.trace(3, 300), off.trace(3, 300))
+    _states_equal(on, off, 3)
