@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--otf-only", type=int, default=0,
                     help="run only the otf sample (--otf-ntraj trajectories, --otf-steps timed steps) and print it")
     ap.add_argument("--otf-ntraj", type=int, default=2048)
-    ap.add_argument("--otf-steps", type=int, default=0, help="timed otf steps per trajectory (0: about 1.5 s)")
+    ap.add_argument("--otf-steps", type=int, default=0, help="timed otf steps per trajectory (0: OTF_TIMED)")
     ap.add_argument("--serving", type=int, default=1,
                     help="also run a short serving sample (configuration 5 stream, 1 s of arrivals, steps x 0.05)")
     return ap.parse_args()
@@ -275,33 +275,45 @@ def _otf_model_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "models", "intZGB_otf.json")
 
 
+OTF_WARM = 5000     # untimed otf steps per trajectory (the lattice fills from empty)
+OTF_TIMED = 20000   # timed otf steps per trajectory, GPU and CPU alike
+OTF_CPU_PER_CORE = 24
+
+
 def _otf_cpu_worker(args):
-    traj, steps = args
+    trajs, warm, steps = args
     from kmos_gb300 import model as M, program as PG
     from oracle import oracle as O
     prog = PG.compile_model(M.load_json(_otf_model_path()), "otf")
-    o = O.Oracle(prog, (32, 32), seed=11, rng=O.RNG_PHILOX, traj=traj)
-    o.set_rates(OTF_RATES)
-    o.set_user_parameters(OTF_PARAMS)
-    o.recalculate_rates_matrix()
-    o.update_accum_rate()
-    o.do_kmc_steps(300)
-    t0 = time.perf_counter()
-    o.do_kmc_steps(steps)
-    return steps, time.perf_counter() - t0
+    busy = 0.0
+    for traj in trajs:
+        o = O.Oracle(prog, (32, 32), seed=11, rng=O.RNG_PHILOX, traj=traj)
+        o.set_rates(OTF_RATES)
+        o.set_user_parameters(OTF_PARAMS)
+        o.recalculate_rates_matrix()
+        o.update_accum_rate()
+        o.do_kmc_steps(warm)
+        t0 = time.perf_counter()
+        o.do_kmc_steps(steps)
+        busy += time.perf_counter() - t0
+    return steps * len(trajs), busy
 
 
-def otf_cpu_sample(steps: int = 800_000):
-    """The oracle's otf backend on all host cores, one intZGB trajectory (32 x 32) per
-    core process: (aggregate steps/s, cores, sample)."""
+def otf_cpu_sample(warm: int = OTF_WARM, steps: int = OTF_TIMED, per_core: int = OTF_CPU_PER_CORE):
+    """The oracle's otf backend on all host cores over the GPU sample's window: trajectories
+    0 .. cores*per_core-1 of the GPU batch (same seed and Philox ids), each ``warm``
+    untimed then ``steps`` timed steps, ``per_core`` trajectories in turn per core
+    process: (aggregate steps/s, cores, sample)."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
+    work = [(list(range(c * per_core, (c + 1) * per_core)), warm, steps) for c in range(cores)]
     with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_otf_cpu_worker, [(i, steps) for i in range(cores)])
-    wall = max(t for _, t in res)
-    sample = "%d trajectories x %d otf steps (intZGB 32x32), one process per core" % (cores, steps)
-    return sum(s for s, _ in res) / wall, cores, sample
+        res = pool.map(_otf_cpu_worker, work)
+    busy = max(t for _, t in res)
+    sample = ("%d trajectories (intZGB 32x32, ids 0-%d of the GPU batch), each %d untimed then %d timed otf steps, "
+              "%d in turn per core process" % (cores * per_core, cores * per_core - 1, warm, steps, per_core))
+    return sum(s for s, _ in res) / busy, cores, sample
 
 
 def replica_trajs(trajs, rank: int):
@@ -558,9 +570,10 @@ def serving_sample():
 def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
     """The otf backend (per-entry rates from bystanders) after the timed region: intZGB
     (tests/golden/models/intZGB_otf.json, the reference's tests/export_test/intZGB_otf.xml)
-    on a 32 x 32 lattice, 2048 Philox trajectories, steps/s over every trajectory from
-    CUDA events around one do_kmc_steps launch (inputs resident), beside the oracle's
-    otf backend on every host core (one trajectory of the same configuration each)."""
+    on a 32 x 32 lattice, 2048 Philox trajectories from an empty lattice: OTF_WARM
+    untimed steps, then steps/s over every trajectory from CUDA events around one
+    do_kmc_steps launch of OTF_TIMED steps (inputs resident), beside the oracle's otf
+    backend on every host core over the same window of the same trajectories."""
     from kmos_gb300 import engine as E, model as M, otf as OTF, program as PG
     m = M.load_json(_otf_model_path())
     prog = PG.compile_model(m, "otf")
@@ -571,21 +584,18 @@ def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
     b.set_user_parameters(params)
     b.recalculate_rates_matrix()
     b.update_accum_rate()
-    b.do_kmc_steps(300)                       # warm-up: tables leave the initial state
-    if fixed_steps:
-        steps = fixed_steps
-    else:
-        b.do_kmc_steps(100)
-        ms100 = b.last_kernel_ms()
-        steps = max(100, min(20000, int(100 * 1500.0 / max(ms100, 1e-3))))
+    b.do_kmc_steps(OTF_WARM)                  # untimed: the lattice fills from empty
+    steps = fixed_steps or OTF_TIMED
     b.do_kmc_steps(steps)
     ms = b.last_kernel_ms()
-    out = {"workload": "intZGB otf, 32x32, %d trajectories" % ntraj, "steps_per_traj": steps,
-           "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1}
+    out = {"workload": "intZGB otf, 32x32, %d trajectories" % ntraj, "window": [OTF_WARM, OTF_WARM + steps],
+           "steps_per_traj": steps, "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1,
+           "rate_table_entries": b.rate_table_entries()}
     b.close()
     if cpu:
-        value, cores, sample = otf_cpu_sample()
+        value, cores, sample = otf_cpu_sample(OTF_WARM, steps)
         out["cpu_baseline"] = {"value": value, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample}
+        out["speedup_vs_cpu"] = out["steps_per_s"] / value
     return out
 
 

@@ -371,6 +371,33 @@ KMC_API int kmc_otf_run_proc_nr(kmc_otf *h, int32_t traj, int32_t proc, int32_t 
 KMC_API int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, int32_t *as2,
                               int32_t *nr_of_sites, int64_t *procstat, double *integ_rates, double *accum_rates,
                               double *rates_matrix, double *totals, double clock[2], int64_t *kmc_step);
+/* base.set_kmc_time (base_otf.f90:968-982) of one trajectory. */
+KMC_API int kmc_otf_set_kmc_time(kmc_otf *h, int32_t traj, double kmc_time);
+/* base.replace_species (base_otf.f90:1344-1383): KMC_ERR_SPECIES unless the site holds
+ * old_species; the tables are not touched (kmos.run's put then touches up every cell). */
+KMC_API int kmc_otf_replace_species(kmc_otf *h, int32_t traj, int32_t site, int32_t old_species,
+                                    int32_t new_species);
+/* proclist.touchup_cell (io:3240-3284) of n cells, cells[3i..3i+2] = (x, y, z), in the
+ * given order (kmos.run's _adjust_database runs x outermost, run/__init__.py:1439-1457),
+ * one launch. */
+KMC_API int kmc_otf_touchup_cells(kmc_otf *h, int32_t traj, int32_t n, const int32_t *cells);
+/* A trajectory's state from the host, as reload_system restores it (base_otf.f90:448-599):
+ * lattice[V], avail_sites(:, :, 1) as as1[P][V+1] (entry 0 unused; column 2 is rebuilt as
+ * its inverse), nr_of_sites[P], procstat[P], integ_rates[P] (NULL: zero), clock =
+ * {kmc_time, kmc_time_step}, kmc_step.  rates_matrix is zero, as the reference's file does
+ * not hold it, until kmc_otf_recalculate_rates_matrix.  KMC_ERR_ARG / KMC_ERR_TABLE for a
+ * species out of range or a list that names a site twice. */
+KMC_API int kmc_otf_set_state(kmc_otf *h, int32_t traj, const int32_t *lattice, const int32_t *as1,
+                              const int32_t *nr_of_sites, const int64_t *procstat, const double *integ_rates,
+                              const double clock[2], int64_t kmc_step);
+/* base.save_system / reload_system of one trajectory (base_otf.f90:448-663): the
+ * reference's .reload layout with the same "#gb300" comment lines kmc_save_reload writes
+ * (exact clock, rate constants, integ_rates, random stream).  Loading sets the batch's
+ * rate constants from the file; walltime: the file's (may be NULL). */
+KMC_API int kmc_otf_save_reload(kmc_otf *h, int32_t traj, const char *path, double walltime);
+KMC_API int kmc_otf_load_reload(kmc_otf *h, int32_t traj, const char *path, double *walltime);
+/* The batch's rate constants (base.rates), P values. */
+KMC_API int kmc_otf_get_rate_consts(kmc_otf *h, double *rates);
 /* Rate tables (no reference counterpart; results are the same either way): a process's
  * rate depends only on its bystander counts, so for models whose counts take at most
  * 4096 combinations in all, each combination's rate is computed once by the process's

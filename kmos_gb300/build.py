@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libkmcgb300.so")
 SOURCES = [os.path.join(CSRC, "kmc_engine.cu"), os.path.join(CSRC, "kmc_run_g16.cu"),
            os.path.join(CSRC, "kmc_solo.cu"), os.path.join(CSRC, "kmc_state.cu"), os.path.join(CSRC, "kmc_otf.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, "kmc_device.cuh"), os.path.join(CSRC, "kmc_run.cuh"),
-                  os.path.join(CSRC, "kmc_host.h"), os.path.join(ROOT, "include", "kmc_gb300.h")]
+                  os.path.join(CSRC, "kmc_host.h"), os.path.join(CSRC, "kmc_reload.h"), os.path.join(ROOT, "include", "kmc_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

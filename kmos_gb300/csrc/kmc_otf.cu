@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -37,6 +38,7 @@
 #include "../../include/kmc_gb300.h"
 #include "kmc_device.cuh"
 #include "kmc_host.h"
+#include "kmc_reload.h"
 
 namespace otfdev {
 using namespace kmc;
@@ -737,7 +739,8 @@ struct Smem {
 // cmd: 0 = do_kmc_steps(n) on every trajectory (trace: only trajectory `only`, pairs to
 // trace); 1 = update_accum_rate; 2 = update_integ_rate; 3 = get_next_kmc_step of `only`
 // (out[0..1]); 4 = run_proc_nr(out[0], out[1]) on `only`; 5 = initialize_state(layer = n);
-// 6 = recalculate_rates_matrix.
+// 6 = recalculate_rates_matrix; 7 = touchup_cell of the n cells (x, y, z) in io, in
+// order, on `only`.
 __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
   __shared__ Smem sm;
   extern __shared__ __align__(16) int32_t prog_s[];  // the program, when staged
@@ -809,6 +812,14 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
   if (cmd == 2) {
     for (int p0 = lane; p0 < P; p0 += 32)
       v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(v.tot[p0], tr.kmc_time_step));
+    return;
+  }
+  if (cmd == 7) {  // touchup_cell (io:3240-3284): the cell's first site stripped, its adds
+    if (lane == 0) {
+      for (int64_t i = 0; i < n && !v.err; i++) run_stream(v, v.prog[d.off_touch], io[3 * i], io[3 * i + 1], io[3 * i + 2]);
+      tr.status = v.err;
+      d.traj[t] = tr;
+    }
     return;
   }
   if (cmd == 4) {
@@ -1197,6 +1208,61 @@ int traj_status(kmc_otf *h, int traj) {
   return tr.status ? fail(tr.status, "trajectory stopped with a table, species or dead-lock error") : KMC_OK;
 }
 
+// A trajectory's state from the host (reload_system, base_otf.f90:448-599): lattice,
+// avail_sites(:, :, 1) as [P][V+1] (entry 0 unused), nr_of_sites, procstat, integ_rates
+// (NULL: zero), the clock, kmc_step, and the random stream when rng is given.  Checked
+// first: species in range, each list's entries distinct sites.  avail_sites(:, :, 2) is
+// rebuilt as the inverse; rates_matrix is zero as after allocate_system (the reference's
+// file does not hold it) until recalculate_rates_matrix.
+int otf_store(kmc_otf *h, int traj, const int32_t *lattice, const int32_t *as1, const int32_t *nsites,
+              const int64_t *procstat, const double *integ, const double clock[2], int64_t kmc_step, const Traj *rng) {
+  const Dev &d = h->d;
+  const int P = d.P, V = d.V;
+  const size_t PV = (size_t)P * (V + 1);
+  std::vector<int8_t> lat(V);
+  for (int i = 0; i < V; i++) {
+    if (lattice[i] < -1 || lattice[i] > d.nspecies) return fail(KMC_ERR_ARG, "state: unknown species");
+    lat[i] = (int8_t)lattice[i];
+  }
+  std::vector<int32_t> a1(PV, 0), a2(PV, 0), dirty(P, 1);
+  for (int q = 0; q < P; q++) {
+    const int n = nsites[q];
+    if (n < 0 || n > V) return fail(KMC_ERR_TABLE, "state: nr_of_sites out of range");
+    for (int i = 1; i <= n; i++) {
+      const int s = as1[(size_t)q * (V + 1) + i];
+      if (s < 1 || s > V || a2[(size_t)q * (V + 1) + s] != 0) return fail(KMC_ERR_TABLE, "state: avail_sites entry");
+      a1[(size_t)q * (V + 1) + i] = s;
+      a2[(size_t)q * (V + 1) + s] = i;
+    }
+  }
+  std::vector<double> zeros(PV, 0.0), integ0(P, 0.0);
+  Traj tr;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&tr, d.traj + traj, sizeof(Traj), cudaMemcpyDeviceToHost));
+  tr.kmc_time = clock[0];
+  tr.kmc_time_step = clock[1];
+  tr.kmc_step = kmc_step;
+  tr.status = 0;
+  if (rng) {
+    tr.rng_kind = rng->rng_kind; tr.seed = rng->seed; tr.traj = rng->traj;
+    for (int i = 0; i < 4; i++) tr.rng[i] = rng->rng[i];
+  }
+  CK(cudaMemcpy(d.lat + (size_t)traj * V, lat.data(), V, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.as1 + traj * PV, a1.data(), PV * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.as2 + traj * PV, a2.data(), PV * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.rm + traj * PV, zeros.data(), PV * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.pm + traj * PV, zeros.data(), PV * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.dirty + (size_t)traj * P, dirty.data(), P * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.ns + (size_t)traj * P, nsites, P * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.procstat + (size_t)traj * P, procstat, P * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.integ + (size_t)traj * P, integ ? integ : integ0.data(), P * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.accum + (size_t)traj * P, integ0.data(), P * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.tot + (size_t)traj * P, integ0.data(), P * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.traj + traj, &tr, sizeof(Traj), cudaMemcpyHostToDevice));
+  h->uni_ok = false;  // the entries' rates are zero, not the constant-rate processes' rates
+  return KMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1419,6 +1485,120 @@ int kmc_otf_get_state(kmc_otf *h, int32_t traj, int32_t *lattice, int32_t *as1, 
 int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on) {
   if (!h) return fail(KMC_ERR_ARG, "bad handle");
   h->d.tab_on = on && h->d.tab_entries > 0 ? 1 : 0;
+  return KMC_OK;
+}
+
+int kmc_otf_get_rate_consts(kmc_otf *h, double *rates) {
+  if (!h || !rates) return fail(KMC_ERR_ARG, "bad arguments");
+  std::copy(h->rates.begin(), h->rates.end(), rates);
+  return KMC_OK;
+}
+
+int kmc_otf_set_kmc_time(kmc_otf *h, int32_t traj, double kmc_time) {
+  if (!h || traj < 0 || traj >= h->d.T) return fail(KMC_ERR_ARG, "bad arguments");
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&h->d.traj[traj].kmc_time, &kmc_time, sizeof(double), cudaMemcpyHostToDevice));
+  return KMC_OK;
+}
+
+int kmc_otf_replace_species(kmc_otf *h, int32_t traj, int32_t site, int32_t old_species, int32_t new_species) {
+  if (!h || traj < 0 || traj >= h->d.T || site < 1 || site > h->d.V) return fail(KMC_ERR_ARG, "bad arguments");
+  if (new_species < -1 || new_species > h->d.nspecies) return fail(KMC_ERR_ARG, "unknown species");
+  int8_t *cell = h->d.lat + (size_t)traj * h->d.V + (site - 1);
+  int8_t cur;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&cur, cell, 1, cudaMemcpyDeviceToHost));
+  if (cur != old_species) return fail(KMC_ERR_SPECIES, "replace_species: the site holds another species");
+  const int8_t nw = (int8_t)new_species;
+  CK(cudaMemcpy(cell, &nw, 1, cudaMemcpyHostToDevice));
+  return KMC_OK;
+}
+
+int kmc_otf_touchup_cells(kmc_otf *h, int32_t traj, int32_t n, const int32_t *cells) {
+  if (!h || traj < 0 || traj >= h->d.T || n < 0 || (n > 0 && !cells)) return fail(KMC_ERR_ARG, "bad arguments");
+  if (n == 0) return KMC_OK;
+  for (int32_t i = 0; i < n; i++)
+    if (cells[3 * i] < 0 || cells[3 * i] >= h->d.X || cells[3 * i + 1] < 0 || cells[3 * i + 1] >= h->d.Y ||
+        cells[3 * i + 2] < 0 || cells[3 * i + 2] >= h->d.Z)
+      return fail(KMC_ERR_ARG, "cell out of range");
+  int rc = io_buffer(h, (size_t)3 * n);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->d_io, cells, (size_t)12 * n, cudaMemcpyHostToDevice, h->stream));
+  rc = launch(h, 7, n, traj, h->d_io);
+  if (rc) return rc;
+  rc = sync_timed(h);
+  return rc ? rc : traj_status(h, traj);
+}
+
+int kmc_otf_set_state(kmc_otf *h, int32_t traj, const int32_t *lattice, const int32_t *as1, const int32_t *nr_of_sites,
+                      const int64_t *procstat, const double *integ_rates, const double clock[2], int64_t kmc_step) {
+  if (!h || traj < 0 || traj >= h->d.T || !lattice || !as1 || !nr_of_sites || !procstat || !clock || kmc_step < 0)
+    return fail(KMC_ERR_ARG, "bad arguments");
+  return otf_store(h, traj, lattice, as1, nr_of_sites, procstat, integ_rates, clock, kmc_step, nullptr);
+}
+
+int kmc_otf_save_reload(kmc_otf *h, int32_t traj, const char *path, double walltime) {
+  if (!h || traj < 0 || traj >= h->d.T || !path) return fail(KMC_ERR_ARG, "bad arguments");
+  const Dev &dv = h->d;
+  const int P = dv.P, V = dv.V;
+  const size_t PV = (size_t)P * (V + 1);
+  std::vector<int8_t> lat(V);
+  std::vector<int32_t> a1(PV), ns(P);
+  kmc_reload::ReloadData d;
+  d.P = P;
+  d.V = V;
+  d.procstat.resize(P);
+  d.integ.resize(P);
+  Traj tr;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(lat.data(), dv.lat + (size_t)traj * V, V, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(a1.data(), dv.as1 + traj * PV, PV * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ns.data(), dv.ns + (size_t)traj * P, P * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(d.procstat.data(), dv.procstat + (size_t)traj * P, P * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(d.integ.data(), dv.integ + (size_t)traj * P, P * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&tr, dv.traj + traj, sizeof(Traj), cudaMemcpyDeviceToHost));
+  d.dims[0] = dv.X; d.dims[1] = dv.Y; d.dims[2] = dv.Z;
+  d.kmc_time = tr.kmc_time;
+  d.kmc_time_step = tr.kmc_time_step;
+  d.walltime = walltime;
+  d.kmc_step = tr.kmc_step;
+  d.rng_kind = tr.rng_kind; d.seed = tr.seed; d.traj = tr.traj;
+  for (int i = 0; i < 4; i++) d.rng[i] = tr.rng[i];
+  d.rates = h->rates;
+  d.nsites = ns;
+  d.lattice.assign(lat.begin(), lat.end());
+  d.as1.resize(P);
+  for (int q = 0; q < P; q++) d.as1[q].assign(a1.begin() + (size_t)q * (V + 1) + 1, a1.begin() + (size_t)q * (V + 1) + 1 + ns[q]);
+  return kmc_reload::write_reload(path, d);
+}
+
+int kmc_otf_load_reload(kmc_otf *h, int32_t traj, const char *path, double *walltime) {
+  if (!h || traj < 0 || traj >= h->d.T || !path) return fail(KMC_ERR_ARG, "bad arguments");
+  kmc_reload::ReloadFile r;
+  int rc = kmc_reload::parse_reload(path, r, false);
+  if (rc) return rc;
+  kmc_reload::ReloadData d;
+  rc = kmc_reload::read_reload(r, h->d.P, h->d.V, h->d.nspecies, d);
+  if (rc) return rc;
+  const int P = h->d.P, V = h->d.V;
+  std::vector<int32_t> a1((size_t)P * (V + 1), 0);
+  for (int q = 0; q < P; q++)
+    std::copy(d.as1[q].begin(), d.as1[q].end(), a1.begin() + (size_t)q * (V + 1) + 1);
+  const double clock[2] = {d.kmc_time, d.kmc_time_step};
+  Traj rng{};
+  if (r.have_rng) {
+    rng.rng_kind = d.rng_kind; rng.seed = d.seed; rng.traj = d.traj;
+    for (int i = 0; i < 4; i++) rng.rng[i] = d.rng[i];
+  }
+  rc = otf_store(h, traj, d.lattice.data(), a1.data(), d.nsites.data(), d.procstat.data(), d.integ.data(), clock,
+                 d.kmc_step, r.have_rng ? &rng : nullptr);
+  if (rc) return rc;
+  // the file's rate constants (base.reload_system reads `rates`)
+  h->rates = d.rates;
+  h->tab_stale = true;
+  CK(cudaMemcpyAsync(h->d_rates, h->rates.data(), h->rates.size() * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (walltime) *walltime = d.walltime;
   return KMC_OK;
 }
 

@@ -130,6 +130,13 @@ SIGNATURES = {
     "kmc_otf_launch_count": (_i32, [_vp, _p64]),
     "kmc_otf_phase_cycles": (_i32, [_vp, ctypes.POINTER(ctypes.c_uint64), _i32]),
     "kmc_otf_set_rate_tables": (_i32, [_vp, _i32]),
+    "kmc_otf_set_kmc_time": (_i32, [_vp, _i32, _dbl]),
+    "kmc_otf_replace_species": (_i32, [_vp, _i32, _i32, _i32, _i32]),
+    "kmc_otf_touchup_cells": (_i32, [_vp, _i32, _i32, _p32]),
+    "kmc_otf_set_state": (_i32, [_vp, _i32, _p32, _p32, _p32, _p64, _pd, _pd, _i64]),
+    "kmc_otf_save_reload": (_i32, [_vp, _i32, ctypes.c_char_p, _dbl]),
+    "kmc_otf_load_reload": (_i32, [_vp, _i32, ctypes.c_char_p, _pd]),
+    "kmc_otf_get_rate_consts": (_i32, [_vp, _pd]),
     "kmc_otf_set_constant_rate_sums": (_i32, [_vp, _i32]),
     "kmc_otf_rate_table_entries": (_i32, [_vp, _p32]),
 }
@@ -747,6 +754,44 @@ class OtfBatch:
 
     def run_proc_nr(self, proc: int, site: int, traj: int = 0):
         _check(load().kmc_otf_run_proc_nr(self.h, int(traj), int(proc), int(site)))
+
+    def set_kmc_time(self, traj: int, t: float):
+        _check(load().kmc_otf_set_kmc_time(self.h, int(traj), float(t)))
+
+    def replace_species(self, traj: int, site: int, old: int, new: int):
+        _check(load().kmc_otf_replace_species(self.h, int(traj), int(site), int(old), int(new)))
+
+    def touchup_cells(self, traj: int, cells):
+        """touchup_cell of each (x, y, z) in order, one launch (``kmc_otf_touchup_cells``)."""
+        c = np.ascontiguousarray(np.asarray(cells, dtype=np.int32).reshape(-1, 3))
+        _check(load().kmc_otf_touchup_cells(self.h, int(traj), len(c), _ptr(c, _i32)))
+
+    def set_state(self, traj: int, lattice, as1, nsites, procstat, integ=None, kmc_time: float = 0.0,
+                  kmc_time_step: float = 0.0, kmc_step: int = 0):
+        """Uploads one trajectory's state (``kmc_otf_set_state``); as1 is [P][V+1]."""
+        lat = _a32(lattice)
+        a1 = _a32(np.asarray(as1).reshape(-1))
+        ns = _a32(nsites)
+        ps = np.ascontiguousarray(procstat, dtype=np.int64)
+        ig = None if integ is None else np.ascontiguousarray(integ, dtype=np.float64)
+        clock = np.array([kmc_time, kmc_time_step], dtype=np.float64)
+        _check(load().kmc_otf_set_state(self.h, int(traj), _ptr(lat, _i32), _ptr(a1, _i32), _ptr(ns, _i32),
+                                        _ptr(ps, _i64), None if ig is None else _ptr(ig, _dbl), _ptr(clock, _dbl),
+                                        int(kmc_step)))
+
+    def save_reload(self, traj: int, path: str, walltime: float = 0.0):
+        _check(load().kmc_otf_save_reload(self.h, int(traj), os.fsencode(path), float(walltime)))
+
+    def load_reload(self, traj: int, path: str) -> float:
+        """Loads a .reload file into one trajectory; returns the file's walltime."""
+        w = _dbl()
+        _check(load().kmc_otf_load_reload(self.h, int(traj), os.fsencode(path), ctypes.byref(w)))
+        return w.value
+
+    def rate_consts(self) -> np.ndarray:
+        out = np.zeros(self.P, np.float64)
+        _check(load().kmc_otf_get_rate_consts(self.h, _ptr(out, _dbl)))
+        return out
 
     STATE_FIELDS = ("lattice", "as1", "as2", "nsites", "procstat", "integ", "accum", "rates_matrix", "totals",
                     "clock")

@@ -36,9 +36,7 @@ from .program import compile_model
 
 class _OtfTrajectory:
     """One otf trajectory (``engine.OtfBatch`` of one, on the gfortran stream of the
-    seed) behind the calls the base / lattice / proclist namespaces make.  Lattice edits
-    (replace_species, touch-ups), reload files and setting the clock are not offered by
-    the otf engine and raise KMCError."""
+    seed) behind the calls the base / lattice / proclist namespaces make."""
 
     def __init__(self, program, size, layer: int, seed: int):
         self.b = E.OtfBatch(program, size, ntraj=1, layer=layer, seed=seed, rng=E.RNG_GFORTRAN)
@@ -82,7 +80,7 @@ class _OtfTrajectory:
 
     @kmc_time.setter
     def kmc_time(self, t: float):
-        raise E.KMCError(1, "set_kmc_time is not offered by the otf engine")
+        self.b.set_kmc_time(0, t)
 
     @property
     def kmc_time_step(self) -> float:
@@ -134,10 +132,24 @@ class _OtfTrajectory:
             occ[sp] = (lat == sp).sum(axis=0) / self.cells
         return occ
 
-    def _refuse(self, *_a, **_k):
-        raise E.KMCError(1, "lattice edits, touch-ups and reload files are not offered by the otf engine")
+    def replace_species(self, site: int, old: int, new: int):
+        self.b.replace_species(0, site, old, new)
 
-    replace_species = touchup_many = save_reload = load_reload = _refuse
+    def touchup_many(self, sites):
+        """touchup_cell of the cells whose first sites are ``sites``, in order (the
+        _State queue holds site numbers)."""
+        X, Y = self.b.size[0], self.b.size[1]
+        c = (np.asarray(sites, dtype=np.int64) - 1) // self.spuck
+        self.b.touchup_cells(0, np.stack([c % X, (c // X) % Y, c // (X * Y)], axis=1))
+
+    def save_reload(self, path: str):
+        self.b.save_reload(0, path, self.walltime)
+
+    def load_reload(self, path: str):
+        """The file's state, rate constants and walltime (base_otf.f90:448-599)."""
+        w = self.b.load_reload(0, path)
+        self._rates = self.b.rate_consts()
+        self._t0 = time.time() - w
 
 
 class _State:
@@ -247,7 +259,13 @@ def _reload_system(S: _State, input_system_name) -> bool:
                                 "first" % (path, volume))
     S.system_size[:] = dims
     layer = S.model.layer_ids()[S.model.default_layer]
-    S.traj = E.Trajectory(S.program, dims, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
+    if S.backend == "otf":
+        S.traj = _OtfTrajectory(S.program, dims, layer, S.seed)
+        pars = _pars(S)
+        for k, v in enumerate(pars.userpar[:int(S.program.words[23])], start=1):
+            S.traj.b.set_user_parameter(k, float(v))
+    else:
+        S.traj = E.Trajectory(S.program, dims, layer=layer, seed=S.seed, rng=E.RNG_GFORTRAN)
     S.traj.load_reload(path)
     return True
 
@@ -344,7 +362,7 @@ def _proclist(S: _State) -> types.SimpleNamespace:
         for k, v in vars(pars).items():
             if not hasattr(ns, k):
                 setattr(ns, k, v)
-        ns.touchup_cell = lambda cell: S.t().touchup_many([cell])
+        ns.touchup_cell = lambda cell: S.touchup([cell[0], cell[1], cell[2], 1])
     elif S.backend == "lat_int":
         ns.touchup_cell = lambda cell: S.touchup([cell[0], cell[1], cell[2], 1])
     else:

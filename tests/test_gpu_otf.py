@@ -166,6 +166,83 @@ def test_dropin_module_otf_build():
     lattice.deallocate_system()
 
 
+def test_dropin_module_otf_put_reload_and_clock(tmp_path, monkeypatch):
+    """The otf build of kmos_gb300.kmc_model under kmos.run's put (lattice.replace_species,
+    proclist.touchup_cell of every cell x-outermost, base.update_accum_rate;
+    run/__init__.py:1243-1314, 1439-1457) equals the oracle doing the same; then
+    base.save_system / reload_system into a fresh allocation continues as the original
+    would, and base.set_kmc_time sets the clock."""
+    from kmos_gb300 import kmc_model
+    monkeypatch.chdir(tmp_path)
+    m = fixture_model("intZGB_otf")
+    params = dict(zip(OTF.user_parameters(m), INTZGB_PARAMS))
+    size = (9, 8)
+
+    def setup():
+        base, lattice, proclist = kmc_model.configure(m, "otf")
+        return base, lattice, proclist
+
+    base, lattice, proclist = setup()
+    proclist.init(size, "otfrun", lattice.default_layer, 3, True)
+    for p, r in enumerate(INTZGB_RATES, start=1):
+        base.set_rate_const(p, r)
+    for name, v in params.items():
+        proclist.update_user_parameter(getattr(proclist, name.lower()), v)
+    proclist.recalculate_rates_matrix()
+    base.update_accum_rate()
+    base.update_integ_rate()
+    proclist.do_kmc_steps(400)
+    prog = PG.compile_model(m, "otf")
+    o = O.Oracle(prog, size, seed=3, rng=O.RNG_GFORTRAN)
+    o.set_rates(INTZGB_RATES)
+    o.set_user_parameters(INTZGB_PARAMS)
+    o.recalculate_rates_matrix()
+    o.update_accum_rate()
+    o.update_integ_rate()
+    o.do_kmc_steps(400)
+    # put CO at (2, 3) and O at (7, 1): model.put = _put then _adjust_database
+    for (x, y), spec in (((2, 3), proclist.co), ((7, 1), proclist.o)):
+        site = [x, y, 0, 1]
+        old = lattice.get_species(site)
+        lattice.replace_species(site, old, spec)
+        o.replace_species(_lattice2nr(size, 1, x, y, 0, 1), old, spec)
+        for cx in range(size[0]):
+            for cy in range(size[1]):
+                proclist.touchup_cell([cx, cy, 0, 0])
+                o.touchup(_lattice2nr(size, 1, cx, cy, 0, 1))
+        base.update_accum_rate()
+        o.update_accum_rate()
+    proclist.do_kmc_steps(600)
+    o.do_kmc_steps(600)
+    _rm, tot = o.rates_matrix()
+    assert base.get_kmc_step() == 1000
+    np.testing.assert_allclose(base.get_kmc_time(), o.kmc_time, rtol=1e-12)
+    for p in range(1, len(INTZGB_RATES) + 1):
+        assert base.get_procstat(p) == o.procstat()[p - 1]
+        assert base.get_nrofsites(p) == o.nr_of_sites()[p - 1]
+        assert base.get_rate(p) == tot[p - 1]
+    np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
+    # save_system, then reload_system into a fresh allocation
+    base.save_system()
+    before = [base.get_procstat(p) for p in range(1, len(INTZGB_RATES) + 1)]
+    proclist.do_kmc_steps(300)
+    after = ([base.get_procstat(p) for p in range(1, len(INTZGB_RATES) + 1)], base.get_kmc_time())
+    lattice.deallocate_system()
+    base2, lattice2, proclist2 = setup()
+    assert base2.reload_system("otfrun")
+    assert [base2.get_procstat(p) for p in range(1, len(INTZGB_RATES) + 1)] == before
+    for name, v in params.items():
+        proclist2.update_user_parameter(getattr(proclist2, name.lower()), v)
+    proclist2.recalculate_rates_matrix()
+    base2.update_accum_rate()
+    proclist2.do_kmc_steps(300)
+    assert [base2.get_procstat(p) for p in range(1, len(INTZGB_RATES) + 1)] == after[0]
+    assert base2.get_kmc_time() == after[1]
+    base2.set_kmc_time(0.0)
+    assert base2.get_kmc_time() == 0.0
+    lattice2.deallocate_system()
+
+
 def _states_equal(a, b, t):
     ga, gb = a.state(t), b.state(t)
     for k in ga:
@@ -241,3 +318,106 @@ def test_constant_rate_sums_equal_summed_lists():
     assert on.get_next_kmc_step(2) == off.get_next_kmc_step(2)
     np.testing.assert_array_equal(on.trace(3, 300), off.trace(3, 300))
     _states_equal(on, off, 3)
+
+
+def _lattice2nr(size, spuck, x, y, z, n):
+    X, Y = size[0], size[1]
+    return spuck * (x + X * (y + Y * z)) + n
+
+
+def test_put_and_adjust_database_match_oracle():
+    """kmos.run's put on an otf model (run/__init__.py:1243-1314, 1439-1457):
+    replace_species at some sites, touchup_cell of every cell x-outermost, then
+    update_accum_rate -- on the device and in the oracle, then more steps; every table,
+    rate and pick equal."""
+    m = fixture_model("intZGB_otf")
+    size = (10, 9)
+    prog, b, (o,) = setup_both(m, size, INTZGB_RATES, INTZGB_PARAMS, 1, traj0=4)
+    sp = int(prog.words[6])
+    b.do_kmc_steps(700)
+    o.do_kmc_steps(700)
+    compare(b, 0, o)
+    ids = m.species_ids()
+    lat = b.state(0, ["lattice"])["lattice"]
+    edits = [(3, 4), (0, 0), (9, 8), (5, 5)]
+    for k, (x, y) in enumerate(edits):
+        site = _lattice2nr(size, sp, x, y, 0, 1)
+        old = int(lat[site - 1])
+        new = [ids["CO"], ids["O"], ids["empty"], ids["CO"]][k]
+        b.replace_species(0, site, old, new)
+        o.replace_species(site, old, new)
+    cur = int(b.state(0, ["lattice"])["lattice"][0])
+    with pytest.raises(E.KMCError):
+        b.replace_species(0, 1, (cur + 1) % 3, cur)   # the site holds another species
+    cells = [(x, y, 0) for x in range(size[0]) for y in range(size[1])]
+    b.touchup_cells(0, cells)
+    for (x, y, z) in cells:
+        o.touchup(_lattice2nr(size, sp, x, y, z, 1))
+    b.update_accum_rate()
+    o.update_accum_rate()
+    compare(b, 0, o)
+    b.do_kmc_steps(900)
+    o.do_kmc_steps(900)
+    compare(b, 0, o)
+
+
+def test_set_kmc_time():
+    m = fixture_model("intZGB_otf")
+    _prog, b, _o = setup_both(m, (8, 8), INTZGB_RATES, INTZGB_PARAMS, 2)
+    b.do_kmc_steps(50)
+    b.set_kmc_time(1, 123.25)
+    assert b.state(1, ["clock"])["kmc_time"] == 123.25
+    assert b.state(0, ["clock"])["kmc_time"] != 123.25
+    b.do_kmc_steps(10)
+    assert b.state(1, ["clock"])["kmc_time"] > 123.25
+
+
+def test_reload_round_trip_continues_bit_for_bit(tmp_path):
+    """save_system of one trajectory, reload_system into a fresh batch (the file's
+    lattice, avail_sites, counters, clock, rate constants and random stream; rates_matrix
+    rebuilt by recalculate_rates_matrix as kmos.run does), then both run on: every state
+    field equal.  The file is the reference's layout: the oracle's reader takes it."""
+    m = fixture_model("intZGB_otf")
+    size = (12, 10)
+    prog = PG.compile_model(m, "otf")
+    a = E.OtfBatch(prog, size, ntraj=3, seed=5, rng=E.RNG_PHILOX)
+    a.set_rates(INTZGB_RATES)
+    a.set_user_parameters(INTZGB_PARAMS)
+    a.recalculate_rates_matrix()
+    a.update_accum_rate()
+    a.update_integ_rate()
+    a.do_kmc_steps(800)
+    path = str(tmp_path / "otf.reload")
+    a.save_reload(2, path, walltime=3.5)
+    b = E.OtfBatch(prog, size, ntraj=1, seed=1, rng=E.RNG_PHILOX)
+    b.set_user_parameters(INTZGB_PARAMS)
+    assert b.load_reload(0, path) == pytest.approx(3.5)
+    np.testing.assert_array_equal(b.rate_consts(), np.array(INTZGB_RATES))
+    ga, gb = a.state(2), b.state(0)
+    for k in ("lattice", "as1", "as2", "nsites", "procstat", "integ"):
+        np.testing.assert_array_equal(ga[k], gb[k], err_msg=k)
+    assert (ga["kmc_time"], ga["kmc_time_step"], ga["kmc_step"]) == (gb["kmc_time"], gb["kmc_time_step"], gb["kmc_step"])
+    for x in (a, b):
+        x.recalculate_rates_matrix()
+        x.update_accum_rate()
+    ga, gb = a.state(2), b.state(0)
+    np.testing.assert_array_equal(ga["rates_matrix"], gb["rates_matrix"])
+    a.do_kmc_steps(1500)
+    b.do_kmc_steps(1500)
+    ga, gb = a.state(2), b.state(0)
+    for k in ga:
+        np.testing.assert_array_equal(np.asarray(ga[k]), np.asarray(gb[k]), err_msg=k)
+    from oracle import reload as R
+    f = R.read_reload(path)
+    assert f["nr_of_proc"] == len(m.processes) and f["volume"] == size[0] * size[1]
+    saved = E.OtfBatch(prog, size, ntraj=1, seed=1, rng=E.RNG_PHILOX)
+    saved.load_reload(0, path)
+    g = saved.state(0)
+    np.testing.assert_array_equal(f["lattice"], g["lattice"])
+    np.testing.assert_array_equal(f["nr_of_sites"], g["nsites"])
+    np.testing.assert_array_equal(f["procstat"], g["procstat"])
+    for p in range(1, len(m.processes) + 1):
+        np.testing.assert_array_equal(f["as1"][p], g["as1"][p - 1, 1:])
+        np.testing.assert_array_equal(f["as2"][p], g["as2"][p - 1, 1:])
+    with pytest.raises(E.KMCError):
+        b.set_state(0, np.full(b.V, 99), np.zeros((b.P, b.V + 1)), np.zeros(b.P), np.zeros(b.P))

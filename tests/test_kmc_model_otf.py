@@ -19,6 +19,7 @@ class OracleOtfBatch:
         assert ntraj == 1
         self.o = O.Oracle(program, size, layer=layer, seed=seed, rng=rng, traj=traj0)
         self.P, self.V, self.spuck = self.o.P, self.o.V, self.o.spuck
+        self.size = [int(v) for v in (list(size) + [1, 1])[:3]]
 
     def close(self):
         pass
@@ -46,6 +47,16 @@ class OracleOtfBatch:
 
     def run_proc_nr(self, proc, site, traj=0):
         self.o.run_proc_nr(proc, site)
+
+    def replace_species(self, traj, site, old, new):
+        if self.o.get_species(site) != old:
+            raise E.KMCError(2, "replace_species: the site holds another species")
+        self.o.replace_species(site, old, new)
+
+    def touchup_cells(self, traj, cells):
+        X, Y = self.size[0], self.size[1]
+        for x, y, z in np.asarray(cells).reshape(-1, 3):
+            self.o.touchup(self.spuck * (int(x) + X * (int(y) + Y * int(z))) + 1)
 
     def state(self, traj=0, fields=None):
         ex = self.o.export()
@@ -101,9 +112,28 @@ def test_otf_dropin_sequence(monkeypatch):
     proclist.run_proc_nr(p, s)
     o.run_proc_nr(p, s)
     np.testing.assert_array_equal(proclist.get_occupation(), o.occupation(len(m.species)))
+    # kmos.run's put (run/__init__.py:1243-1314): replace_species, then _adjust_database
+    # (touchup_cell of every cell, x outermost; 1439-1457) and update_accum_rate
     import pytest
+    old = lattice.get_species((0, 0, 0, 1))
     with pytest.raises(E.KMCError):
-        lattice.replace_species((0, 0, 0, 1), 0, 1)
+        lattice.replace_species((0, 0, 0, 1), (old + 1) % 3, 1)
+    new = (old + 1) % 3
+    lattice.replace_species((0, 0, 0, 1), old, new)
+    o.replace_species(1, old, new)
+    for x in range(12):
+        for y in range(10):
+            proclist.touchup_cell([x, y, 0, 0])
+            o.touchup(1 + x + 12 * y)
+    base.update_accum_rate()
+    o.update_accum_rate()
+    proclist.do_kmc_steps(300)
+    o.do_kmc_steps(300)
+    ex = o.export()
+    assert base.get_kmc_time() == o.kmc_time
+    for p in range(1, len(rates) + 1):
+        assert base.get_procstat(p) == ex["procstat"][p - 1]
+        assert base.get_nrofsites(p) == ex["nsites"][p - 1]
     lattice.deallocate_system()
     assert not base.is_allocated()
 
