@@ -472,7 +472,7 @@ struct EventSmem {
 // was absent before the event is absent at its turn too and needs no rate.  A stream of
 // more than OTF_RATE_OPS ops is replayed by lane 0 alone, in program order, the ops past
 // the listed ones evaluated there.
-__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane OTF_PH_PARAMS) {
+__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane, bool keep_tot OTF_PH_PARAMS) {
   const int32_t *w = v.prog;
   int32_t *offs = es.off;
   int nops = 0;
@@ -563,17 +563,81 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     };
     if (v.d->P <= OTF_PMASK_PROCS) {
       // each lane walks only its own processes' ops (bits of their masks, cleared as
-      // read), so the lanes' replays run side by side
-      for (int q = lane; q < v.d->P; q += 32)
+      // read), so the lanes' replays run side by side.  A process's list length, stale
+      // mark and running total stay in registers over its ops: add_proc, del_proc and
+      // update_rates_matrix (base_otf.f90:221-364) on them, then one write back.  The
+      // total rates_matrix(p, V+1) is only kept where it is read before the next
+      // update_accum_rate overwrites it (keep_tot: the last step of a launch).
+      const int V = v.d->V;
+      for (int q = lane; q < v.d->P; q += 32) {
+        uint32_t any = 0;
+        for (int wd = 0; wd < OTF_RATE_OPS / 32; wd++) any |= es.pmask[q][wd];
+        if (!any) continue;
+        int32_t *a1 = v.as1 + v.row(q), *a2 = v.as2 + v.row(q);
+        double *r = v.rm + v.row(q);
+        int n = v.ns[q], dq = v.dirty[q];
+        double tq = keep_tot ? v.tot[q] : 0.0;
+        bool mv = false;  // an op of this event deleted or added an entry of q
+        int err = ST_OK;
+#pragma unroll 1
         for (int wd = 0; wd < OTF_RATE_OPS / 32; wd++) {
           uint32_t b = es.pmask[q][wd];
           es.pmask[q][wd] = 0u;
-          while (b && !v.err) {
+          while (b && err == ST_OK) {
             const int k = 32 * wd + __ffs(b) - 1;
             b &= b - 1;
-            apply(k);
+            const int op = (uint32_t)w[es.off[k]] & 0xFF;
+            const int site = es.site[k];
+            const int m = mv ? a2[site] : es.m0[k];
+            if (op == OP_GDEL) {
+              if (m == 0) continue;
+              if (m < 1 || m > n) { err = ST_TABLE; break; }
+              if (keep_tot) tq = __dsub_rn(tq, r[m]);
+              if (m < n) {
+                const int last = a1[n];
+                if (last < 1 || last > V) { err = ST_TABLE; break; }
+                a1[m] = last;
+                a1[n] = 0;
+                r[m] = r[n];
+                r[n] = 0.0;
+                a2[last] = m;
+              } else {
+                a1[m] = 0;
+                r[m] = 0.0;
+              }
+              a2[site] = 0;
+              n -= 1;
+              dq = min(dq, m);
+              mv = true;
+            } else if (op == OP_ADD) {
+              if (!es.ok[k]) continue;
+              if (site < 1 || site > V || m != 0 || n + 1 > V) { err = ST_TABLE; break; }
+              n += 1;
+              a1[n] = site;
+              a2[site] = n;
+              if (keep_tot) tq = __dadd_rn(tq, es.rate[k]);
+              r[n] = es.rate[k];
+              dq = min(dq, n);
+              mv = true;
+            } else if (m != 0) {  // OP_UPDATE (base_otf.f90:333-364)
+              double rate = es.rate[k];
+              if (!es.ok[k]) {  // absent before the event, present now
+                int cx, cy, cz;
+                v.g.cell(bx, by, bz, w[es.off[k] + 1], cx, cy, cz);
+                rate = rate_of(v, q + 1, cx, cy, cz);
+              }
+              if (keep_tot) tq = __dsub_rn(__dadd_rn(tq, rate), r[m]);
+              r[m] = rate;
+              dq = min(dq, m);
+            }
           }
         }
+        v.ns[q] = n;
+        v.dirty[q] = dq;
+        if (keep_tot) v.tot[q] = tq;
+        if (err) v.err = err;
+        // bits of later words left unread after an error: cleared above already
+      }
     } else {
       for (int k = 0; k < nops && !v.err; k++)
         if ((es.p0[k] & 31) == lane) apply(k);
@@ -910,7 +974,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
     {
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_event(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane OTF_PH_ARGS);
+      run_event(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane, step + 1 == n OTF_PH_ARGS);
     }
     err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
