@@ -795,10 +795,19 @@ __device__ void accum_step(View &v, double *sacc, double *stot, int lane) {
 }
 
 struct Smem {
-  double acc[OTF_WARPS][OTF_PMAX + 1];
-  double tot[OTF_WARPS][OTF_PMAX];
   EventSmem ev[OTF_WARPS];
 };
+
+// Dynamic shared memory of a block: the image (when staged; its size rounded to 16
+// bytes), then each warp's accum_rates (P + 1 doubles, 1-based) and process totals (P).
+// Sized by the model's P rather than OTF_PMAX, a block of intZGB takes 37 KB in all, so
+// four blocks leave most of the SM's on-chip memory to the L1 cache of the tables.
+__host__ __device__ inline size_t otf_image_bytes(int prog_len, int staged) {
+  return staged ? ((size_t)prog_len * 4 + 15) / 16 * 16 : 0;
+}
+__host__ __device__ inline size_t otf_dyn_bytes(int prog_len, int staged, int P) {
+  return otf_image_bytes(prog_len, staged) + (size_t)OTF_WARPS * (2 * P + 1) * 8;
+}
 
 // cmd: 0 = do_kmc_steps(n) on every trajectory (trace: only trajectory `only`, pairs to
 // trace); 1 = update_accum_rate; 2 = update_integ_rate; 3 = get_next_kmc_step of `only`
@@ -807,8 +816,10 @@ struct Smem {
 // order, on `only`.
 __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
   __shared__ Smem sm;
-  extern __shared__ __align__(16) int32_t prog_s[];  // the program, when staged
-  // the block copies the program to shared memory first (every thread is still here)
+  extern __shared__ __align__(16) unsigned char dyn_s[];
+  int32_t *prog_s = reinterpret_cast<int32_t *>(dyn_s);  // the image, when staged
+  double *sums_s = reinterpret_cast<double *>(dyn_s + otf_image_bytes(d.prog_len, d.prog_staged));
+  // the block copies the image to shared memory first (every thread is still here)
   if (d.prog_staged) {
     for (int i = threadIdx.x; i < d.prog_len; i += blockDim.x) prog_s[i] = d.prog[i];
     __syncthreads();
@@ -820,8 +831,8 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
   if (d.prog_staged) v.prog = prog_s;
   Traj tr = d.traj[t];
   if (tr.status && cmd != 5) return;
-  double *sacc = sm.acc[warp], *stot = sm.tot[warp];
   const int P = d.P;
+  double *sacc = sums_s + (size_t)warp * (P + 1), *stot = sums_s + (size_t)OTF_WARPS * (P + 1) + (size_t)warp * P;
   if (cmd == 5) {  // initialize_state (proclist_generic_subroutines.mpy:236-304), the cell touch-up
     if (lane == 0) {
       const int32_t *site_layer = v.prog + d.off_site_layer, *site_def = v.prog + d.off_site_default;
@@ -1214,7 +1225,8 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     d.accum += (size_t)only * d.P; d.tot += (size_t)only * d.P; d.procstat += (size_t)only * d.P;
     d.traj += only; d.T = 1;
   }
-  // the program goes to every block's shared memory when it fits beside the static part
+  // the image goes to every block's shared memory when it fits beside the static part
+  // and the warps' accum_rates and totals
   size_t dyn = 0;
   {
     cudaFuncAttributes fa;
@@ -1223,10 +1235,10 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const int64_t cap = optin - (int64_t)fa.sharedSizeBytes;
-    const size_t want = align_up((size_t)d.prog_len * 4, 16);
-    d.prog_staged = (int64_t)want <= cap ? 1 : 0;
-    if (d.prog_staged) dyn = want;
-    if (dyn > 0 && fa.maxDynamicSharedSizeBytes < (int)dyn)
+    d.prog_staged = (int64_t)otfdev::otf_dyn_bytes(d.prog_len, 1, d.P) <= cap ? 1 : 0;
+    dyn = otfdev::otf_dyn_bytes(d.prog_len, d.prog_staged, d.P);
+    if ((int64_t)dyn > cap) return fail(KMC_ERR_ARG, "otf: too many processes for shared memory");
+    if (fa.maxDynamicSharedSizeBytes < (int)dyn)
       CK(cudaFuncSetAttribute(otfdev::otf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   }
   if (h->tab_stale) {
