@@ -375,9 +375,8 @@ namespace kmc {
 
 constexpr int FAST_SLOTS = 128;
 constexpr int FAST_EDITS = 128;  // largest fast stream: 4 rounds of 32 edits
-constexpr int LOG_MAX = 16;   // lane-private write log entries (a multiple of 4)
+constexpr int LOG_MAX = 8;    // lane-private write log entries (a multiple of 4)
 constexpr int TAIL_MAX = 6;   // prefetched list-tail entries per process
-constexpr int TAIL_PROCS = 64; // processes 0..63 get prefetched tails
 constexpr int FAST_MAXV = (1 << 23) - 1;
 
 enum EditKind { E_GDEL = 0, E_DEL = 1, E_ADD = 2 };
@@ -391,7 +390,7 @@ __host__ __device__ inline int fast_rec_offset(int nlat, int nchk, int nwr) {
 // R rounds of 32 edits: the step kernel comes in R = 3 (streams of up to 96 edits, the
 // common case) and R = 4 (up to 128, large lateral-interaction groups).  G lanes run one
 // trajectory (32: a warp; 16: half a warp), each with its own write log.
-template <int R, int G = 32>
+template <int R, int G = 32, int TP = 32>
 struct FastSmem {
   int32_t latv[FAST_SLOTS];
   int32_t latsite[FAST_SLOTS];
@@ -399,7 +398,7 @@ struct FastSmem {
   int16_t ep[32 * R];      // process, 0-based
   int32_t esite[32 * R];   // target site
   int32_t em[32 * R];      // prefetched avail_sites(p, site, 2) of del edits
-  int32_t tail[TAIL_PROCS][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, p < TAIL_PROCS
+  int32_t tail[TP][TAIL_MAX];  // avail_sites(p, n0 - j, 1), j < TAIL_MAX, for the TP processes of the kernel
   uint4 lkey4[LOG_MAX / 4][G];  // lane-private write logs, four keys per 16 bytes (lane-minor)
   int32_t lval[LOG_MAX][G];
 };

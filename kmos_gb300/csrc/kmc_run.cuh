@@ -102,18 +102,18 @@ struct WarpSmem {
   int32_t ndel[NP * G];       // del edits of each process so far this step (0 between steps)
   long long ph[KMC_NPHASE];   // phase cycle accounting (KMC_PHASE_TIMING builds)
   long long tprev;
-  FastSmem<R, G> f;
+  FastSmem<R, G, NP * G> f;  // list tails for every process the kernel holds
 };
 
 // Replays the edits of process p (bits of pmask[p], in program order).  Lane-private;
 // returns a status.  Clears pmask[p] and ndel[p].  The loads it needs were issued
 // group-parallel while the edits were evaluated: em[k] = avail_sites(p, site_k, 2) for
-// every del edit k, and for p < TAIL_PROCS tail[p][j] = avail_sites(p, n0 - j, 1) for
+// every del edit k, and tail[p][j] = avail_sites(p, n0 - j, 1) for
 // j < min(nd, TAIL_MAX), nd = its del edits.  In a dels-first stream (every del before
 // every add, no (process, site) named by two dels or by two adds) only the moves of
 // the dels are read back, so the cleared position entries and the adds are not logged.
 template <int NP, int R, int G>
-__device__ int replay_process(FastSmem<R, G> &f, int32_t *ns, uint32_t (*pmask)[R], int32_t *ndel,
+__device__ int replay_process(FastSmem<R, G, NP * G> &f, int32_t *ns, uint32_t (*pmask)[R], int32_t *ndel,
                               const View &v, int p, int rounds, bool dels_first, int gl) {
   const size_t row = (size_t)p * v.stride;
   int32_t *a1 = v.as1 + row;
@@ -127,7 +127,6 @@ __device__ int replay_process(FastSmem<R, G> &f, int32_t *ns, uint32_t (*pmask)[
     pmask[p][r] = 0u;
   }
   ndel[p] = 0;
-  const bool has_tail = p < TAIL_PROCS;
   // apply the edits; reads look in the write log, then at the prefetched values.  The
   // log is append-only (a later entry for a key shadows earlier ones) and is searched
   // newest first, four keys per shared-memory load; once full, reads go to memory, which
@@ -192,7 +191,7 @@ __device__ int replay_process(FastSmem<R, G> &f, int32_t *ns, uint32_t (*pmask)[
         int last;
         if (!logok) last = a1[n];
         else if (nlog == 0 || !logged(0, n, last))
-          last = (has_tail && n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
+          last = (n0 - n < TAIL_MAX && n <= n0) ? f.tail[p][n0 - n] : a1[n];
         if (!KMC_IN(last, 1, v.stride - 1)) return ST_TABLE;
         put(0, m, last);
         a1[n] = 0;  // vacated top entry: read again only after an add (logged) refills it
@@ -216,7 +215,7 @@ __device__ int fast_step(WarpSmem<NP, R, G> &sm, const Hot &H, View &v, const in
                          const Group<G> &grp) {
   constexpr int RR = 32 * R / G;  // evaluation rounds of G edits
   const int gl = grp.gl;
-  FastSmem<R, G> &f = sm.f;
+  FastSmem<R, G, NP * G> &f = sm.f;
   const int nlat = fs[0], nchk = fs[1], nwr = fs[2];
   const uint32_t w3 = (uint32_t)fs[3];
   const int nedit = w3 & 0xFFFF, nq = (w3 >> 16) & 0xF;
@@ -320,7 +319,7 @@ __device__ int fast_step(WarpSmem<NP, R, G> &sm, const Hot &H, View &v, const in
     if (on && kind != E_ADD) {
       const int q = p - 1;
       const int rank = atomicAdd(&sm.ndel[q], 1);
-      if (rank < TAIL_MAX && q < TAIL_PROCS) {
+      if (rank < TAIL_MAX) {
         const int n0 = sm.ns[q];
         tslot[rr] = q * TAIL_MAX + rank;
         if (n0 - rank >= 1) tv[rr] = v.as1[(size_t)q * v.stride + n0 - rank];
