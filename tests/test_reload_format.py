@@ -2,6 +2,7 @@
 descriptors of base.mpy:528-575 on known values, and a write / read round trip of an
 oracle trajectory's state."""
 import numpy as np
+import pytest
 
 from conftest import fixture_model
 from kmos_gb300 import program as PG
@@ -44,3 +45,35 @@ def test_round_trip(tmp_path):
     for p in range(prog.nproc):
         np.testing.assert_array_equal(r["as1"][p + 1], ex["as1"][p][1:])
         np.testing.assert_array_equal(r["as2"][p + 1], ex["as2"][p][1:])
+
+
+def test_native_reader_takes_the_oracle_writers_file(tmp_path):
+    """The library's .reload reader (kmos_gb300/csrc/kmc_reload.h, shared by the lattice
+    and otf backends; kmc_reload_info needs no device) parses the oracle's independently
+    written file: nr_of_proc and volume, no system-size line (the reference's own files
+    have none), and the #gb300 system_size line when one is added; a file without the
+    counts, or with an unreadable count, is refused."""
+    from kmos_gb300 import engine as E
+    prog = PG.compile_model(fixture_model("CO_oxidation_Ruo2"), "local_smart")
+    o = O.Oracle(prog, (6, 5), seed=3, rng=O.RNG_PHILOX, traj=1)
+    o.set_rates(np.linspace(1.0, 50.0, prog.nproc))
+    o.update_accum_rate()
+    o.do_kmc_steps(500)
+    path = str(tmp_path / "t.reload")
+    RL.write_oracle_reload(path, o, walltime=0.5)
+    assert E.reload_info(path) == (prog.nproc, o.V, None)
+    text = open(path).read()
+    with open(path, "w") as f:
+        f.write("#gb300 system_size 6 5 1\n" + text)
+    assert E.reload_info(path) == (prog.nproc, o.V, [6, 5, 1])
+    bad = str(tmp_path / "bad.reload")
+    with open(bad, "w") as f:
+        f.write("\n".join(l for l in text.splitlines() if not l.strip().startswith("nr_of_proc")) + "\n")
+    with pytest.raises(E.KMCError):
+        E.reload_info(bad)
+    with open(bad, "w") as f:
+        f.write(text.replace("nr_of_proc", "nr_of_proc x", 1))
+    with pytest.raises(E.KMCError):
+        E.reload_info(bad)
+    with pytest.raises(E.KMCError):
+        E.reload_info(str(tmp_path / "missing.reload"))
