@@ -238,6 +238,30 @@ __device__ inline const int32_t *rate_code(const int32_t *prog, const Dev &d, in
   return b;
 }
 
+// gr_<p>(cell) evaluated: the bystander counts, then the rate program.  Out of line:
+// with rate tables it runs only for the processes that have none, and a single copy
+// keeps the step loop's code small.
+__device__ __noinline__ double rate_counted(const Dev *dp, const int32_t *prog, const int8_t *lat, Geometry g, int p,
+                                            int cx, int cy, int cz, int *err) {
+  const Dev &d = *dp;
+  const int32_t *r = prog + prog[d.off_rate + p - 1];
+  const int nb = r[0], nv = r[1];
+  int32_t nr[OTF_NRMAX];
+  for (int k = 0; k < nv; k++) nr[k] = 0;
+  const int32_t *b = r + 4;
+  for (int k = 0; k < nb; k++) {
+    const int sp = lat[g.site(cx, cy, cz, b[0]) - 1];
+    const int npairs = b[1];
+    for (int j = 0; j < npairs; j++)
+      if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
+    b += 2 + 2 * npairs;
+  }
+  int e = ST_OK;
+  const double rate = rate_program(d, b, p, nr, e);
+  *err = e;
+  return rate;
+}
+
 // gr_<p>(cell).  With rate tables: a process's rate depends only on its bystander counts
 // (rates and user parameters are fixed between launches), so the counts select an entry
 // of the process's table, which otf_table_kernel filled with rate_program's value for
@@ -264,19 +288,10 @@ __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
       return reinterpret_cast<const double *>(v.prog + d.tab_values)[idx];
     }
   }
-  const int32_t *r = v.prog + v.prog[d.off_rate + p - 1];
-  const int nb = r[0], nv = r[1];
-  int32_t nr[OTF_NRMAX];
-  for (int k = 0; k < nv; k++) nr[k] = 0;
-  const int32_t *b = r + 4;
-  for (int k = 0; k < nb; k++) {
-    const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
-    const int npairs = b[1];
-    for (int j = 0; j < npairs; j++)
-      if (sp == b[2 + 2 * j]) nr[b[3 + 2 * j]] += 1;
-    b += 2 + 2 * npairs;
-  }
-  return rate_program(d, b, p, nr, v.err);
+  int err = ST_OK;
+  const double rate = rate_counted(v.d, v.prog, v.lat, v.g, p, cx, cy, cz, &err);
+  if (err) v.err = err;
+  return rate;
 }
 
 // Fills the rate tables: thread e computes entry e -- the process whose table holds it,
