@@ -208,6 +208,16 @@ __device__ int replay_process(FastSmem<R, G, NP * G> &f, int32_t *ns, uint32_t (
   return ST_OK;
 }
 
+// The serial interpreter (run_stream) for the step kernel's steps without a fast stream,
+// out of line on a copy of the view: a single copy of its code away from the step loop,
+// and the caller's view stays in registers.  Returns the status.
+static __device__ __noinline__ int run_stream_copy(View v, int pos, int bx, int by, int bz) {
+  v.minp = v.P;
+  v.err = ST_OK;
+  run_stream(v, pos, bx, by, bz);
+  return v.err;
+}
+
 // One kMC step's run_proc_nr through the gather / evaluate / replay path.  All lanes of
 // the group call it and get the status.
 template <int NP, int R, int G>
@@ -643,12 +653,7 @@ __global__ void __launch_bounds__(512, 1) kmc_run_kernel(RunArgs a) {
       if (fs_off) {
         err = fast_step<NP, R, G>(sm, H, v, H.h + fs_off, bx, by, bz, grp);
       } else {
-        if (gl == 0) {
-          v.minp = P;
-          v.err = ST_OK;
-          run_stream(v, M.prog[M.off_proc + proc], bx, by, bz);
-          err = v.err;
-        }
+        if (gl == 0) err = run_stream_copy(v, M.prog[M.off_proc + proc], bx, by, bz);
         err = grp.shfl(err, 0);
         grp.sync();
         KMC_PHASE(sm, 9, grp);
