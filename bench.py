@@ -335,13 +335,25 @@ def run_reference(args, dist: Dist):
         dist.close()
         return
     start, length = timed_phase(args)
-    steps = args.cpu_steps or min(length, CPU_STEPS[args.config])
+    # K timed samples that tile the GPU's timed window of the same trajectories (sample j
+    # runs its part of the window after the steps before it, untimed), the value the
+    # aggregate rate over all of them -- the CPU's rate over the GPU's window; W warm-up
+    # samples before them
+    full = args.cpu_steps or min(length, CPU_STEPS[args.config])
+    k = max(1, args.steps)
+    per = max(1000, full // k)
     sides = [int(x) for x in args.sides.split(",")] if args.sides else None
     ntraj = args.ntraj or None
-    warm = [cpu_sample(args.config, start, steps, ntraj, sides) for _ in range(min(args.warmup, 1))]
-    vals = [cpu_sample(args.config, start, steps, ntraj, sides) for _ in range(max(1, min(args.steps, 3)))]
-    value = statistics.median(v[0] for v in vals)
-    cores, sample = vals[0][1], vals[0][2]
+    warm = [cpu_sample(args.config, start, max(1000, per // 10), ntraj, sides) for _ in range(args.warmup)]
+    vals, parts = [], []
+    for j in range(k):
+        n = per if j < k - 1 else max(1000, full - per * (k - 1))
+        vals.append(cpu_sample(args.config, start + j * per, n, ntraj, sides))
+        parts.append(n)
+    value = sum(parts) / sum(n / v[0] for n, v in zip(parts, vals))
+    cores = vals[0][1]
+    sample = ("%s, one process per core; %d samples tiling steps %d-%d of each trajectory (%d warm-up "
+              "samples first)" % (vals[0][2].split(", each")[0], k, start, start + sum(parts), len(warm)))
     from kmos_gb300 import configs
     wl = configs.build(args.config, n=1, steps=1)
     line = {
