@@ -31,6 +31,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -238,6 +239,14 @@ __device__ inline const int32_t *rate_code(const int32_t *prog, const Dev &d, in
   return b;
 }
 
+// A site of the event's neighbourhood: Geometry::site_near when every offset of the
+// program (an op's plus its bystanders') stays within one lattice period (NEAR, chosen on
+// the host), Geometry::site otherwise.
+template <bool NEAR>
+__device__ __forceinline__ int gsite(const Geometry &g, int bx, int by, int bz, int32_t w) {
+  return NEAR ? g.site_near(bx, by, bz, w) : g.site(bx, by, bz, w);
+}
+
 // gr_<p>(cell) evaluated: the bystander counts, then the rate program.  Out of line:
 // with rate tables it runs only for the processes that have none, and a single copy
 // keeps the step loop's code small.
@@ -268,6 +277,7 @@ __device__ __noinline__ double rate_counted(const Dev *dp, const int32_t *prog, 
 // those counts -- the same double the program gives here.  The table index is the counts
 // in mixed radix: each bystander matching a pair adds the stride of that pair's
 // variable.  Otherwise the counts are taken and the program run.
+template <bool NEAR = false>
 __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
   const Dev &d = *v.d;
   if (d.tab_on) {
@@ -279,7 +289,7 @@ __device__ double rate_of(View &v, int p, int cx, int cy, int cz) {
       const int32_t *b = m + 3 + nv;
       int idx = m[0];
       for (int k = 0; k < nb; k++) {
-        const int sp = v.lat[v.g.site(cx, cy, cz, b[0]) - 1];
+        const int sp = v.lat[gsite<NEAR>(v.g, cx, cy, cz, b[0]) - 1];
         const int npairs = b[1];
         for (int j = 0; j < npairs; j++)
           if (sp == b[2 + 2 * j]) idx += b[3 + 2 * j];
@@ -487,6 +497,7 @@ struct EventSmem {
 // was absent before the event is absent at its turn too and needs no rate.  A stream of
 // more than OTF_RATE_OPS ops is replayed by lane 0 alone, in program order, the ops past
 // the listed ones evaluated there.
+template <bool NEAR>
 __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane, bool keep_tot OTF_PH_PARAMS) {
   const int32_t *w = v.prog;
   int32_t *offs = es.off;
@@ -498,7 +509,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
       const int op = h & 0xFF, cnt = (h >> 8) & 0xFF;
       if (op == OP_END) break;
       if (op == OP_REPLACE) {
-        const int site = v.g.site(bx, by, bz, w[p + 1]);
+        const int site = gsite<NEAR>(v.g, bx, by, bz, w[p + 1]);
         if (!in_mask(v.lat[site - 1], w[p + 2])) { v.err = ST_SPECIES; break; }
         v.lat[site - 1] = (int8_t)w[p + 3];
         p += 4;
@@ -522,17 +533,17 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     const int p = offs[k];
     const uint32_t h = (uint32_t)w[p];
     const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
-    const int site = v.g.site(bx, by, bz, w[p + 1]);
+    const int site = gsite<NEAR>(v.g, bx, by, bz, w[p + 1]);
     const int m0 = v.as2[v.row(arg - 1) + site];
     bool ok = op == OP_ADD || (op == OP_UPDATE && m0 != 0);
     if (op == OP_ADD)
       for (int c = 0; c < cnt && ok; c++)
-        ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
+        ok = in_mask(v.lat[gsite<NEAR>(v.g, bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
     double rate = 0.0;
     if (ok) {
       int cx, cy, cz;
       v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
-      rate = rate_of(v, arg, cx, cy, cz);
+      rate = rate_of<NEAR>(v, arg, cx, cy, cz);
     }
     es.m0[k] = m0;
     es.rate[k] = rate;
@@ -568,7 +579,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
         if (!es.ok[k]) {  // absent before the event, present now
           int cx, cy, cz;
           v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
-          rate = rate_of(v, p0 + 1, cx, cy, cz);
+          rate = rate_of<NEAR>(v, p0 + 1, cx, cy, cz);
         }
         double *r = v.rm + v.row(p0);
         v.tot[p0] = __dsub_rn(__dadd_rn(v.tot[p0], rate), r[m]);
@@ -639,7 +650,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
               if (!es.ok[k]) {  // absent before the event, present now
                 int cx, cy, cz;
                 v.g.cell(bx, by, bz, w[es.off[k] + 1], cx, cy, cz);
-                rate = rate_of(v, q + 1, cx, cy, cz);
+                rate = rate_of<NEAR>(v, q + 1, cx, cy, cz);
               }
               if (keep_tot) tq = __dsub_rn(__dadd_rn(tq, rate), r[m]);
               r[m] = rate;
@@ -673,7 +684,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
     const int op = h & 0xFF, cnt = (h >> 8) & 0xFF, arg = (h >> 16) & 0xFFFF;
     if (op == OP_END) return;
     if (op == OP_REPLACE) { p += 4; continue; }
-    const int site = v.g.site(bx, by, bz, w[p + 1]);
+    const int site = gsite<NEAR>(v.g, bx, by, bz, w[p + 1]);
     const int p0 = arg - 1;
     const bool pre = k < nops && p0 < 64 && !((moved >> p0) & 1ull);
     const int m = pre ? es.m0[k] : v.as2[v.row(p0) + site];
@@ -695,10 +706,10 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
       if (!have) {
         ok = true;
         for (int c = 0; c < cnt && ok; c++)
-          ok = in_mask(v.lat[v.g.site(bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
+          ok = in_mask(v.lat[gsite<NEAR>(v.g, bx, by, bz, w[p + 2 + 2 * c]) - 1], w[p + 3 + 2 * c]);
         int cx, cy, cz;
         v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
-        rate = ok ? rate_of(v, arg, cx, cy, cz) : 0.0;
+        rate = ok ? rate_of<NEAR>(v, arg, cx, cy, cz) : 0.0;
       }
       if (ok) {
         add_at(v, arg, site, rate, m);
@@ -713,7 +724,7 @@ __device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int b
       if (!ok0) {  // not evaluated ahead (past the listed ops)
         int cx, cy, cz;
         v.g.cell(bx, by, bz, w[p + 1], cx, cy, cz);
-        rate = rate_of(v, arg, cx, cy, cz);
+        rate = rate_of<NEAR>(v, arg, cx, cy, cz);
       }
       double *r = v.rm + v.row(p0);
       v.tot[p0] = __dsub_rn(__dadd_rn(v.tot[p0], rate), r[m]);
@@ -829,6 +840,7 @@ __host__ __device__ inline size_t otf_dyn_bytes(int prog_len, int staged, int P)
 // (out[0..1]); 4 = run_proc_nr(out[0], out[1]) on `only`; 5 = initialize_state(layer = n);
 // 6 = recalculate_rates_matrix; 7 = touchup_cell of the n cells (x, y, z) in io, in
 // order, on `only`.
+template <bool NEAR>
 __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
   __shared__ Smem sm;
   extern __shared__ __align__(16) unsigned char dyn_s[];
@@ -869,7 +881,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
       for (int i = 1 + lane; i <= nn; i += 32) {
         int x, y, z, s;
         v.g.coords(v.as1[v.row(p0) + i], x, y, z, s);
-        v.rm[v.row(p0) + i] = rate_of(v, p0 + 1, x, y, z);
+        v.rm[v.row(p0) + i] = rate_of<NEAR>(v, p0 + 1, x, y, z);
       }
       if (lane == 0) v.dirty[p0] = 1;
     }
@@ -1000,7 +1012,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, 
     {
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_event(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane, step + 1 == n OTF_PH_ARGS);
+      run_event<NEAR>(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane, step + 1 == n OTF_PH_ARGS);
     }
     err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
@@ -1042,6 +1054,7 @@ struct kmc_otf {
   bool uni_ok = true;         // every entry of a constant-rate process holds the current rate
   bool uni_enabled = true;    // kmc_otf_set_constant_rate_sums
   int uni_rows = 0;           // constant-rate processes
+  bool near = false;          // every offset of the program within one lattice period
   Dev d{};
   std::vector<double> rates, userpar;
   double *d_rates = nullptr, *d_userpar = nullptr;
@@ -1161,6 +1174,42 @@ int validate_otf(const int32_t *w, int32_t len) {
   return KMC_OK;
 }
 
+// The largest |offset| per axis an event's site computations reach: an op's coordinate
+// plus, for the rates it evaluates, a bystander's (process streams and rate records).
+void otf_reach(const int32_t *w, int r[3]) {
+  const int P = w[3];
+  const int64_t off_proc = w[10], off_rate = w[22];
+  int op_r[3] = {0, 0, 0}, by_r[3] = {0, 0, 0};
+  auto take = [](int32_t c, int *m) {
+    const uint32_t u = (uint32_t)c;
+    const int d[3] = {(int8_t)(u & 0xFF), (int8_t)((u >> 8) & 0xFF), (int8_t)((u >> 16) & 0xFF)};
+    for (int a = 0; a < 3; a++) m[a] = std::max(m[a], std::abs(d[a]));
+  };
+  for (int p = 0; p < P; p++) {
+    for (int64_t pos = w[off_proc + p];;) {
+      const uint32_t h = (uint32_t)w[pos];
+      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF;
+      if (op == OP_END) break;
+      take(w[pos + 1], op_r);
+      if (op == OP_REPLACE) { pos += 4; continue; }
+      if (op == OP_ADD) {
+        for (int c = 0; c < cnt; c++) take(w[pos + 2 + 2 * c], op_r);
+        pos += 2 + 2 * cnt;
+        continue;
+      }
+      pos += 2;
+    }
+    const int64_t rr = w[off_rate + p];
+    const int nb = w[rr];
+    int64_t b = rr + 4;
+    for (int k = 0; k < nb; k++) {
+      take(w[b], by_r);
+      b += 2 + 2 * (int64_t)w[b + 1];
+    }
+  }
+  for (int a = 0; a < 3; a++) r[a] = op_r[a] + by_r[a];
+}
+
 constexpr int64_t OTF_TABLE_MAX = 4096;  // table entries of one model (32 KB of doubles)
 
 // Appends the rate-table records to a checked program: for each process whose counts
@@ -1240,12 +1289,14 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     d.accum += (size_t)only * d.P; d.tot += (size_t)only * d.P; d.procstat += (size_t)only * d.P;
     d.traj += only; d.T = 1;
   }
+  // site_near for programs whose every offset stays within one period of this lattice
+  const void *kfn = h->near ? (const void *)otfdev::otf_kernel<true> : (const void *)otfdev::otf_kernel<false>;
   // the image goes to every block's shared memory when it fits beside the static part
   // and the warps' accum_rates and totals
   size_t dyn = 0;
   {
     cudaFuncAttributes fa;
-    CK(cudaFuncGetAttributes(&fa, otfdev::otf_kernel));
+    CK(cudaFuncGetAttributes(&fa, kfn));
     int optin = 0, dev = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -1254,7 +1305,7 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
     dyn = otfdev::otf_dyn_bytes(d.prog_len, d.prog_staged, d.P);
     if ((int64_t)dyn > cap) return fail(KMC_ERR_ARG, "otf: too many processes for shared memory");
     if (fa.maxDynamicSharedSizeBytes < (int)dyn)
-      CK(cudaFuncSetAttribute(otfdev::otf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+      CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
   }
   if (h->tab_stale) {
     if (h->d.tab_entries > 0) {
@@ -1271,7 +1322,9 @@ int launch(kmc_otf *h, int cmd, int64_t n, int only, int32_t *d_io) {
   if (cmd == 6) h->uni_ok = true;
   d.uni_on = h->uni_enabled && h->uni_ok && d.uni_index >= 0 ? 1 : 0;
   CK(cudaEventRecord(h->ev0, h->stream));
-  otfdev::otf_kernel<<<blocks, 32 * otfdev::OTF_WARPS, dyn, h->stream>>>(d, cmd, n, only >= 0 ? 0 : -1, d_io);
+  int only_arg = only >= 0 ? 0 : -1;
+  void *args[] = {&d, &cmd, &n, &only_arg, &d_io};
+  CK(cudaLaunchKernel(kfn, dim3(blocks), dim3(32 * otfdev::OTF_WARPS), args, dyn, h->stream));
   CK(cudaGetLastError());
   CK(cudaEventRecord(h->ev1, h->stream));
   h->launches++;
@@ -1375,6 +1428,11 @@ int kmc_otf_create(const int32_t *program, int32_t len, const int32_t dims[3], i
   Dev &d = h->d;
   build_image(program, len, h->prog, d, h->uni_rows);
   const int32_t img_len = (int32_t)h->prog.size();
+  {
+    int reach[3];
+    otf_reach(program, reach);
+    h->near = reach[0] <= dims[0] && reach[1] <= dims[1] && reach[2] <= dims[2];
+  }
   d.P = P; d.nspecies = program[4]; d.null_species = program[5]; d.spuck = program[6];
   d.nuser = program[23]; d.off_proc = program[10]; d.off_touch = program[11]; d.off_rate = program[22];
   d.off_site_layer = program[13]; d.off_site_default = program[14];
