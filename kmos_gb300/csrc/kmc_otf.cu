@@ -18,7 +18,7 @@
 // left-to-right sums bit for bit, and pm is at once the accum_rates_proc array
 // determine_procsite (base_otf.f90:1213-1277) searches.
 //
-// One warp per trajectory, four per block; each block first copies the program to its
+// One warp per trajectory, eight per block; each block first copies the program to its
 // shared memory.  A step: lanes re-sum the stale lists (one process per lane, a serial
 // chain each), lane 0 chains the process totals into accum_rates, every lane advances
 // the clock and integ_rates of its processes, lane 0 picks the process and the entry
@@ -45,7 +45,7 @@ namespace otfdev {
 using namespace kmc;
 
 constexpr int OTF_PMAX = 256;
-constexpr int OTF_WARPS = 4;  // trajectories per block
+constexpr int OTF_WARPS = 8;  // trajectories per block (two blocks per SM at 128 registers)
 constexpr int OTF_NRMAX = 64;
 constexpr int OTF_STACK = 16;
 constexpr int OTF_AUX = 8;
@@ -826,8 +826,9 @@ struct Smem {
 
 // Dynamic shared memory of a block: the image (when staged; its size rounded to 16
 // bytes), then each warp's accum_rates (P + 1 doubles, 1-based) and process totals (P).
-// Sized by the model's P rather than OTF_PMAX, a block of intZGB takes 37 KB in all, so
-// four blocks leave most of the SM's on-chip memory to the L1 cache of the tables.
+// Sized by the model's P rather than OTF_PMAX, a block of eight intZGB trajectories takes
+// 54 KB in all, so the two blocks of an SM leave most of its on-chip memory to the L1
+// cache of the tables (and hold two copies of the image, not four as blocks of four).
 __host__ __device__ inline size_t otf_image_bytes(int prog_len, int staged) {
   return staged ? ((size_t)prog_len * 4 + 15) / 16 * 16 : 0;
 }
@@ -841,7 +842,7 @@ __host__ __device__ inline size_t otf_dyn_bytes(int prog_len, int staged, int P)
 // 6 = recalculate_rates_matrix; 7 = touchup_cell of the n cells (x, y, z) in io, in
 // order, on `only`.
 template <bool NEAR>
-__global__ void __launch_bounds__(32 * OTF_WARPS, 4) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
+__global__ void __launch_bounds__(32 * OTF_WARPS, 2) otf_kernel(Dev d, int cmd, int64_t n, int only, int32_t *io) {
   __shared__ Smem sm;
   extern __shared__ __align__(16) unsigned char dyn_s[];
   int32_t *prog_s = reinterpret_cast<int32_t *>(dyn_s);  // the image, when staged
