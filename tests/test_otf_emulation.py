@@ -180,3 +180,47 @@ def test_event_replay_and_running_sums(name, size, rates, params):
                 assert (pm[-1] if n else 0.0) == full[q]
             checked += 1
     assert checked == 60
+
+
+def test_constant_rate_running_sums_are_one_table():
+    """The identity behind the otf kernel's constant-rate sums (otf_uniform_kernel): for
+    every process whose rate program reads no bystander count, after
+    recalculate_rates_matrix and any number of steps every entry of its list holds the same
+    rate c, and the oracle's total of the list (update_accum_rate's left-to-right sum) is
+    F(n), F(i) = F(i-1) + c from F(0) = 0 -- the same for every trajectory.  Checked on the
+    oracle's intZGB trajectories, including through a rate change followed by
+    recalculate_rates_matrix."""
+    m = fixture_model("intZGB_otf")
+    prog = PG.compile_model(m, "otf")
+    w = np.asarray(prog.words)
+    off_rate = int(w[22])
+    const = [p for p in range(int(w[3])) if int(w[int(w[off_rate + p]) + 1]) == 0]
+    assert len(const) == 3   # CO and the two O2 desorption directions
+    rates = [0.4, 0.05, 0.1, 0.1, 0.1, 0.1, 0.02, 0.02, 0.3, 0.3]
+    params = [1.3, 0.7, 1.9, 1e-10, 0.5]
+    for traj in (0, 3):
+        o = O.Oracle(prog, (24, 20), seed=11, rng=O.RNG_PHILOX, traj=traj)
+        o.set_rates(rates)
+        o.set_user_parameters(params)
+        o.recalculate_rates_matrix()
+        o.update_accum_rate()
+        for block, change in ((3000, False), (2000, True), (2000, False)):
+            if change:
+                o.set_rates([r * 1.7 for r in rates])
+                o.recalculate_rates_matrix()
+            o.do_kmc_steps(block)
+            o.update_accum_rate()
+            rm, tot = o.rates_matrix()
+            ns = o.export()["nsites"]
+            for p in const:
+                n = int(ns[p])
+                row = rm[p, 1:n + 1]
+                if n == 0:
+                    assert tot[p] == 0.0
+                    continue
+                c = row[0]
+                assert (row == c).all()
+                f = 0.0
+                for _ in range(n):
+                    f = f + c
+                assert tot[p] == f
