@@ -18,15 +18,17 @@
 // left-to-right sums bit for bit, and pm is at once the accum_rates_proc array
 // determine_procsite (base_otf.f90:1213-1277) searches.
 //
-// One warp per trajectory, eight per block; each block first copies the program to its
-// shared memory.  A step: lanes re-sum the stale lists (one process per lane, a serial
-// chain each), lane 0 chains the process totals into accum_rates, every lane advances
-// the clock and integ_rates of its processes, lane 0 picks the process and the entry
-// (interval_search_real on accum_rates and on the chosen list's running sums), and the
-// event runs (run_event): lane 0 writes the lattice, the lanes load the table positions
-// and evaluate the add conditions and the rate programs (gr_<name>, io:2800-2965) in
-// parallel, then every lane replays the guarded dels, rate updates and adds of its own
-// processes in program order (ops of different processes touch different rows).
+// One warp per trajectory, eight per block; each block first copies the image -- the
+// program, then the rate tables -- to its shared memory.  A step: lanes re-sum the stale
+// lists (one process per lane, a serial chain each; a constant-rate process's sums come
+// from its one-table row instead), lane 0 chains the process totals into accum_rates,
+// every lane advances the clock and integ_rates of its processes, lane 0 picks the
+// process and the entry (interval_search_real on accum_rates and on the chosen list's
+// running sums), and the event runs (run_event): lane 0 writes the lattice, the lanes
+// load the table positions and evaluate the add conditions and the rates (gr_<name>,
+// io:2800-2965: a table lookup by bystander counts, or the rate program) in parallel,
+// then every lane replays the guarded dels, rate updates and adds of its own processes
+// in program order (ops of different processes touch different rows).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
