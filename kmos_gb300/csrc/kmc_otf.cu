@@ -86,6 +86,7 @@ struct Dev {
   int32_t uni_index;          // image word of the P constant-rate row numbers (-1: none)
   int32_t uni_on;             // 1: constant-rate processes' running sums come from usum
   double *usum;               // per constant-rate process: its running sums of 0..V entries
+  int32_t ev_index;           // image word of the P event records (built by build_image)
 };
 
 // Cycle accounting of the step loop (builds with -DKMC_PHASE_TIMING only): lane 0 adds
@@ -500,33 +501,28 @@ struct EventSmem {
 // more than OTF_RATE_OPS ops is replayed by lane 0 alone, in program order, the ops past
 // the listed ones evaluated there.
 template <bool NEAR>
-__device__ void run_event(View &v, EventSmem &es, int pos, int bx, int by, int bz, int lane, bool keep_tot OTF_PH_PARAMS) {
+__device__ void run_event(View &v, EventSmem &es, int proc0, int pos, int bx, int by, int bz, int lane,
+                          bool keep_tot OTF_PH_PARAMS) {
   const int32_t *w = v.prog;
   int32_t *offs = es.off;
-  int nops = 0;
-  bool over = false;
-  if (lane == 0) {
-    for (int p = pos;;) {
-      const uint32_t h = (uint32_t)w[p];
-      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF;
-      if (op == OP_END) break;
-      if (op == OP_REPLACE) {
+  int nops, ntab;
+  {
+    // the process's event record (built on the host): its replaces, applied by lane 0,
+    // and the offsets of its table ops, copied to offs by all lanes
+    const int32_t *rec = w + w[v.d->ev_index + proc0];
+    const int nrep = rec[0];
+    ntab = rec[1];
+    nops = min(ntab, OTF_RATE_OPS);
+    if (lane == 0)
+      for (int i = 0; i < nrep; i++) {
+        const int p = rec[2 + i];
         const int site = gsite<NEAR>(v.g, bx, by, bz, w[p + 1]);
         if (!in_mask(v.lat[site - 1], w[p + 2])) { v.err = ST_SPECIES; break; }
         v.lat[site - 1] = (int8_t)w[p + 3];
-        p += 4;
-      } else if (op == OP_ADD || op == OP_UPDATE || op == OP_GDEL) {
-        if (nops < OTF_RATE_OPS) offs[nops++] = p;
-        else over = true;
-        p += op == OP_ADD ? 2 + 2 * cnt : 2;
-      } else {
-        v.err = ST_PROGRAM;
-        break;
       }
-    }
+    for (int k = lane; k < nops; k += 32) offs[k] = rec[2 + nrep + k];
   }
-  nops = __shfl_sync(0xFFFFFFFFu, nops, 0);
-  over = __shfl_sync(0xFFFFFFFFu, over, 0);
+  const bool over = ntab > OTF_RATE_OPS;
   const int err0 = __shfl_sync(0xFFFFFFFFu, v.err, 0);
   __syncwarp();
   OTF_MARK(4);
@@ -1015,7 +1011,7 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 2) otf_kernel(Dev d, int cmd, 
     {
       int x, y, z, s;
       v.g.coords(site, x, y, z, s);
-      run_event<NEAR>(v, sm.ev[warp], v.prog[d.off_proc + proc - 1], x, y, z, lane, step + 1 == n OTF_PH_ARGS);
+      run_event<NEAR>(v, sm.ev[warp], proc - 1, v.prog[d.off_proc + proc - 1], x, y, z, lane, step + 1 == n OTF_PH_ARGS);
     }
     err = __shfl_sync(0xFFFFFFFFu, v.err, 0);
     __syncwarp();
@@ -1274,6 +1270,31 @@ void build_image(const int32_t *w, int32_t len, std::vector<int32_t> &img, Dev &
     if (w[w[off_rate + p] + 1] == 0) img[d.uni_index + p] = rows++;
   if (!rows) d.uni_index = -1;
   uni_rows = rows;
+  d.ev_index = (int32_t)img.size();
+  img.resize(img.size() + P, 0);
+  const int64_t off_proc = w[10];
+  for (int p = 0; p < P; p++) {
+    std::vector<int32_t> reps, tab;
+    int64_t ntab = 0;
+    for (int64_t pos = w[off_proc + p];;) {
+      const uint32_t h = (uint32_t)w[pos];
+      const int op = h & 0xFF, cnt = (h >> 8) & 0xFF;
+      if (op == OP_END) break;
+      if (op == OP_REPLACE) {
+        reps.push_back((int32_t)pos);
+        pos += 4;
+      } else {
+        if (ntab < otfdev::OTF_RATE_OPS) tab.push_back((int32_t)pos);
+        ntab++;
+        pos += op == OP_ADD ? 2 + 2 * cnt : 2;
+      }
+    }
+    img[d.ev_index + p] = (int32_t)img.size();
+    img.push_back((int32_t)reps.size());
+    img.push_back((int32_t)ntab);
+    img.insert(img.end(), reps.begin(), reps.end());
+    img.insert(img.end(), tab.begin(), tab.end());
+  }
   img.resize(align_up(img.size(), 4), 0);
   d.tab_values = (int32_t)img.size();
   img.resize(img.size() + 2 * (size_t)entries, 0);
