@@ -764,6 +764,41 @@ __device__ inline const double *sums_of(const View &v, int p0) {
   return v.pm + v.row(p0);
 }
 
+// interval_search with the whole warp, for arr[1..size] non-decreasing (running sums of
+// non-negative rates).  The bisection above returns the first index i with
+// value < arr[i], arr[size] never tested (as if true); here that index comes from a
+// 32-way search -- each round every lane tests one of 32 evenly spaced indices of the
+// remaining range and a ballot keeps the part holding the first true one -- and then the
+// same scans right past zeros and left over equal values, by every lane alike.
+__device__ int interval_search_warp(const double *arr, int size, double value, int lane) {
+  int lo = 1, hi = size;  // the answer lies in [lo, hi]; the test at hi is true
+  while (lo < hi) {
+    const int step = (hi - lo + 32) >> 5;  // ceil((hi - lo + 1) / 32)
+    const int p = lo + lane * step;
+    const bool t = p >= hi || value < arr[p];
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, t);
+    if (!b) {
+      lo += 31 * step + 1;  // every tested index false: the answer is past the last
+      continue;
+    }
+    const int j = __ffs(b) - 1;
+    if (j == 0) { hi = lo; break; }
+    const int pj = lo + j * step;
+    lo = lo + (j - 1) * step + 1;
+    hi = pj < hi ? pj : hi;
+  }
+  int mid = lo;
+  if (arr[mid] == 0.0) {
+    for (;;) {
+      if (arr[mid] > 0.0) break;
+      if (mid >= size) return 0;
+      mid = mid + 1;
+    }
+  }
+  while (mid != 1 && arr[mid - 1] >= arr[mid]) mid = mid - 1;
+  return mid;
+}
+
 // update_accum_rate: stale running sums re-summed (lanes: processes), then the totals
 // chained into accum_rates on lane 0.  sacc is the warp's accum_rates (1-based).  A
 // constant-rate process's total is read from its usum row; its pm row is left stale,
@@ -985,27 +1020,25 @@ __global__ void __launch_bounds__(32 * OTF_WARPS, 2) otf_kernel(Dev d, int cmd, 
     for (int p0 = lane; p0 < P; p0 += 32)
       v.integ[p0] = __dadd_rn(v.integ[p0], __dmul_rn(stot[p0], tr.kmc_time_step));
     OTF_MARK(2);
-    int err = 0, proc = 0, site = 0;
-    if (lane == 0) {
-      proc = interval_search(sacc, P, __dmul_rn(r1, total));
-      const int nn = proc ? v.ns[proc - 1] : 0;
-      if (!proc || nn <= 0) {
+    // determine_procsite: the process on lane 0 (accum_rates in shared memory), the entry
+    // with the whole warp (the list's running sums in device memory)
+    int proc = 0, site = 0;
+    if (lane == 0) proc = interval_search(sacc, P, __dmul_rn(r1, total));
+    proc = __shfl_sync(0xFFFFFFFFu, proc, 0);
+    const int nn = proc ? v.ns[proc - 1] : 0;
+    int err = !proc || nn <= 0 ? ST_DEADLOCK : ST_OK;
+    if (!err) {
+      const double *pm = sums_of(v, proc - 1);
+      const int k = interval_search_warp(pm, nn, __dmul_rn(r2, pm[nn]), lane);
+      if (!k) {
         err = ST_DEADLOCK;
-      } else {
-        const double *pm = sums_of(v, proc - 1);
-        const int k = interval_search(pm, nn, __dmul_rn(r2, pm[nn]));
-        if (!k) {
-          err = ST_DEADLOCK;
-        } else {
-          site = v.as1[v.row(proc - 1) + k];
-          if (io) { io[2 * step] = proc; io[2 * step + 1] = site; }
-          v.procstat[proc - 1] += 1;
-        }
+      } else if (lane == 0) {
+        site = v.as1[v.row(proc - 1) + k];
+        if (io) { io[2 * step] = proc; io[2 * step + 1] = site; }
+        v.procstat[proc - 1] += 1;
       }
     }
-    err = __shfl_sync(0xFFFFFFFFu, err, 0);
     if (err) { tr.status = err; break; }
-    proc = __shfl_sync(0xFFFFFFFFu, proc, 0);
     site = __shfl_sync(0xFFFFFFFFu, site, 0);
     OTF_MARK(3);
     {

@@ -224,3 +224,79 @@ def test_constant_rate_running_sums_are_one_table():
                 for _ in range(n):
                     f = f + c
                 assert tot[p] == f
+
+
+def _bisect(arr, size, value):
+    """interval_search_real as kmc_otf.cu's interval_search runs it (lane 0)."""
+    left, right = 1, size
+    while True:
+        mid = (right + left) >> 1
+        if left >= right:
+            break
+        if value < arr[mid]:
+            right = mid
+        else:
+            left = mid + 1
+    if arr[mid] == 0.0:
+        while True:
+            if arr[mid] > 0.0:
+                break
+            if mid >= size:
+                return 0
+            mid += 1
+    while mid != 1 and arr[mid - 1] >= arr[mid]:
+        mid -= 1
+    return mid
+
+
+def _warp_search(arr, size, value):
+    """kmc_otf.cu's interval_search_warp, the 32 lanes emulated."""
+    lo, hi = 1, size
+    while lo < hi:
+        step = (hi - lo + 32) >> 5
+        t = [(lo + lane * step >= hi) or (value < arr[lo + lane * step]) for lane in range(32)]
+        if not any(t):
+            lo += 31 * step + 1
+            continue
+        j = t.index(True)
+        if j == 0:
+            hi = lo
+            break
+        pj = lo + j * step
+        lo = lo + (j - 1) * step + 1
+        hi = min(pj, hi)
+    mid = lo
+    if arr[mid] == 0.0:
+        while True:
+            if arr[mid] > 0.0:
+                break
+            if mid >= size:
+                return 0
+            mid += 1
+    while mid != 1 and arr[mid - 1] >= arr[mid]:
+        mid -= 1
+    return mid
+
+
+def test_warp_entry_search_equals_the_bisection():
+    """The otf kernel's warp-parallel entry search returns the bisection's index on running
+    sums of non-negative rates: random lists of every size class around the 32-way round
+    boundaries, with zeros, plateaus, one positive entry, constant rates, and values at 0,
+    inside, at and past the total."""
+    rng = np.random.default_rng(1)
+    for _ in range(3000):
+        size = int(rng.choice([1, 2, 3, 31, 32, 33, 63, 64, 65, 1023, 1024, 1025, 1057, 5000]))
+        kind = int(rng.integers(0, 4))
+        if kind == 0:
+            r = rng.uniform(0, 1, size)
+        elif kind == 1:
+            r = rng.choice([0.0, 0.5, 1.0], size)
+        elif kind == 2:
+            r = np.zeros(size)
+            r[rng.integers(0, size)] = 1.0
+        else:
+            r = np.full(size, 0.02)
+        arr = np.concatenate([[0.0], np.cumsum(r)])
+        tot = arr[size]
+        for value in (rng.uniform(0, tot) if tot > 0 else 0.0, 0.0, tot, rng.uniform(0, 2 * tot + 1)):
+            assert _warp_search(arr, size, value) == _bisect(arr, size, value)
