@@ -396,14 +396,14 @@ KMC_API int kmc_otf_set_state(kmc_otf *h, int32_t traj, const int32_t *lattice, 
  * rate constants from the file; walltime: the file's (may be NULL). */
 KMC_API int kmc_otf_save_reload(kmc_otf *h, int32_t traj, const char *path, double walltime);
 KMC_API int kmc_otf_load_reload(kmc_otf *h, int32_t traj, const char *path, double *walltime);
-/* The batch's rate constants (base.rates), P values. */
+/* The batch's rate constants (base.rates, base_otf.f90:152, set by set_rate_const,
+ * base_otf.f90:665-685), P values. */
 KMC_API int kmc_otf_get_rate_consts(kmc_otf *h, double *rates);
 /* Rate tables (no reference counterpart; results are the same either way): a process's
  * rate depends only on its bystander counts, so for models whose counts take at most
  * 4096 combinations in all, each combination's rate is computed once by the process's
  * rate program after the rates or user parameters change, and steps look it up.  on = 0
- * evaluates every rate (gr_<name>, io:2800-2965) instead.  entries: the table size (0:
- * the model has none). */
+ * evaluates every rate (gr_<name>, io:2800-2965) instead. */
 KMC_API int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on);
 /* Constant-rate running sums (no reference counterpart; results are the same either
  * way): every entry of a process whose rate program reads no bystander count holds the
@@ -413,6 +413,8 @@ KMC_API int kmc_otf_set_rate_tables(kmc_otf *h, int32_t on);
  * list.  Used between recalculate_rates_matrix and the next rate or parameter change,
  * for lattices of up to 65536 sites; on = 0 always sums the lists. */
 KMC_API int kmc_otf_set_constant_rate_sums(kmc_otf *h, int32_t on);
+/* entries: the rate tables' size in values, whether or not they are in use (0: the model
+ * has none). */
 KMC_API int kmc_otf_rate_table_entries(kmc_otf *h, int32_t *entries);
 /* Device time of the last launch (CUDA events on the handle's stream) and launch count. */
 KMC_API int kmc_otf_last_kernel_ms(kmc_otf *h, float *ms);
