@@ -83,7 +83,7 @@ KMC_API int kmc_check_program(const int32_t *program, int32_t program_len);
  * KMC_RNG_GFORTRAN).  The initial state is built on the device. */
 KMC_API int kmc_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer,
                int32_t seed, int32_t rng_kind, uint32_t traj_id, kmc_handle **out);
-/* lattice.deallocate_system (lattice.mpy) */
+/* lattice.deallocate_system (lattice.mpy:324-340, base.mpy:753) */
 KMC_API int kmc_destroy(kmc_handle *h);
 
 /* base.set_rate_const(proc, rate) (base.mpy:581-601); proc is 1-based. */
@@ -121,17 +121,18 @@ KMC_API int kmc_get_kmc_time(kmc_handle *h, double *t);
 KMC_API int kmc_set_kmc_time(kmc_handle *h, double t);
 KMC_API int kmc_get_kmc_time_step(kmc_handle *h, double *dt);
 KMC_API int kmc_get_kmc_step(kmc_handle *h, int64_t *step);
-/* base.get_volume, nr_of_proc */
+/* base.get_volume (base.mpy:1042), base.nr_of_proc (base.mpy:189) */
 KMC_API int kmc_get_volume(kmc_handle *h, int32_t *volume);
 KMC_API int kmc_get_nr_of_proc(kmc_handle *h, int32_t *nproc);
 /* Whole P-vectors: base.get_procstat(i), get_integ_rate(i), get_rate(i),
- * get_accum_rate(i), get_nrofsites(i) for i = 1..P, copied into host arrays. */
+ * get_accum_rate(i), get_nrofsites(i) for i = 1..P (base.mpy:888, 968, 991, 945, 907),
+ * copied into host arrays. */
 KMC_API int kmc_get_procstat(kmc_handle *h, int64_t *out);
 KMC_API int kmc_get_integ_rates(kmc_handle *h, double *out);
 KMC_API int kmc_get_rates(kmc_handle *h, double *out);
 KMC_API int kmc_get_accum_rates(kmc_handle *h, double *out);
 KMC_API int kmc_get_nr_of_sites(kmc_handle *h, int32_t *out);
-/* base.get_avail_site(proc, idx, sw) (avail_sites(proc, idx, sw), base.mpy) */
+/* base.get_avail_site(proc, idx, sw) (avail_sites(proc, idx, sw), base.mpy:925-942) */
 KMC_API int kmc_get_avail_site(kmc_handle *h, int32_t proc, int32_t idx, int32_t sw, int32_t *out);
 /* The whole lattice (V species ids) and both book-keeping tables in the engine's
  * per-process layout: as1[p][i] = avail_sites(p+1, i, 1), as2[p][s] = avail_sites(p+1, s, 2)
@@ -344,24 +345,29 @@ typedef struct kmc_otf kmc_otf;
 
 /* The checks kmc_otf_create makes on an otf program (no device needed). */
 KMC_API int kmc_otf_check_program(const int32_t *program, int32_t program_len);
-/* allocate_system + initialize_state(layer) (cell touch-ups) for ntraj trajectories. */
+/* proclist.init for ntraj trajectories: base.allocate_system (base_otf.f90:741-865) +
+ * initialize_state(layer) (proclist_generic_subroutines.mpy:166-304, the cell touch-ups);
+ * kmc_otf_destroy is deallocate_system (base_otf.f90:874-932). */
 KMC_API int kmc_otf_create(const int32_t *program, int32_t program_len, const int32_t dims[3], int32_t layer,
                            int32_t ntraj, int32_t seed, int32_t rng_kind, uint32_t traj0, kmc_otf **out);
 KMC_API int kmc_otf_destroy(kmc_otf *h);
 /* base.set_rate_const (base_otf.f90:665-685) */
 KMC_API int kmc_otf_set_rate_const(kmc_otf *h, int32_t proc, double rate);
-/* proclist_pars.update_user_parameter: k = 1.. in sorted parameter-name order */
+/* proclist_pars.update_user_parameter (kmos/io/__init__.py:2756-2765): k = 1.. in sorted
+ * parameter-name order */
 KMC_API int kmc_otf_set_user_parameter(kmc_otf *h, int32_t k, double value);
 /* proclist.recalculate_rates_matrix + reaccumulate_rates_matrix (proclist_generic_subroutines.mpy:307-325) */
 KMC_API int kmc_otf_recalculate_rates_matrix(kmc_otf *h);
 /* base.update_accum_rate (base_otf.f90:687-716) / update_integ_rate (719-738) */
 KMC_API int kmc_otf_update_accum_rate(kmc_otf *h);
 KMC_API int kmc_otf_update_integ_rate(kmc_otf *h);
-/* proclist.do_kmc_steps(n) on every trajectory, one launch */
+/* proclist.do_kmc_steps(n) (proclist_generic_subroutines.mpy:1-44) on every trajectory,
+ * one launch */
 KMC_API int kmc_otf_do_steps(kmc_otf *h, int64_t n);
 /* n steps of trajectory traj alone, its (proc, site) pairs to out[2n] */
 KMC_API int kmc_otf_trace_steps(kmc_otf *h, int32_t traj, int64_t n, int32_t *out);
-/* proclist.get_next_kmc_step / run_proc_nr of one trajectory */
+/* proclist.get_next_kmc_step (proclist_generic_subroutines.mpy:85-110) / run_proc_nr
+ * (kmos/io/__init__.py:3292-3326) of one trajectory */
 KMC_API int kmc_otf_get_next_step(kmc_otf *h, int32_t traj, int32_t *proc, int32_t *site);
 KMC_API int kmc_otf_run_proc_nr(kmc_otf *h, int32_t traj, int32_t proc, int32_t site);
 /* State of one trajectory (NULL skips a field): lattice[V], avail_sites as1/as2[P][V+1],
