@@ -113,7 +113,9 @@ KMC_API int kmc_touchup(kmc_handle *h, int32_t site);
 KMC_API int kmc_touchup_many(kmc_handle *h, const int32_t *sites, int32_t n);
 /* base.get_species(site) (base.mpy:1164-1184) */
 KMC_API int kmc_get_species(kmc_handle *h, int32_t site, int32_t *species);
-/* base.replace_species(site, old, new) (base.mpy:1187-1231) */
+/* base.replace_species(site, old, new) (base.mpy:1187-1231): KMC_ERR_SPECIES unless the
+ * site holds old; KMC_ERR_ARG for a new species outside -1..nspecies (the reference does
+ * not check it). */
 KMC_API int kmc_replace_species(kmc_handle *h, int32_t site, int32_t old_species, int32_t new_species);
 
 /* base.get_kmc_time / set_kmc_time / get_kmc_time_step / get_kmc_step (base.mpy:854-1072) */

@@ -1626,6 +1626,9 @@ int kmc_touchup_many(kmc_handle *h, const int32_t *sites, int32_t n) {
 int kmc_replace_species(kmc_handle *h, int32_t site, int32_t old_species, int32_t new_species) {
   HCHECK(h);
   if (site < 1 || site > h->V) return fail(KMC_ERR_ARG, "site out of range");
+  // the species a lattice can hold: 0..nspecies-1 and null_species (-1 or nspecies), the
+  // range state images and .reload files are checked against
+  if (new_species < -1 || new_species > h->nspecies) return fail(KMC_ERR_ARG, "unknown species");
   return run_command(h->pool, h->slot, CMD_REPLACE, site, old_species, new_species, nullptr, nullptr, nullptr);
 }
 

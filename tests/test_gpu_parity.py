@@ -338,6 +338,29 @@ def test_launch_shape_and_table_placement_do_not_change_results(config):
             assert ca == cb
 
 
+@pytest.mark.parametrize("backend", ["local_smart", "lat_int"])
+def test_replace_species_range(backend):
+    """replace_species refuses a new species outside -1..nspecies (the range state images
+    and .reload files are checked against) and leaves the site as it was; the wrong old
+    species is KMC_ERR_SPECIES as in the reference's stop."""
+    m = fixture_model("ZGB_model")
+    prog = PG.compile_model(m, backend)
+    t = E.Trajectory(prog, (6, 6), seed=3)
+    cur = t.get_species(1)
+    ns = len(m.species)
+    for bad in (ns + 1, -2, 127):
+        with pytest.raises(E.KMCError) as e:
+            t.replace_species(1, cur, bad)
+        assert e.value.code == 1
+        assert t.get_species(1) == cur
+    with pytest.raises(E.KMCError) as e:
+        t.replace_species(1, (cur + 1) % ns, cur)
+    assert e.value.code == 2
+    new = (cur + 1) % ns
+    t.replace_species(1, cur, new)
+    assert t.get_species(1) == new
+
+
 def test_run_list_checks():
     """A slot listed twice in one run, and negative rate offsets, are refused before any
     launch."""
