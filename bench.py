@@ -74,6 +74,9 @@ def parse():
                     help="run only the otf sample (--otf-ntraj trajectories, --otf-steps timed steps) and print it")
     ap.add_argument("--otf-ntraj", type=int, default=2048)
     ap.add_argument("--otf-steps", type=int, default=0, help="timed otf steps per trajectory (0: OTF_TIMED)")
+    ap.add_argument("--otf-phases", type=int, default=0,
+                    help="with --otf-only: run the phase-timing build and add the step loop's cycles per step "
+                         "by phase (that build's timing is not a bench figure)")
     ap.add_argument("--serving", type=int, default=1,
                     help="also run a short serving sample (configuration 5 stream, 1 s of arrivals, steps x 0.05)")
     return ap.parse_args()
@@ -579,7 +582,11 @@ def serving_sample():
     return out
 
 
-def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
+OTF_PHASES = ["draws", "running sums and accum_rates", "clock and integ_rates", "pick", "event op list",
+              "event evaluation", "event replay"]
+
+
+def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0, phases: bool = False):
     """The otf backend (per-entry rates from bystanders) after the timed region: intZGB
     (tests/golden/models/intZGB_otf.json, the reference's tests/export_test/intZGB_otf.xml)
     on a 32 x 32 lattice, 2048 Philox trajectories from an empty lattice: OTF_WARM
@@ -598,11 +605,18 @@ def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
     b.update_accum_rate()
     b.do_kmc_steps(OTF_WARM)                  # untimed: the lattice fills from empty
     steps = fixed_steps or OTF_TIMED
+    if phases:
+        b.phase_cycles(reset=True)
     b.do_kmc_steps(steps)
     ms = b.last_kernel_ms()
     out = {"workload": "intZGB otf, 32x32, %d trajectories" % ntraj, "window": [OTF_WARM, OTF_WARM + steps],
            "steps_per_traj": steps, "kernel_ms": ms, "steps_per_s": ntraj * steps / (ms * 1e-3), "gpu_launches": 1,
            "rate_table_entries": b.rate_table_entries()}
+    if phases:  # cycles of one trajectory's step, by phase (clock64 on lane 0, summed over warps)
+        cyc = b.phase_cycles(reset=True)[:len(OTF_PHASES)].astype(float) / (ntraj * steps)
+        out["build"] = "phase timing (KMC_PHASE_TIMING): slower than the product build"
+        out["cycles_per_step"] = {n: round(float(c), 1) for n, c in zip(OTF_PHASES, cyc)}
+        out["cycles_per_step_total"] = round(float(cyc.sum()), 1)
     b.close()
     if cpu:
         value, cores, sample = otf_cpu_sample(OTF_WARM, steps)
@@ -613,8 +627,13 @@ def otf_sample(cpu: int = 1, ntraj: int = 2048, fixed_steps: int = 0):
 
 def main():
     args = parse()
+    if args.otf_phases and not args.otf_only:
+        raise SystemExit("--otf-phases needs --otf-only 1")
     if args.otf_only:
-        print(json.dumps(otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps)))
+        if args.otf_phases:
+            from kmos_gb300 import build as _build
+            os.environ["KMC_GB300_LIB"] = _build.build(phase_timing=True)
+        print(json.dumps(otf_sample(args.cpu_baseline, args.otf_ntraj, args.otf_steps, bool(args.otf_phases))))
         return
     dist = Dist()
     if args.impl == "reference":
