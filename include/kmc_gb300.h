@@ -299,6 +299,14 @@ KMC_API int kmc_save_reload(kmc_handle *h, const char *path);
 /* First pass of base.reload_system (base.mpy:363-440): nr_of_proc, volume and, from a
  * "#gb300 system_size" line, the system size (zeros when the file has none). */
 KMC_API int kmc_reload_info(const char *path, int32_t *nr_of_proc, int32_t *volume, int32_t dims[3]);
+/* Checks a .reload file against a model program (lattice or otf) and a system size
+ * without a device: the checks kmc_load_reload / kmc_otf_load_reload make before anything
+ * reaches the GPU (the counts, every vector's length, species in -1..nspecies, each
+ * process's avail_sites columns inverse to each other over its nr_of_sites entries, a
+ * known random stream).  No reference counterpart (base.mpy:363-578 reads without
+ * checks).  KMC_OK, KMC_ERR_PROGRAM (bad program), KMC_ERR_ARG or KMC_ERR_TABLE (bad
+ * file). */
+KMC_API int kmc_check_reload(const int32_t *program, int32_t program_len, const int32_t dims[3], const char *path);
 /* Second pass of base.reload_system (base.mpy:442-486) into an allocated handle of the
  * same model and volume: kmc_time, walltime, kmc_step, lattice, nr_of_sites, rates,
  * procstat, avail_sites and avail_sites_back, checked for consistency (KMC_ERR_TABLE).

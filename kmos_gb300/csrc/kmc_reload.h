@@ -169,21 +169,24 @@ inline int parse_reload(const char *path, ReloadFile &r, bool header_only) {
       else if (k == "kmc_time_step" && tok.size() == 3) r.have_dt = parse_real(tok[2], &r.x_dt);
       else if (k == "rates") r.exact_rates = reals(tok, 2, r.x_rates);
       else if (k == "integ_rates") r.exact_integ = reals(tok, 2, r.x_integ);
-      else if (k == "rng" && tok.size() == 9) {
+      else if (k == "rng") {
+        // kind, seed, trajectory id, four state words; a line that is there but does not
+        // read is refused rather than skipped (the trajectory would keep another stream)
         int64_t kind, seed, traj;
-        bool ok = parse_int(tok[2], &kind) && parse_int(tok[3], &seed) && parse_int(tok[4], &traj);
+        bool ok = tok.size() == 9 && parse_int(tok[2], &kind) && parse_int(tok[3], &seed) &&
+                  parse_int(tok[4], &traj) && seed >= 0 && seed <= 0xFFFFFFFFll && traj >= 0 &&
+                  traj <= 0xFFFFFFFFll;
         for (int i = 0; i < 4 && ok; i++) {
           errno = 0;
           char *end = nullptr;
           r.rng[i] = strtoull(tok[5 + i].c_str(), &end, 10);
-          ok = end && *end == 0 && !errno;
+          ok = end != tok[5 + i].c_str() && *end == 0 && !errno && tok[5 + i][0] != '-';
         }
-        if (ok) {
-          r.have_rng = true;
-          r.rng_kind = (int32_t)kind;
-          r.seed = (uint32_t)seed;
-          r.traj = (uint32_t)traj;
-        }
+        if (!ok) { bad("#gb300 rng"); break; }
+        r.have_rng = true;
+        r.rng_kind = kind >= 0 && kind <= 1 ? (int32_t)kind : -1;  // -1: refused by read_reload
+        r.seed = (uint32_t)seed;
+        r.traj = (uint32_t)traj;
       }
       continue;
     }
@@ -292,8 +295,8 @@ inline int write_reload(const char *path, const ReloadData &d) {
 
 // The second pass of reload_system into a model of P processes on V sites: every vector
 // present with its length, species in -1..nspecies, and each process's two avail_sites
-// columns inverse to each other over its first nr_of_sites entries (zero past them).
-// Fills d's vectors (as1 entries per process; rates and integ_rates exact where the
+// columns inverse to each other over its first nr_of_sites entries (zero past them), a
+// "#gb300 rng" line of a known stream.  Fills d's vectors (as1 entries per process; rates and integ_rates exact where the
 // file's "#gb300" lines hold them, integ_rates 0 otherwise) and scalars.
 inline int read_reload(const ReloadFile &r, int P, int V, int nspecies, ReloadData &d) {
   if (!r.have_proc || r.nr_of_proc != P) return fail(KMC_ERR_ARG, "reload file: nr_of_proc differs from the model");
@@ -343,6 +346,12 @@ inline int read_reload(const ReloadFile &r, int P, int V, int nspecies, ReloadDa
   d.walltime = r.have_walltime ? r.walltime : 0.0;
   for (int i = 0; i < 3; i++) d.dims[i] = r.dims[i];
   if (r.have_rng) {
+    // the "#gb300 rng" line: a known stream, and for the gfortran one a xoshiro256**
+    // state that is not all zero (that state only ever yields zero)
+    if (r.rng_kind != kmc::RNG_GFORTRAN && r.rng_kind != kmc::RNG_PHILOX)
+      return fail(KMC_ERR_ARG, "reload file: unknown random stream");
+    if (r.rng_kind == kmc::RNG_GFORTRAN && !(r.rng[0] | r.rng[1] | r.rng[2] | r.rng[3]))
+      return fail(KMC_ERR_ARG, "reload file: all-zero gfortran random state");
     d.rng_kind = r.rng_kind;
     d.seed = r.seed;
     d.traj = r.traj;

@@ -567,6 +567,29 @@ int kmc_reload_info(const char *path, int32_t *nr_of_proc, int32_t *volume, int3
   return KMC_OK;
 }
 
+int kmc_check_reload(const int32_t *program, int32_t program_len, const int32_t dims[3], const char *path) {
+  if (!program || program_len < 7 || !dims || !path) return fail(KMC_ERR_ARG, "bad arguments");
+  int P = 0, nspecies = 0, spuck = 0;
+  if (program[2] == 2) {  // otf program: the checks kmc_otf_create makes
+    int rc = kmc_otf_check_program(program, program_len);
+    if (rc) return rc;
+    P = program[3]; nspecies = program[4]; spuck = program[6];
+  } else {
+    ModelDev md{};
+    int rc = validate_program(program, program_len, &md);
+    if (rc) return rc;
+    P = md.P; nspecies = md.nspecies; spuck = md.spuck;
+  }
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(KMC_ERR_ARG, "bad system size");
+  const int64_t V = (int64_t)dims[0] * dims[1] * dims[2] * spuck;
+  if (V > (program[2] == 2 ? (1 << 24) : (1 << 28))) return fail(KMC_ERR_ARG, "lattice too large");
+  kmc_reload::ReloadFile r;
+  int rc = kmc_reload::parse_reload(path, r, false);
+  if (rc) return rc;
+  kmc_reload::ReloadData d;
+  return kmc_reload::read_reload(r, P, (int)V, nspecies, d);
+}
+
 int kmc_load_reload(kmc_handle *h, const char *path) {
   if (!h || !h->pool || !path) return fail(KMC_ERR_ARG, "bad arguments");
   kmc_pool *p = h->pool;

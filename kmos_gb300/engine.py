@@ -107,6 +107,7 @@ SIGNATURES = {
     "kmc_load_state": (_i32, [_vp, _vp, _sz]),
     "kmc_save_reload": (_i32, [_vp, ctypes.c_char_p]),
     "kmc_reload_info": (_i32, [ctypes.c_char_p, _p32, _p32, _p32]),
+    "kmc_check_reload": (_i32, [_p32, _i32, _p32, ctypes.c_char_p]),
     "kmc_load_reload": (_i32, [_vp, ctypes.c_char_p]),
     "kmc_get_walltime": (_i32, [_vp, _pd]),
     "kmc_pool_sample_begin": (_i32, [_vp, _p32, _i32]),
@@ -389,6 +390,15 @@ def reload_info(path: str):
     dims = np.zeros(3, np.int32)
     _check(load().kmc_reload_info(os.fsencode(path), ctypes.byref(P), ctypes.byref(V), _ptr(dims, _i32)))
     return P.value, V.value, (None if dims[0] == 0 else [int(d) for d in dims])
+
+
+def check_reload(program, size, path: str) -> None:
+    """Raises KMCError unless the .reload file at ``path`` would be accepted for
+    ``program`` (lattice or otf) on a lattice of ``size`` (``kmc_check_reload``; no GPU
+    needed)."""
+    words = np.ascontiguousarray(getattr(program, "words", program), dtype=np.int32)
+    dims = _dims3(size)
+    _check(load().kmc_check_reload(_ptr(words, _i32), len(words), _ptr(dims, _i32), os.fsencode(path)))
 
 
 class Pool:
